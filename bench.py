@@ -1,0 +1,301 @@
+"""Benchmark of the photon-propagation hot path on one GB300 (or N replicas).
+
+Workload (one step): the cascade_string workload of
+neutrinotelescopes_gb300.workloads -- 4 electromagnetic cascades with
+energies log-uniform in 1e3-1e5 GeV (fixed by seed, 7.5e9 photons in total),
+1.3e5 photons/GeV, gamma longitudinal profile, on a string of 20 POM modules
+15 m apart, in water with n = 1.35, group index 1.39, absorption 30 m at
+400 nm, scattering 50 m, 0.85 HG(0.97) + 0.15 Rayleigh.  Every step draws a
+new Philox key, so each step simulates different photons.
+
+Metric: photons/s (whole job).  Timed on the device with CUDA events per
+step; the L2 is flushed (a 512 MB write) between steps, outside the events.
+e2e: the same metric through the public call propagate_photons(), host
+buffers and all copies included, timed on the host.
+"""
+from __future__ import annotations
+
+import argparse
+import ctypes as C
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+from pathlib import Path
+
+ROOT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT))
+
+N_CASCADES = 4
+WORKLOAD_SEED = 1
+METRIC = "photons/s"
+# Algorithmic lane-operations per photon-step (one scatter segment): one
+# Philox4x32-10 block (10 rounds x 6 integer ops + 10 for counter / uniform
+# conversion), about 50 FP32 operations for the step length, phase function,
+# rotation and position / time update, 5 special-function operations (log,
+# sin, cos, sqrt, reciprocal), and 12 FP32 operations per sphere tested.
+OPS_BASE = 70 + 50 + 5
+OPS_PER_TARGET = 12
+
+
+def algo_ops_per_step(n_targets: int) -> int:
+    return OPS_BASE + OPS_PER_TARGET * n_targets
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    ap.add_argument("--cpu-seconds", type=float, default=10.0, help="target length of the CPU baseline sample")
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--e2e-steps", type=int, default=3)
+    return ap.parse_args()
+
+
+class ClockSampler:
+    """nvidia-smi clock / throttle sampling during the timed region."""
+
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
+         "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+         "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index: int):
+        self.index = index
+        self.proc = None
+        self.path = None
+
+    def __enter__(self):
+        try:
+            fd, self.path = tempfile.mkstemp(suffix=".csv")
+            os.close(fd)
+            self.proc = subprocess.Popen(["nvidia-smi", f"--id={self.index}", f"--query-gpu={self.Q}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=open(self.path, "w"), stderr=subprocess.DEVNULL)
+        except (OSError, FileNotFoundError):
+            self.proc = None
+        return self
+
+    def __exit__(self, *a):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self) -> dict:
+        if not self.path or not os.path.exists(self.path):
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        rows = []
+        for line in open(self.path):
+            f = [x.strip() for x in line.split(",")]
+            if len(f) >= 9:
+                try:
+                    rows.append((float(f[1]), float(f[2]), float(f[3]), f[5], f[6], f[7], f[8]))
+                except ValueError:
+                    pass
+        os.unlink(self.path)
+        if not rows:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["no samples"]}
+        pmax = max(r[2] for r in rows)
+        loaded = [r for r in rows if r[2] >= 0.5 * pmax] or rows
+        reasons = set()
+        for r in loaded:
+            for name, v in zip(("hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"), r[3:]):
+                if v.lower() == "active":
+                    reasons.add(name)
+        return {"sm_mhz": statistics.median(r[0] for r in loaded), "sm_max_mhz": max(r[1] for r in rows),
+                "power_w_max": pmax, "samples": len(loaded), "reasons": sorted(reasons)}
+
+
+def dist_setup():
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if world > 1:
+        import torch.distributed as dist
+        import torch
+        backend = "nccl" if torch.cuda.is_available() else "gloo"
+        dist.init_process_group(backend)
+    return world, rank, local
+
+
+def max_over_ranks(x: float, world: int) -> float:
+    if world == 1:
+        return x
+    import torch
+    import torch.distributed as dist
+    dev = "cuda" if torch.cuda.is_available() and dist.get_backend() == "nccl" else "cpu"
+    t = torch.tensor([x], dtype=torch.float64, device=dev)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def barrier(world: int):
+    if world > 1:
+        import torch.distributed as dist
+        dist.barrier()
+
+
+def cpu_baseline(setup, seconds: float, threads: int) -> dict:
+    """The oracle's single-precision port on the host cores, on a bounded
+    sample (the first photons of the step's sources)."""
+    import oracle
+    oracle.build()
+    total = sum(int(s.photons) for s in setup.sources)
+    n = 20_000
+    t0 = time.perf_counter()
+    oracle.propagate_f32(setup, seed=7, gid_begin=0, gid_end=n, threads=threads)
+    dt = time.perf_counter() - t0
+    n = int(min(total, max(n, n * seconds / max(dt, 1e-6))))
+    t0 = time.perf_counter()
+    oracle.propagate_f32(setup, seed=8, gid_begin=0, gid_end=n, threads=threads)
+    dt = time.perf_counter() - t0
+    return {"value": n / dt, "unit": METRIC, "cores": threads, "kind": "port",
+            "sample": f"first {n} photons of the step's cascades (of {total}), {dt:.1f} s, single-precision "
+                      f"oracle port, OpenMP"}
+
+
+def run_reference(args, world, rank):
+    """--impl reference: the reference's step law on the host cores (the
+    reference itself is Julia + CUDA.jl and has no CPU path; its restatement in
+    oracle/ runs instead), on a bounded sample per step."""
+    if rank != 0:
+        return
+    from neutrinotelescopes_gb300 import workloads
+    import oracle
+    oracle.build()
+    setup = workloads.cascade_string_setup(N_CASCADES, WORKLOAD_SEED)
+    threads = os.cpu_count() or 1
+    total = sum(int(s.photons) for s in setup.sources)
+    n = 20_000
+    t0 = time.perf_counter()
+    oracle.propagate_f32(setup, seed=1, gid_begin=0, gid_end=n, threads=threads)
+    per = (time.perf_counter() - t0) / n
+    n = int(min(total, max(n, 5.0 / per)))
+    for i in range(args.warmup):
+        oracle.propagate_f32(setup, seed=100 + i, gid_begin=0, gid_end=min(n, 20_000), threads=threads)
+    times = []
+    for i in range(args.steps):
+        t0 = time.perf_counter()
+        oracle.propagate_f32(setup, seed=1000 + i, gid_begin=0, gid_end=n, threads=threads)
+        times.append(time.perf_counter() - t0)
+    value = n * len(times) / sum(times)
+    out = {"metric": METRIC, "value": value, "unit": METRIC, "impl": "reference", "n_gpus": args.gpus,
+           "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * sum(times) / len(times),
+           "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+           "data": "synthetic",
+           "config": {"workload": "cascade_string: 4 EM cascades 1e3-1e5 GeV, 20 POM modules, simple water",
+                      "photons_per_step": n, "sample_of": total},
+           "cpu_baseline": {"value": value, "unit": METRIC, "cores": threads, "kind": "port",
+                            "sample": f"first {n} photons of the workload per step"},
+           "e2e": {"value": value, "unit": METRIC, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(out))
+
+
+def main():
+    args = parse()
+    world, rank, local = dist_setup()
+    if args.impl == "reference":
+        run_reference(args, world, rank)
+        return
+    import numpy as np
+    import torch
+
+    import neutrinotelescopes_gb300 as nt
+    from neutrinotelescopes_gb300 import _abi, workloads
+    from neutrinotelescopes_gb300.photon_prop import pack_sources
+
+    torch.cuda.set_device(local)
+    setup = workloads.cascade_string_setup(N_CASCADES, WORKLOAD_SEED, device=local)
+    lib, ctx = setup.context()
+    srcs = pack_sources(setup.sources)
+    n_src = len(setup.sources)
+    photons = sum(int(s.photons) for s in setup.sources)
+    cap = 1 << 24
+    hits = torch.empty((cap, 64), dtype=torch.uint8, device=f"cuda:{local}")
+    flush = torch.empty(512 << 20, dtype=torch.uint8, device=f"cuda:{local}")
+    stream = torch.cuda.current_stream()
+    opts = setup.prop_opts(stream=stream.cuda_stream)
+    nh, ns = C.c_uint64(), C.c_uint64()
+    stats = _abi.NtpRunStats()
+
+    def step(i: int) -> None:
+        seed = workloads.SEED_BASE + 1 + rank * 1_000_003 + i
+        st = lib.ntp_propagate(ctx, srcs, n_src, seed, C.byref(opts), hits.data_ptr(), cap, 1, C.byref(nh),
+                               C.byref(ns))
+        if st != _abi.NTP_OK:
+            raise _abi.NtpError(st, lib.ntp_last_error(ctx).decode())
+
+    for i in range(args.warmup):
+        step(10_000 + i)
+    barrier(world)
+    torch.cuda.synchronize()
+    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
+    steps_taken, hit_counts = [], []
+    with ClockSampler(local) as clk:
+        for i in range(args.steps):
+            flush.zero_()
+            ev[i][0].record(stream)
+            step(i)
+            ev[i][1].record(stream)
+            lib.ntp_get_run_stats(ctx, C.byref(stats))
+            steps_taken.append(stats.photon_steps)
+            hit_counts.append(stats.hits)
+        torch.cuda.synchronize()
+    barrier(world)
+    ms = [a.elapsed_time(b) for a, b in ev]
+    t_dev = max_over_ranks(sum(ms) / 1e3, world)
+    value = photons * args.steps * world / t_dev
+    clocks = clk.summary()
+
+    # roofline of the propagation kernel: algorithmic lane-ops / kernel time
+    ops_step = algo_ops_per_step(len(setup.targets))
+    achieved = sum(steps_taken) * ops_step / (sum(ms) / 1e3) / 1e9
+    sm_mhz = clocks.get("sm_mhz") or 2070.0
+    peak = 152 * 4 * 32 * sm_mhz * 1e6 / 1e9  # lane-instructions issued per second at the sampled clock
+    roofline = {"bound": "issue", "achieved": achieved, "peak": peak, "unit": "Gop/s",
+                "frac": achieved / peak,
+                "peak_source": f"nominal issue rate 152 SM x 4 schedulers x 32 lanes at the sampled {sm_mhz:.0f} MHz",
+                "ops_per_photon_step": ops_step, "photon_steps_per_step": int(statistics.mean(steps_taken)),
+                "traffic": None}
+
+    # e2e through the public call with host buffers
+    e2e_t, e2e_hits = [], []
+    for i in range(args.e2e_steps):
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        h = nt.propagate_photons(setup, seed=workloads.SEED_BASE + 500 + i, capacity=cap)
+        e2e_t.append(time.perf_counter() - t0)
+        e2e_hits.append(len(h))
+    e2e_val = photons * len(e2e_t) * world / max_over_ranks(sum(e2e_t), world)
+    h2d = C.sizeof(_abi.NtpSource) * n_src + 8 * (n_src + 1)
+    d2h = int(statistics.mean(e2e_hits)) * 64 + 32
+
+    out = {"metric": METRIC, "value": value, "unit": METRIC, "n_gpus": world, "steps": args.steps,
+           "warmup": args.warmup, "ms_per_step": statistics.mean(ms), "higher_is_better": True,
+           "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+           "config": {"workload": "cascade_string: 4 EM cascades 1e3-1e5 GeV (7.5e9 photons), 20 POM modules x 16 PMTs "
+                                  "on one string, simple water", "photons_per_step": photons,
+                      "hits_per_step": int(statistics.mean(hit_counts)), "l2": "flushed between steps (512 MB write)",
+                      "parallelism": f"replicas x{world}"},
+           "roofline": roofline, "clocks": clocks,
+           "e2e": {"value": e2e_val, "unit": METRIC, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
+           "gpu_launches": args.steps}
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+        out["cpu_baseline"] = cpu_baseline(setup, args.cpu_seconds, os.cpu_count() or 1)
+    if rank == 0:
+        print(json.dumps(out))
+    setup.close()
+    if world > 1:
+        import torch.distributed as dist
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,254 @@
+/*
+ * ntp.h -- C ABI of the GB300-native photon-propagation library (libntp.so).
+ *
+ * The library replaces the photon-propagation hot path of NeutrinoTelescopes
+ * (Julia + CUDA.jl).  Every entry point below names the reference function it
+ * stands in for.  All structs are plain old data with fixed sizes, all
+ * buffers are raw pointers plus element counts, and every call returns an
+ * ntp_status.  A context is used by one host thread at a time (or is
+ * synchronised by the caller).
+ *
+ * Units follow the reference: metres, nanoseconds, nanometres, radians.
+ */
+#ifndef NTP_H
+#define NTP_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define NTP_ABI_VERSION 1
+
+typedef enum ntp_status {
+    NTP_OK = 0,
+    NTP_ERR_INVALID = 1,   /* bad argument: null pointer, size out of range, unknown kind   */
+    NTP_ERR_OVERFLOW = 2,  /* hit buffer too small: hits truncated, returned counts exact   */
+    NTP_ERR_CUDA = 3,      /* CUDA runtime error; text in ntp_last_error()                 */
+    NTP_ERR_NOT_READY = 4, /* medium, spectrum or targets not set on the context           */
+    NTP_ERR_TIMEOUT = 5,   /* a bounded wait gave up                                        */
+    NTP_ERR_NOMEM = 6      /* device allocation failed or an HBM budget would be exceeded   */
+} ntp_status;
+
+/* ------------------------------------------------------------------ sources
+ * Photon emitters, src/photon_propagation/lightyield.jl:421-530.  One record
+ * type carries every emitter kind; fields a kind does not use are ignored.   */
+enum ntp_source_kind {
+    NTP_SRC_POINT_ISOTROPIC = 0,    /* PointlikeIsotropicEmitter   lightyield.jl:436-440 */
+    NTP_SRC_POINT_TIME_RANGE = 1,   /* PointlikeTimeRangeEmitter   lightyield.jl:449-453 */
+    NTP_SRC_AXICONE = 2,            /* AxiconeEmitter              lightyield.jl:421-427 */
+    NTP_SRC_PENCIL = 3,             /* PencilEmitter               lightyield.jl:429-434 */
+    NTP_SRC_EXTENDED_CHERENKOV = 4, /* ExtendedCherenkovEmitter    lightyield.jl:463-481 */
+    NTP_SRC_POINT_CHERENKOV = 5,    /* PointlikeCherenkovEmitter   lightyield.jl:491-509 */
+    NTP_SRC_CHERENKOV_TRACK = 6     /* CherenkovTrackEmitter       lightyield.jl:519-530 */
+};
+
+typedef struct ntp_source {  /* 64 bytes */
+    float position[3];
+    float time;          /* emission time (ns); start of the range for TIME_RANGE       */
+    float direction[3];  /* unit vector (AXICONE, PENCIL, Cherenkov kinds)               */
+    float angle;         /* AXICONE opening angle (rad)                                  */
+    uint64_t photons;    /* number of photons to emit                                    */
+    int32_t kind;        /* enum ntp_source_kind                                         */
+    float time_end;      /* TIME_RANGE end of the range (ns)                             */
+    float long_a;        /* EXTENDED_CHERENKOV: gamma shape a of the longitudinal profile */
+    float long_b;        /* EXTENDED_CHERENKOV: gamma rate b                              */
+    float long_lrad;     /* EXTENDED_CHERENKOV: radiation length (m)                      */
+    float length;        /* CHERENKOV_TRACK: track length (m)                             */
+} ntp_source;
+
+/* ------------------------------------------------------------------ targets
+ * Optical modules, src/photon_propagation/detection.jl:29-46.               */
+enum ntp_target_kind {
+    NTP_TARGET_SPHERE = 0,    /* DetectionSphere   detection.jl:29-36 */
+    NTP_TARGET_MULTI_PMT = 1  /* MultiPMTDetector  detection.jl:39-46 */
+};
+
+typedef struct ntp_target {  /* 48 bytes */
+    float position[3];
+    float radius;
+    uint32_t module_id;   /* written into every hit on this module                     */
+    int32_t kind;         /* enum ntp_target_kind                                      */
+    float pmt_area;       /* m^2                                                       */
+    int32_t n_pmts;       /* SPHERE: PMT count (area acceptance); MULTI_PMT: PMTs in layout */
+    int32_t pmt_offset;   /* MULTI_PMT: first (theta, phi) pair in the PMT coordinate table */
+    int32_t reserved[3];
+} ntp_target;
+
+/* --------------------------------------------------------------------- hits
+ * One photon that reached a module, PhotonHit photon_prop_cuda.jl:391-399,
+ * plus the photon's identity so that a run can be replayed and photons can be
+ * assigned to their sources.  64 bytes, 16-byte aligned, stored as an array. */
+typedef struct ntp_hit {
+    float position[3];
+    float time;
+    float direction[3];          /* direction at the hit                        */
+    float wavelength;
+    float initial_direction[3];  /* direction at emission                       */
+    float dist_travelled;
+    uint32_t module_id;
+    uint32_t source_index;       /* index of the source in the ntp_propagate call */
+    uint64_t photon_index;       /* index of the photon within its source        */
+} ntp_hit;
+
+/* ------------------------------------------------------------------- medium
+ * Water optics, src/photon_propagation/medium.jl.  The per-photon quantities
+ * are tabulated by the caller on a uniform wavelength grid (the caller
+ * evaluates its own refractive_index / group_velocity / scattering_length at
+ * the knots); absorption is a per-hit weight on its own, possibly non-uniform,
+ * knots, as in medium.jl:392-414.                                            */
+typedef struct ntp_medium_desc {
+    int32_t n_knots;               /* >= 2, <= NTP_MAX_MEDIUM_KNOTS                         */
+    float wl_min;                  /* nm, first knot                                        */
+    float wl_max;                  /* nm, last knot                                         */
+    const float* ref_index;        /* phase refractive index n(lambda), medium.jl:234-244   */
+    const float* group_velocity;   /* m/ns, medium.jl:313-318                               */
+    const float* scattering_length;/* m, medium.jl:331-370                                  */
+    int32_t n_abs_knots;           /* >= 2, <= NTP_MAX_ABS_KNOTS                             */
+    const float* abs_wavelength;   /* nm, ascending                                         */
+    const float* abs_length;       /* m, medium.jl:392-414                                  */
+    float hg_g;                    /* Henyey-Greenstein mean cosine, photon_prop_cuda.jl:70-77 */
+    float rayleigh_fraction;       /* share of Rayleigh scatters, 0 for the reference medium */
+} ntp_medium_desc;
+
+#define NTP_MAX_MEDIUM_KNOTS 2048
+#define NTP_MAX_ABS_KNOTS 1024
+
+/* ----------------------------------------------------------------- spectrum
+ * Wavelength sampling, src/photon_propagation/spectrum.jl:89-108 and
+ * photon_prop_cuda.jl:128-130.                                               */
+enum ntp_spectrum_kind {
+    NTP_SPEC_MONOCHROMATIC = 0,  /* Monochromatic spectrum.jl:21-23                          */
+    NTP_SPEC_TABLE_LINEAR = 1,   /* inverse-CDF knots at u = k/(n-1), linear interpolation   */
+    NTP_SPEC_TABLE_TEXTURE = 2,  /* inverse-CDF knots read like the reference's 1-D texture:
+                                    normalised coordinate u*n-0.5, clamp, linear filter with
+                                    an 8-bit fraction (spectrum.jl:102-103)                  */
+    NTP_SPEC_INV_SQUARE = 3      /* dN/dlambda ~ 1/lambda^2 on [wl_min, wl_max], exact inverse */
+};
+
+typedef struct ntp_spectrum_desc {
+    int32_t kind;              /* enum ntp_spectrum_kind                         */
+    int32_t n_knots;           /* TABLE kinds: >= 2, <= NTP_MAX_SPECTRUM_KNOTS    */
+    const float* icdf_knots;   /* TABLE kinds: wavelength (nm) at each knot      */
+    float wl_min;              /* INV_SQUARE range (nm)                           */
+    float wl_max;
+    float wavelength;          /* MONOCHROMATIC wavelength (nm)                   */
+} ntp_spectrum_desc;
+
+#define NTP_MAX_SPECTRUM_KNOTS 4096
+
+/* ---------------------------------------------------------- propagation opts */
+enum ntp_hit_policy {
+    NTP_HIT_FIRST_IN_LIST = 0,  /* first intersecting target in list order wins, photon_prop_cuda.jl:460-468 */
+    NTP_HIT_NEAREST = 1         /* nearest intersecting target wins                                       */
+};
+
+enum ntp_prop_flags {
+    /* rot_from_ez_fast (utils.jl:228-243) maps v to (v1, copysign(v2,a3), copysign(v3,a3))
+       when |a3| == 1.  By default that is reproduced; this flag applies the true rotation. */
+    NTP_FLAG_EXACT_POLE_ROTATION = 1
+};
+
+typedef struct ntp_prop_opts {
+    int32_t max_steps;   /* scatter steps per photon, photon_prop_cuda.jl:449 uses 15 */
+    int32_t hit_policy;  /* enum ntp_hit_policy                                       */
+    int32_t flags;       /* enum ntp_prop_flags                                       */
+    int32_t reserved;
+    void* stream;        /* cudaStream_t for device-buffer calls; NULL = context stream */
+} ntp_prop_opts;
+
+/* -------------------------------------------------------------------- calls */
+typedef struct ntp_ctx ntp_ctx;
+
+/* ABI version compiled into the library (NTP_ABI_VERSION). */
+int ntp_abi_version(void);
+
+/* Creates a context on CUDA device `device`.  Replaces the implicit CUDA.jl
+   device state used by run_photon_prop_no_local_cache, photon_prop_cuda.jl:726-759. */
+ntp_status ntp_create(int device, ntp_ctx** out);
+void ntp_destroy(ntp_ctx* ctx);
+
+/* Text of the last error on this context ("" if none).  With ctx == NULL,
+   the last error of a failed ntp_create. */
+const char* ntp_last_error(const ntp_ctx* ctx);
+
+/* Medium of PhotonPropSetup (photon_prop_cuda.jl:34-39): copies the tables to
+   the device. */
+ntp_status ntp_set_medium(ntp_ctx* ctx, const ntp_medium_desc* medium);
+
+/* Spectrum of PhotonPropSetup; replaces the CuTexture built by
+   CherenkovSpectrum, spectrum.jl:97-106. */
+ntp_status ntp_set_spectrum(ntp_ctx* ctx, const ntp_spectrum_desc* spectrum);
+
+/* Targets of PhotonPropSetup (CuVector(targets), photon_prop_cuda.jl:740),
+   with the (theta, phi) PMT coordinate table of MultiPMTDetector
+   (pmt_coords holds n_pmt_coords pairs; may be NULL if no MULTI_PMT target). */
+ntp_status ntp_set_targets(ntp_ctx* ctx, const ntp_target* targets, int32_t n_targets,
+                           const float* pmt_coords, int32_t n_pmt_coords);
+
+/* propagate_photons(setup), photon_prop_cuda.jl:804-817 with the kernel
+   cuda_propagate_photons!, :402-506.  Simulates every photon of every source
+   and appends hits to `hits` (capacity records).  hits_on_device != 0: `hits`
+   is a device pointer and the call is asynchronous on opts->stream except for
+   the final count read; otherwise `hits` is host memory.  On return
+   *n_hits is the exact number of hits (it may exceed capacity: then
+   NTP_ERR_OVERFLOW, and the first `capacity` slots are filled) and
+   *n_photons_simulated the number of photons stepped.  Photon k of source s
+   draws its random numbers from the Philox4x32-10 counter (draw, k, s) under
+   key `seed`, so a rerun with the same arguments yields the same set of hits. */
+ntp_status ntp_propagate(ntp_ctx* ctx, const ntp_source* sources, int32_t n_sources,
+                         uint64_t seed, const ntp_prop_opts* opts,
+                         ntp_hit* hits, uint64_t capacity, int32_t hits_on_device,
+                         uint64_t* n_hits, uint64_t* n_photons_simulated);
+
+/* Counters of the last ntp_propagate on this context (no reference
+   counterpart beyond n_ph_sim of photon_prop_cuda.jl:758). */
+typedef struct ntp_run_stats {
+    uint64_t photons;        /* photons simulated                                  */
+    uint64_t hits;           /* hits found (may exceed the buffer capacity)         */
+    uint64_t photon_steps;   /* scatter segments stepped over all photons          */
+    int32_t grid;            /* blocks launched                                    */
+    int32_t block;           /* threads per block                                  */
+    uint64_t chunk;          /* photons a warp claims at once                      */
+} ntp_run_stats;
+
+ntp_status ntp_get_run_stats(const ntp_ctx* ctx, ntp_run_stats* out);
+
+/* make_hits_from_photons, photon_prop_cuda.jl:884-904 with check_pmt_hit,
+   detection.jl:88-104: for each hit the 1-based index of the PMT whose
+   opening cone contains the hit position, 0 for none.  `orientation` is a
+   row-major 3x3 rotation applied to every module's PMT axes.  A hit on a
+   SPHERE target gets PMT 1 (detection.jl:86).  buffers_on_device selects
+   device or host pointers for hits and pmt_id. */
+ntp_status ntp_make_hits(ntp_ctx* ctx, const ntp_hit* hits, uint64_t n_hits,
+                         const double orientation[9], int32_t* pmt_id,
+                         int32_t buffers_on_device, void* stream);
+
+/* calc_total_weight!, photon_prop_cuda.jl:850-882: per hit the area
+   acceptance (detection.jl:139-146), the PMT wavelength acceptance
+   (detection.jl:148-163, table set by ntp_set_wavelength_acceptance) and the
+   absorption weight exp(-dist/abs_length(lambda)).  Any output pointer may be
+   NULL.  total_weight = area_acc * wl_acc * abs_weight. */
+ntp_status ntp_calc_total_weight(ntp_ctx* ctx, const ntp_hit* hits, uint64_t n_hits,
+                                 double* area_acc, double* wl_acc, double* abs_weight,
+                                 double* total_weight, int32_t buffers_on_device, void* stream);
+
+/* Wavelength acceptance table of one PMT (assets/PMTAcc.csv in the
+   reference, detection.jl:161-163): n ascending knots, linear interpolation. */
+ntp_status ntp_set_wavelength_acceptance(ntp_ctx* ctx, const double* wavelength,
+                                         const double* acceptance, int32_t n);
+
+/* calc_time_residual!, photon_prop_cuda.jl:906-924: tres = time - tgeo(module),
+   tgeo = (|source_position - module_position| - radius) / (c_vac / n800),
+   n800 = refractive index at 800 nm. */
+ntp_status ntp_calc_time_residual(ntp_ctx* ctx, const ntp_hit* hits, uint64_t n_hits,
+                                  const float source_position[3], float n800,
+                                  double* tres, int32_t buffers_on_device, void* stream);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* NTP_H */

@@ -1,0 +1,226 @@
+"""ctypes view of the C ABI in include/ntp.h and the loader of libntp.so.
+
+The library is the only compute path: if it is missing or fails to load,
+every call raises.  There is no CPU fallback.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import threading
+from pathlib import Path
+
+import numpy as np
+
+PKG = Path(__file__).resolve().parent
+LIB_PATH = PKG / "libntp.so"
+
+NTP_ABI_VERSION = 1
+
+# ntp_status
+NTP_OK = 0
+NTP_ERR_INVALID = 1
+NTP_ERR_OVERFLOW = 2
+NTP_ERR_CUDA = 3
+NTP_ERR_NOT_READY = 4
+NTP_ERR_TIMEOUT = 5
+NTP_ERR_NOMEM = 6
+
+# ntp_source_kind
+SRC_POINT_ISOTROPIC = 0
+SRC_POINT_TIME_RANGE = 1
+SRC_AXICONE = 2
+SRC_PENCIL = 3
+SRC_EXTENDED_CHERENKOV = 4
+SRC_POINT_CHERENKOV = 5
+SRC_CHERENKOV_TRACK = 6
+
+# ntp_target_kind
+TARGET_SPHERE = 0
+TARGET_MULTI_PMT = 1
+
+# ntp_spectrum_kind
+SPEC_MONOCHROMATIC = 0
+SPEC_TABLE_LINEAR = 1
+SPEC_TABLE_TEXTURE = 2
+SPEC_INV_SQUARE = 3
+
+# ntp_hit_policy / flags
+HIT_FIRST_IN_LIST = 0
+HIT_NEAREST = 1
+FLAG_EXACT_POLE_ROTATION = 1
+
+
+class NtpSource(C.Structure):
+    _fields_ = [
+        ("position", C.c_float * 3),
+        ("time", C.c_float),
+        ("direction", C.c_float * 3),
+        ("angle", C.c_float),
+        ("photons", C.c_uint64),
+        ("kind", C.c_int32),
+        ("time_end", C.c_float),
+        ("long_a", C.c_float),
+        ("long_b", C.c_float),
+        ("long_lrad", C.c_float),
+        ("length", C.c_float),
+    ]
+
+
+class NtpTarget(C.Structure):
+    _fields_ = [
+        ("position", C.c_float * 3),
+        ("radius", C.c_float),
+        ("module_id", C.c_uint32),
+        ("kind", C.c_int32),
+        ("pmt_area", C.c_float),
+        ("n_pmts", C.c_int32),
+        ("pmt_offset", C.c_int32),
+        ("reserved", C.c_int32 * 3),
+    ]
+
+
+class NtpMediumDesc(C.Structure):
+    _fields_ = [
+        ("n_knots", C.c_int32),
+        ("wl_min", C.c_float),
+        ("wl_max", C.c_float),
+        ("ref_index", C.POINTER(C.c_float)),
+        ("group_velocity", C.POINTER(C.c_float)),
+        ("scattering_length", C.POINTER(C.c_float)),
+        ("n_abs_knots", C.c_int32),
+        ("abs_wavelength", C.POINTER(C.c_float)),
+        ("abs_length", C.POINTER(C.c_float)),
+        ("hg_g", C.c_float),
+        ("rayleigh_fraction", C.c_float),
+    ]
+
+
+class NtpSpectrumDesc(C.Structure):
+    _fields_ = [
+        ("kind", C.c_int32),
+        ("n_knots", C.c_int32),
+        ("icdf_knots", C.POINTER(C.c_float)),
+        ("wl_min", C.c_float),
+        ("wl_max", C.c_float),
+        ("wavelength", C.c_float),
+    ]
+
+
+class NtpPropOpts(C.Structure):
+    _fields_ = [
+        ("max_steps", C.c_int32),
+        ("hit_policy", C.c_int32),
+        ("flags", C.c_int32),
+        ("reserved", C.c_int32),
+        ("stream", C.c_void_p),
+    ]
+
+
+class NtpRunStats(C.Structure):
+    _fields_ = [
+        ("photons", C.c_uint64),
+        ("hits", C.c_uint64),
+        ("photon_steps", C.c_uint64),
+        ("grid", C.c_int32),
+        ("block", C.c_int32),
+        ("chunk", C.c_uint64),
+    ]
+
+
+assert C.sizeof(NtpSource) == 64
+assert C.sizeof(NtpTarget) == 48
+
+# ntp_hit as a numpy record (64 bytes)
+HIT_DTYPE = np.dtype(
+    [
+        ("position", np.float32, (3,)),
+        ("time", np.float32),
+        ("direction", np.float32, (3,)),
+        ("wavelength", np.float32),
+        ("initial_direction", np.float32, (3,)),
+        ("dist_travelled", np.float32),
+        ("module_id", np.uint32),
+        ("source_index", np.uint32),
+        ("photon_index", np.uint64),
+    ],
+    align=True,
+)
+assert HIT_DTYPE.itemsize == 64
+
+# every symbol include/ntp.h declares
+EXPORTED = (
+    "ntp_abi_version",
+    "ntp_create",
+    "ntp_destroy",
+    "ntp_last_error",
+    "ntp_set_medium",
+    "ntp_set_spectrum",
+    "ntp_set_targets",
+    "ntp_propagate",
+    "ntp_get_run_stats",
+    "ntp_make_hits",
+    "ntp_calc_total_weight",
+    "ntp_set_wavelength_acceptance",
+    "ntp_calc_time_residual",
+)
+
+_lib = None
+_lock = threading.Lock()
+
+
+def _declare(lib: C.CDLL) -> None:
+    vp, i32, u64 = C.c_void_p, C.c_int32, C.c_uint64
+    lib.ntp_abi_version.restype = C.c_int
+    lib.ntp_create.argtypes = [C.c_int, C.POINTER(vp)]
+    lib.ntp_create.restype = C.c_int
+    lib.ntp_destroy.argtypes = [vp]
+    lib.ntp_destroy.restype = None
+    lib.ntp_last_error.argtypes = [vp]
+    lib.ntp_last_error.restype = C.c_char_p
+    lib.ntp_set_medium.argtypes = [vp, C.POINTER(NtpMediumDesc)]
+    lib.ntp_set_spectrum.argtypes = [vp, C.POINTER(NtpSpectrumDesc)]
+    lib.ntp_set_targets.argtypes = [vp, C.POINTER(NtpTarget), i32, C.POINTER(C.c_float), i32]
+    lib.ntp_propagate.argtypes = [vp, C.POINTER(NtpSource), i32, u64, C.POINTER(NtpPropOpts), vp, u64, i32,
+                                  C.POINTER(u64), C.POINTER(u64)]
+    lib.ntp_get_run_stats.argtypes = [vp, C.POINTER(NtpRunStats)]
+    lib.ntp_make_hits.argtypes = [vp, vp, u64, C.POINTER(C.c_double), vp, i32, vp]
+    lib.ntp_calc_total_weight.argtypes = [vp, vp, u64, vp, vp, vp, vp, i32, vp]
+    lib.ntp_set_wavelength_acceptance.argtypes = [vp, C.POINTER(C.c_double), C.POINTER(C.c_double), i32]
+    lib.ntp_calc_time_residual.argtypes = [vp, vp, u64, C.POINTER(C.c_float), C.c_float, vp, i32, vp]
+    for name in ("ntp_set_medium", "ntp_set_spectrum", "ntp_set_targets", "ntp_propagate", "ntp_get_run_stats",
+                 "ntp_make_hits",
+                 "ntp_calc_total_weight", "ntp_set_wavelength_acceptance", "ntp_calc_time_residual"):
+        getattr(lib, name).restype = C.c_int
+
+
+def load_library(path: Path | str | None = None) -> C.CDLL:
+    """Loads libntp.so (building nothing); raises if it is absent."""
+    global _lib
+    with _lock:
+        if _lib is not None and path is None:
+            return _lib
+        p = Path(path) if path is not None else LIB_PATH
+        if not p.exists():
+            raise RuntimeError(
+                f"{p} is missing: build the CUDA library first "
+                "(python -c 'import __graft_entry__ as g; g.build()' or python neutrinotelescopes_gb300/build.py)"
+            )
+        lib = C.CDLL(str(p))
+        _declare(lib)
+        if lib.ntp_abi_version() != NTP_ABI_VERSION:
+            raise RuntimeError(f"libntp.so ABI {lib.ntp_abi_version()} != {NTP_ABI_VERSION}")
+        if path is None:
+            _lib = lib
+        return lib
+
+
+class NtpError(RuntimeError):
+    """A libntp call returned a status other than NTP_OK."""
+
+    def __init__(self, status: int, message: str):
+        super().__init__(f"libntp status {status}: {message}")
+        self.status = status
+
+
+def fptr(a: np.ndarray):
+    return a.ctypes.data_as(C.POINTER(C.c_float))

@@ -1,0 +1,625 @@
+// ntp_abi.cu -- the extern "C" entry points of libntp.so (declared in
+// include/ntp.h).  Owns the per-context device state: medium / spectrum /
+// target tables (uploaded once by the ntp_set_* calls, like the arguments
+// of PhotonPropSetup, photon_prop_cuda.jl:34-45), the launch scratch
+// (photon / hit counters) and grow-only staging buffers for host-memory calls.
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <mutex>
+#include <string>
+#include <vector>
+
+#include <cuda_runtime.h>
+
+#include "ntp_internal.h"
+
+struct ntp_ctx {
+    int device = 0;
+    int num_sms = 0;
+    cudaStream_t stream = nullptr;
+    std::string err;
+
+    // medium
+    bool have_medium = false;
+    int n_med = 0;
+    float wl_min = 0, wl_max = 0, hg_g = 0, f_ray = 0;
+    float4* d_med = nullptr;
+    int n_abs = 0;
+    float* d_abs_wl = nullptr;
+    float* d_abs_len = nullptr;
+
+    // spectrum
+    bool have_spec = false;
+    int spec_kind = 0, n_spec = 0;
+    float spec_p0 = 0, spec_p1 = 0;
+    float* d_spec = nullptr;
+
+    // targets
+    bool have_targets = false;
+    int n_tgt = 0;
+    std::vector<ntp_target> targets;
+    std::vector<float> pmt_coords;  // (theta, phi) pairs
+    float4* d_tgt = nullptr;
+    uint32_t* d_tgt_id = nullptr;
+    uint2* d_sorted = nullptr;
+    float* d_radius = nullptr;
+    int* d_kind = nullptr;
+    int* d_npmt = nullptr;
+    int* d_pmtoff = nullptr;
+    double* d_opening = nullptr;
+    double* d_area = nullptr;
+    double* d_axes = nullptr;  // PMT axes for the current orientation
+    double* d_tgeo = nullptr;  // per-target tgeo for time residuals
+
+    // wavelength acceptance
+    int n_acc = 0;
+    double* d_acc_wl = nullptr;
+    double* d_acc = nullptr;
+
+    // launch scratch
+    unsigned long long* d_counters = nullptr;  // 4 words
+    unsigned long long* h_counters = nullptr;  // pinned
+    ntp_source* d_src = nullptr;
+    size_t src_cap = 0;
+    unsigned long long* d_prefix = nullptr;
+    size_t prefix_cap = 0;
+
+    ntp_run_stats stats{};
+
+    // staging for host-buffer calls
+    void* d_stage = nullptr;
+    size_t stage_bytes = 0;
+    void* d_stage2 = nullptr;
+    size_t stage2_bytes = 0;
+};
+
+namespace {
+
+std::string g_create_error;
+
+#define NTP_CUDA(ctx, call)                                                                   \
+    do {                                                                                      \
+        cudaError_t e_ = (call);                                                              \
+        if (e_ != cudaSuccess) {                                                              \
+            (ctx)->err = std::string(#call) + ": " + cudaGetErrorString(e_);                  \
+            return NTP_ERR_CUDA;                                                              \
+        }                                                                                     \
+    } while (0)
+
+ntp_status invalid(ntp_ctx* ctx, const std::string& msg) {
+    ctx->err = msg;
+    return NTP_ERR_INVALID;
+}
+
+template <typename T>
+void dfree(T*& p) {
+    if (p) cudaFree(p);
+    p = nullptr;
+}
+
+template <typename T>
+cudaError_t dupload(T*& d, const T* h, size_t n, cudaStream_t s) {
+    dfree(d);
+    if (n == 0) return cudaSuccess;
+    cudaError_t e = cudaMalloc(reinterpret_cast<void**>(&d), sizeof(T) * n);
+    if (e != cudaSuccess) return e;
+    e = cudaMemcpyAsync(d, h, sizeof(T) * n, cudaMemcpyHostToDevice, s);
+    if (e != cudaSuccess) return e;
+    return cudaStreamSynchronize(s);
+}
+
+// Grow-only device buffer: reallocates (by at least 1.5x) when too small.
+cudaError_t ensure(void*& d, size_t& cap, size_t bytes) {
+    if (d && bytes <= cap) return cudaSuccess;
+    const size_t want = std::max(bytes, cap + cap / 2);
+    if (d) cudaFree(d);
+    d = nullptr;
+    cap = 0;
+    cudaError_t e = cudaMalloc(&d, want);
+    if (e == cudaSuccess) cap = want;
+    return e;
+}
+
+bool finite(float x) { return std::isfinite(x); }
+
+cudaStream_t pick_stream(ntp_ctx* ctx, void* s) { return s ? static_cast<cudaStream_t>(s) : ctx->stream; }
+
+ntp::HitTargetTable hit_table(const ntp_ctx* ctx) {
+    ntp::HitTargetTable t;
+    t.sorted_ids = ctx->d_sorted;
+    t.n_targets = ctx->n_tgt;
+    t.targets = ctx->d_tgt;
+    t.radius = ctx->d_radius;
+    t.kind = ctx->d_kind;
+    t.n_pmts = ctx->d_npmt;
+    t.pmt_offset = ctx->d_pmtoff;
+    t.opening = ctx->d_opening;
+    t.area_acc = ctx->d_area;
+    return t;
+}
+
+}  // namespace
+
+extern "C" {
+
+int ntp_abi_version(void) { return NTP_ABI_VERSION; }
+
+ntp_status ntp_create(int device, ntp_ctx** out) {
+    if (!out) return NTP_ERR_INVALID;
+    *out = nullptr;
+    int n = 0;
+    cudaError_t e = cudaGetDeviceCount(&n);
+    if (e != cudaSuccess || device < 0 || device >= n) {
+        g_create_error = e != cudaSuccess ? std::string("cudaGetDeviceCount: ") + cudaGetErrorString(e)
+                                          : "device index out of range";
+        return e != cudaSuccess ? NTP_ERR_CUDA : NTP_ERR_INVALID;
+    }
+    ntp_ctx* ctx = new ntp_ctx();
+    ctx->device = device;
+    auto fail = [&](cudaError_t err, const char* what) {
+        g_create_error = std::string(what) + ": " + cudaGetErrorString(err);
+        ntp_destroy(ctx);
+        return NTP_ERR_CUDA;
+    };
+    if ((e = cudaSetDevice(device)) != cudaSuccess) return fail(e, "cudaSetDevice");
+    if ((e = cudaDeviceGetAttribute(&ctx->num_sms, cudaDevAttrMultiProcessorCount, device)) != cudaSuccess)
+        return fail(e, "cudaDeviceGetAttribute");
+    if ((e = cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking)) != cudaSuccess)
+        return fail(e, "cudaStreamCreate");
+    if ((e = cudaMalloc(&ctx->d_counters, 4 * sizeof(unsigned long long))) != cudaSuccess)
+        return fail(e, "cudaMalloc");
+    if ((e = cudaMallocHost(&ctx->h_counters, 4 * sizeof(unsigned long long))) != cudaSuccess)
+        return fail(e, "cudaMallocHost");
+    *out = ctx;
+    return NTP_OK;
+}
+
+void ntp_destroy(ntp_ctx* ctx) {
+    if (!ctx) return;
+    cudaSetDevice(ctx->device);
+    if (ctx->stream) cudaStreamSynchronize(ctx->stream);
+    dfree(ctx->d_med);
+    dfree(ctx->d_abs_wl);
+    dfree(ctx->d_abs_len);
+    dfree(ctx->d_spec);
+    dfree(ctx->d_tgt);
+    dfree(ctx->d_tgt_id);
+    dfree(ctx->d_sorted);
+    dfree(ctx->d_radius);
+    dfree(ctx->d_kind);
+    dfree(ctx->d_npmt);
+    dfree(ctx->d_pmtoff);
+    dfree(ctx->d_opening);
+    dfree(ctx->d_area);
+    dfree(ctx->d_axes);
+    dfree(ctx->d_tgeo);
+    dfree(ctx->d_acc_wl);
+    dfree(ctx->d_acc);
+    dfree(ctx->d_counters);
+    dfree(ctx->d_src);
+    dfree(ctx->d_prefix);
+    if (ctx->d_stage) cudaFree(ctx->d_stage);
+    if (ctx->d_stage2) cudaFree(ctx->d_stage2);
+    if (ctx->h_counters) cudaFreeHost(ctx->h_counters);
+    if (ctx->stream) cudaStreamDestroy(ctx->stream);
+    delete ctx;
+}
+
+const char* ntp_last_error(const ntp_ctx* ctx) { return ctx ? ctx->err.c_str() : g_create_error.c_str(); }
+
+ntp_status ntp_set_medium(ntp_ctx* ctx, const ntp_medium_desc* m) {
+    if (!ctx) return NTP_ERR_INVALID;
+    if (!m) return invalid(ctx, "ntp_set_medium: medium is NULL");
+    if (m->n_knots < 2 || m->n_knots > NTP_MAX_MEDIUM_KNOTS)
+        return invalid(ctx, "ntp_set_medium: n_knots must be in [2, NTP_MAX_MEDIUM_KNOTS]");
+    if (!m->ref_index || !m->group_velocity || !m->scattering_length)
+        return invalid(ctx, "ntp_set_medium: a medium table is NULL");
+    if (!(m->wl_max > m->wl_min) || !finite(m->wl_min) || !finite(m->wl_max))
+        return invalid(ctx, "ntp_set_medium: need wl_max > wl_min");
+    if (m->n_abs_knots < 2 || m->n_abs_knots > NTP_MAX_ABS_KNOTS || !m->abs_wavelength || !m->abs_length)
+        return invalid(ctx, "ntp_set_medium: absorption table needs 2..NTP_MAX_ABS_KNOTS knots");
+    if (!finite(m->hg_g) || !(m->hg_g > -1.0f && m->hg_g < 1.0f))
+        return invalid(ctx, "ntp_set_medium: hg_g must lie in (-1, 1)");
+    if (!(m->rayleigh_fraction >= 0.0f && m->rayleigh_fraction <= 1.0f))
+        return invalid(ctx, "ntp_set_medium: rayleigh_fraction must lie in [0, 1]");
+    std::vector<float4> tab(m->n_knots);
+    for (int i = 0; i < m->n_knots; ++i) {
+        const float n = m->ref_index[i], vg = m->group_velocity[i], ls = m->scattering_length[i];
+        if (!(n > 1.0f) || !(vg > 0.0f) || !(ls > 0.0f) || !finite(n) || !finite(vg) || !finite(ls))
+            return invalid(ctx, "ntp_set_medium: need n > 1, group velocity > 0, scattering length > 0");
+        tab[i] = make_float4(n, vg, ls, 0.0f);
+    }
+    for (int i = 0; i < m->n_abs_knots; ++i) {
+        if (i && !(m->abs_wavelength[i] > m->abs_wavelength[i - 1]))
+            return invalid(ctx, "ntp_set_medium: absorption wavelengths must ascend");
+        if (!(m->abs_length[i] > 0.0f)) return invalid(ctx, "ntp_set_medium: absorption length must be > 0");
+    }
+    cudaSetDevice(ctx->device);
+    NTP_CUDA(ctx, dupload(ctx->d_med, tab.data(), tab.size(), ctx->stream));
+    NTP_CUDA(ctx, dupload(ctx->d_abs_wl, m->abs_wavelength, m->n_abs_knots, ctx->stream));
+    NTP_CUDA(ctx, dupload(ctx->d_abs_len, m->abs_length, m->n_abs_knots, ctx->stream));
+    ctx->n_med = m->n_knots;
+    ctx->wl_min = m->wl_min;
+    ctx->wl_max = m->wl_max;
+    ctx->n_abs = m->n_abs_knots;
+    ctx->hg_g = m->hg_g;
+    ctx->f_ray = m->rayleigh_fraction;
+    ctx->have_medium = true;
+    return NTP_OK;
+}
+
+ntp_status ntp_set_spectrum(ntp_ctx* ctx, const ntp_spectrum_desc* s) {
+    if (!ctx) return NTP_ERR_INVALID;
+    if (!s) return invalid(ctx, "ntp_set_spectrum: spectrum is NULL");
+    cudaSetDevice(ctx->device);
+    switch (s->kind) {
+    case NTP_SPEC_MONOCHROMATIC:
+        if (!(s->wavelength > 0.0f)) return invalid(ctx, "ntp_set_spectrum: wavelength must be > 0");
+        dfree(ctx->d_spec);
+        ctx->n_spec = 0;
+        ctx->spec_p0 = s->wavelength;
+        ctx->spec_p1 = 0;
+        break;
+    case NTP_SPEC_TABLE_LINEAR:
+    case NTP_SPEC_TABLE_TEXTURE:
+        if (s->n_knots < 2 || s->n_knots > NTP_MAX_SPECTRUM_KNOTS || !s->icdf_knots)
+            return invalid(ctx, "ntp_set_spectrum: table needs 2..NTP_MAX_SPECTRUM_KNOTS knots");
+        for (int i = 0; i < s->n_knots; ++i)
+            if (!(s->icdf_knots[i] > 0.0f) || !finite(s->icdf_knots[i]))
+                return invalid(ctx, "ntp_set_spectrum: knots must be finite wavelengths > 0");
+        NTP_CUDA(ctx, dupload(ctx->d_spec, s->icdf_knots, s->n_knots, ctx->stream));
+        ctx->n_spec = s->n_knots;
+        break;
+    case NTP_SPEC_INV_SQUARE:
+        if (!(s->wl_min > 0.0f) || !(s->wl_max > s->wl_min))
+            return invalid(ctx, "ntp_set_spectrum: need 0 < wl_min < wl_max");
+        dfree(ctx->d_spec);
+        ctx->n_spec = 0;
+        ctx->spec_p0 = 1.0f / s->wl_min;
+        ctx->spec_p1 = 1.0f / s->wl_min - 1.0f / s->wl_max;
+        break;
+    default:
+        return invalid(ctx, "ntp_set_spectrum: unknown kind");
+    }
+    ctx->spec_kind = s->kind;
+    ctx->have_spec = true;
+    return NTP_OK;
+}
+
+ntp_status ntp_set_targets(ntp_ctx* ctx, const ntp_target* t, int32_t n, const float* pmt_coords,
+                           int32_t n_pmt_coords) {
+    if (!ctx) return NTP_ERR_INVALID;
+    if (n < 0 || (n > 0 && !t)) return invalid(ctx, "ntp_set_targets: bad target array");
+    if (n_pmt_coords < 0 || (n_pmt_coords > 0 && !pmt_coords))
+        return invalid(ctx, "ntp_set_targets: bad PMT coordinate table");
+    std::vector<float4> tg(n);
+    std::vector<uint32_t> ids(n);
+    std::vector<uint2> sorted(n);
+    std::vector<float> radius(n);
+    std::vector<int> kind(n), npmt(n), off(n);
+    std::vector<double> opening(n), area(n);
+    for (int i = 0; i < n; ++i) {
+        const ntp_target& x = t[i];
+        if (!(x.radius > 0.0f) || !finite(x.radius) || !finite(x.position[0]) || !finite(x.position[1]) ||
+            !finite(x.position[2]))
+            return invalid(ctx, "ntp_set_targets: target " + std::to_string(i) + " has a bad position or radius");
+        if (x.kind != NTP_TARGET_SPHERE && x.kind != NTP_TARGET_MULTI_PMT)
+            return invalid(ctx, "ntp_set_targets: unknown target kind");
+        if (x.kind == NTP_TARGET_MULTI_PMT &&
+            (x.n_pmts < 0 || x.pmt_offset < 0 || static_cast<long long>(x.pmt_offset) + x.n_pmts > n_pmt_coords))
+            return invalid(ctx, "ntp_set_targets: PMT layout outside the coordinate table");
+        tg[i] = make_float4(x.position[0], x.position[1], x.position[2], x.radius * x.radius);
+        ids[i] = x.module_id;
+        sorted[i] = make_uint2(x.module_id, static_cast<unsigned>(i));
+        radius[i] = x.radius;
+        kind[i] = x.kind;
+        npmt[i] = x.kind == NTP_TARGET_MULTI_PMT ? x.n_pmts : 0;
+        off[i] = x.kind == NTP_TARGET_MULTI_PMT ? x.pmt_offset : 0;
+        // check_pmt_hit, detection.jl:94-95: opening angle in Float32
+        const float pmt_radius = std::sqrt(x.pmt_area / static_cast<float>(M_PI));
+        opening[i] = static_cast<double>(std::asin(pmt_radius / x.radius));
+        // area_acceptance, detection.jl:139-146
+        if (x.kind == NTP_TARGET_SPHERE) {
+            const float total_pmt_area = static_cast<float>(x.n_pmts) * x.pmt_area;
+            const float r2 = x.radius * x.radius;
+            area[i] = static_cast<double>(total_pmt_area) / (4.0 * M_PI * static_cast<double>(r2));
+        } else {
+            area[i] = 1.0;
+        }
+    }
+    std::sort(sorted.begin(), sorted.end(), [](uint2 a, uint2 b) { return a.x < b.x || (a.x == b.x && a.y < b.y); });
+    for (int i = 1; i < n; ++i)
+        if (sorted[i].x == sorted[i - 1].x)
+            return invalid(ctx, "ntp_set_targets: duplicate module_id " + std::to_string(sorted[i].x));
+    cudaSetDevice(ctx->device);
+    NTP_CUDA(ctx, dupload(ctx->d_tgt, tg.data(), n, ctx->stream));
+    NTP_CUDA(ctx, dupload(ctx->d_tgt_id, ids.data(), n, ctx->stream));
+    NTP_CUDA(ctx, dupload(ctx->d_sorted, sorted.data(), n, ctx->stream));
+    NTP_CUDA(ctx, dupload(ctx->d_radius, radius.data(), n, ctx->stream));
+    NTP_CUDA(ctx, dupload(ctx->d_kind, kind.data(), n, ctx->stream));
+    NTP_CUDA(ctx, dupload(ctx->d_npmt, npmt.data(), n, ctx->stream));
+    NTP_CUDA(ctx, dupload(ctx->d_pmtoff, off.data(), n, ctx->stream));
+    NTP_CUDA(ctx, dupload(ctx->d_opening, opening.data(), n, ctx->stream));
+    NTP_CUDA(ctx, dupload(ctx->d_area, area.data(), n, ctx->stream));
+    dfree(ctx->d_axes);
+    dfree(ctx->d_tgeo);
+    if (n_pmt_coords > 0) {
+        NTP_CUDA(ctx, cudaMalloc(&ctx->d_axes, sizeof(double) * 3 * n_pmt_coords));
+    }
+    if (n > 0) {
+        NTP_CUDA(ctx, cudaMalloc(&ctx->d_tgeo, sizeof(double) * n));
+    }
+    ctx->targets.assign(t, t + n);
+    ctx->pmt_coords.assign(pmt_coords, pmt_coords + 2 * static_cast<size_t>(n_pmt_coords));
+    ctx->n_tgt = n;
+    ctx->have_targets = true;
+    return NTP_OK;
+}
+
+ntp_status ntp_set_wavelength_acceptance(ntp_ctx* ctx, const double* wl, const double* acc, int32_t n) {
+    if (!ctx) return NTP_ERR_INVALID;
+    if (n < 2 || !wl || !acc) return invalid(ctx, "ntp_set_wavelength_acceptance: need >= 2 knots");
+    std::vector<double> x(n), y(n);
+    for (int i = 0; i < n; ++i) {
+        if (i && !(wl[i] > wl[i - 1])) return invalid(ctx, "ntp_set_wavelength_acceptance: wavelengths must ascend");
+        x[i] = wl[i];
+        y[i] = acc[i];
+    }
+    cudaSetDevice(ctx->device);
+    NTP_CUDA(ctx, dupload(ctx->d_acc_wl, x.data(), n, ctx->stream));
+    NTP_CUDA(ctx, dupload(ctx->d_acc, y.data(), n, ctx->stream));
+    ctx->n_acc = n;
+    return NTP_OK;
+}
+
+ntp_status ntp_propagate(ntp_ctx* ctx, const ntp_source* sources, int32_t n_sources, uint64_t seed,
+                         const ntp_prop_opts* opts, ntp_hit* hits, uint64_t capacity, int32_t hits_on_device,
+                         uint64_t* n_hits, uint64_t* n_photons_simulated) {
+    if (!ctx) return NTP_ERR_INVALID;
+    if (!ctx->have_medium || !ctx->have_spec || !ctx->have_targets) {
+        ctx->err = "ntp_propagate: medium, spectrum and targets must be set first";
+        return NTP_ERR_NOT_READY;
+    }
+    if (n_sources < 0 || (n_sources > 0 && !sources)) return invalid(ctx, "ntp_propagate: bad source array");
+    if (capacity > 0 && !hits) return invalid(ctx, "ntp_propagate: hits is NULL with capacity > 0");
+    ntp_prop_opts o{15, NTP_HIT_FIRST_IN_LIST, 0, 0, nullptr};
+    if (opts) o = *opts;
+    if (o.max_steps < 1 || o.max_steps > (1 << 24)) return invalid(ctx, "ntp_propagate: max_steps out of range");
+    if (o.hit_policy != NTP_HIT_FIRST_IN_LIST && o.hit_policy != NTP_HIT_NEAREST)
+        return invalid(ctx, "ntp_propagate: unknown hit_policy");
+    if (hits_on_device && (reinterpret_cast<uintptr_t>(hits) & 15u))
+        return invalid(ctx, "ntp_propagate: device hit buffer must be 16-byte aligned");
+
+    std::vector<unsigned long long> prefix(static_cast<size_t>(n_sources) + 1, 0);
+    for (int i = 0; i < n_sources; ++i) {
+        const ntp_source& s = sources[i];
+        if (s.kind < NTP_SRC_POINT_ISOTROPIC || s.kind > NTP_SRC_CHERENKOV_TRACK)
+            return invalid(ctx, "ntp_propagate: source " + std::to_string(i) + " has an unknown kind");
+        if (s.kind == NTP_SRC_EXTENDED_CHERENKOV && s.photons > 0 &&
+            (!(s.long_a > 1.0f) || !(s.long_b > 0.0f) || !(s.long_lrad > 0.0f)))
+            return invalid(ctx, "ntp_propagate: extended source needs long_a > 1, long_b > 0, long_lrad > 0");
+        if (prefix[i] + s.photons < prefix[i]) return invalid(ctx, "ntp_propagate: photon count overflows");
+        prefix[i + 1] = prefix[i] + s.photons;
+    }
+    const unsigned long long total = prefix.back();
+    if (n_hits) *n_hits = 0;
+    if (n_photons_simulated) *n_photons_simulated = 0;
+    if (total == 0) return NTP_OK;
+
+    cudaSetDevice(ctx->device);
+    cudaStream_t st = hits_on_device ? pick_stream(ctx, o.stream) : ctx->stream;
+    void* src_buf = ctx->d_src;
+    NTP_CUDA(ctx, ensure(src_buf, ctx->src_cap, sizeof(ntp_source) * n_sources));
+    ctx->d_src = static_cast<ntp_source*>(src_buf);
+    void* pre_buf = ctx->d_prefix;
+    NTP_CUDA(ctx, ensure(pre_buf, ctx->prefix_cap, sizeof(unsigned long long) * prefix.size()));
+    ctx->d_prefix = static_cast<unsigned long long*>(pre_buf);
+    NTP_CUDA(ctx, cudaMemcpyAsync(ctx->d_src, sources, sizeof(ntp_source) * n_sources, cudaMemcpyHostToDevice, st));
+    NTP_CUDA(ctx, cudaMemcpyAsync(ctx->d_prefix, prefix.data(), sizeof(unsigned long long) * prefix.size(),
+                                  cudaMemcpyHostToDevice, st));
+    NTP_CUDA(ctx, cudaMemsetAsync(ctx->d_counters, 0, 4 * sizeof(unsigned long long), st));
+
+    ntp_hit* d_hits = hits;
+    if (!hits_on_device) {
+        NTP_CUDA(ctx, ensure(ctx->d_stage, ctx->stage_bytes, sizeof(ntp_hit) * std::max<uint64_t>(capacity, 1)));
+        d_hits = static_cast<ntp_hit*>(ctx->d_stage);
+    }
+
+    ntp::PropParams p{};
+    p.sources = ctx->d_src;
+    p.prefix = ctx->d_prefix;
+    p.n_src = n_sources;
+    p.total = total;
+    p.targets = ctx->d_tgt;
+    p.target_ids = ctx->d_tgt_id;
+    p.n_targets = ctx->n_tgt;
+    p.targets_in_smem = ctx->n_tgt <= ntp::kMaxSmemTargets ? 1 : 0;
+    p.medium = ctx->d_med;
+    p.n_medium = ctx->n_med;
+    p.wl_min = ctx->wl_min;
+    p.medium_scale = static_cast<float>(ctx->n_med - 1) / (ctx->wl_max - ctx->wl_min);
+    p.spec_kind = ctx->spec_kind;
+    p.n_spec = ctx->n_spec;
+    p.spec_knots = ctx->d_spec;
+    p.spec_p0 = ctx->spec_p0;
+    p.spec_p1 = ctx->spec_p1;
+    p.hg_g = ctx->hg_g;
+    p.rayleigh_fraction = ctx->f_ray;
+    p.max_steps = o.max_steps;
+    p.hit_policy = o.hit_policy;
+    p.exact_pole = (o.flags & NTP_FLAG_EXACT_POLE_ROTATION) ? 1 : 0;
+    p.key = make_uint2(static_cast<uint32_t>(seed), static_cast<uint32_t>(seed >> 32));
+    p.hits = d_hits;
+    p.capacity = capacity;
+    p.counters = ctx->d_counters;
+
+    int per_sm = 0;
+    NTP_CUDA(ctx, ntp::propagate_occupancy(p, &per_sm));
+    if (per_sm < 1) {
+        ctx->err = "ntp_propagate: kernel does not fit on an SM (too many targets or knots)";
+        return NTP_ERR_INVALID;
+    }
+    const int grid = per_sm * ctx->num_sms;
+    const unsigned long long warps = static_cast<unsigned long long>(grid) * (ntp::kPropBlock / 32);
+    unsigned long long chunk = total / (warps * 8);
+    chunk = std::max<unsigned long long>(32, std::min<unsigned long long>(4096, chunk));
+    p.chunk = (chunk + 31) / 32 * 32;
+
+    NTP_CUDA(ctx, ntp::launch_propagate(p, grid, st));
+    NTP_CUDA(ctx, cudaMemcpyAsync(ctx->h_counters, ctx->d_counters, 4 * sizeof(unsigned long long),
+                                  cudaMemcpyDeviceToHost, st));
+    NTP_CUDA(ctx, cudaStreamSynchronize(st));
+    const unsigned long long nh = ctx->h_counters[1];
+    if (!hits_on_device && nh > 0 && capacity > 0) {
+        const unsigned long long ncopy = std::min<unsigned long long>(nh, capacity);
+        NTP_CUDA(ctx, cudaMemcpyAsync(hits, d_hits, sizeof(ntp_hit) * ncopy, cudaMemcpyDeviceToHost, st));
+        NTP_CUDA(ctx, cudaStreamSynchronize(st));
+    }
+    if (n_hits) *n_hits = nh;
+    if (n_photons_simulated) *n_photons_simulated = ctx->h_counters[2];
+    ctx->stats.photons = ctx->h_counters[2];
+    ctx->stats.hits = nh;
+    ctx->stats.photon_steps = ctx->h_counters[3];
+    ctx->stats.grid = grid;
+    ctx->stats.block = ntp::kPropBlock;
+    ctx->stats.chunk = p.chunk;
+    if (nh > capacity) {
+        ctx->err = "ntp_propagate: hit buffer overflow (" + std::to_string(nh) + " hits, capacity " +
+                   std::to_string(capacity) + ")";
+        return NTP_ERR_OVERFLOW;
+    }
+    return NTP_OK;
+}
+
+ntp_status ntp_get_run_stats(const ntp_ctx* ctx, ntp_run_stats* out) {
+    if (!ctx || !out) return NTP_ERR_INVALID;
+    *out = ctx->stats;
+    return NTP_OK;
+}
+
+static ntp_status stage_hits(ntp_ctx* ctx, const ntp_hit* hits, uint64_t n, int on_device, cudaStream_t st,
+                             const ntp_hit** d_hits) {
+    if (on_device) {
+        *d_hits = hits;
+        return NTP_OK;
+    }
+    NTP_CUDA(ctx, ensure(ctx->d_stage, ctx->stage_bytes, sizeof(ntp_hit) * n));
+    NTP_CUDA(ctx, cudaMemcpyAsync(ctx->d_stage, hits, sizeof(ntp_hit) * n, cudaMemcpyHostToDevice, st));
+    *d_hits = static_cast<const ntp_hit*>(ctx->d_stage);
+    return NTP_OK;
+}
+
+ntp_status ntp_make_hits(ntp_ctx* ctx, const ntp_hit* hits, uint64_t n, const double orientation[9],
+                         int32_t* pmt_id, int32_t on_device, void* stream) {
+    if (!ctx) return NTP_ERR_INVALID;
+    if (!ctx->have_targets) {
+        ctx->err = "ntp_make_hits: targets must be set first";
+        return NTP_ERR_NOT_READY;
+    }
+    if (n == 0) return NTP_OK;
+    if (!hits || !pmt_id || !orientation) return invalid(ctx, "ntp_make_hits: NULL argument");
+    cudaSetDevice(ctx->device);
+    cudaStream_t st = on_device ? pick_stream(ctx, stream) : ctx->stream;
+    // PMT axes: orientation * sph_to_cart(theta, phi), the spherical step in
+    // float as the coordinates are Float32 (detection.jl:60-70)
+    const int npc = static_cast<int>(ctx->pmt_coords.size() / 2);
+    if (npc > 0) {
+        std::vector<double> axes(3 * static_cast<size_t>(npc));
+        for (int j = 0; j < npc; ++j) {
+            const float th = ctx->pmt_coords[2 * j], ph = ctx->pmt_coords[2 * j + 1];
+            const float s_t = sinf(th), c_t = cosf(th), s_p = sinf(ph), c_p = cosf(ph);
+            const double v[3] = {static_cast<double>(c_p * s_t), static_cast<double>(s_p * s_t),
+                                 static_cast<double>(c_t)};
+            for (int r = 0; r < 3; ++r)
+                axes[3 * j + r] = orientation[3 * r] * v[0] + orientation[3 * r + 1] * v[1] + orientation[3 * r + 2] * v[2];
+        }
+        NTP_CUDA(ctx, cudaMemcpyAsync(ctx->d_axes, axes.data(), sizeof(double) * axes.size(),
+                                      cudaMemcpyHostToDevice, st));
+        NTP_CUDA(ctx, cudaStreamSynchronize(st));
+    }
+    const ntp_hit* d_hits = nullptr;
+    ntp_status s = stage_hits(ctx, hits, n, on_device, st, &d_hits);
+    if (s != NTP_OK) return s;
+    int32_t* d_out = pmt_id;
+    if (!on_device) {
+        NTP_CUDA(ctx, ensure(ctx->d_stage2, ctx->stage2_bytes, sizeof(int32_t) * n));
+        d_out = static_cast<int32_t*>(ctx->d_stage2);
+    }
+    NTP_CUDA(ctx, ntp::launch_make_hits(hit_table(ctx), d_hits, n, ctx->d_axes, d_out, st));
+    if (!on_device) {
+        NTP_CUDA(ctx, cudaMemcpyAsync(pmt_id, d_out, sizeof(int32_t) * n, cudaMemcpyDeviceToHost, st));
+    }
+    NTP_CUDA(ctx, cudaStreamSynchronize(st));
+    return NTP_OK;
+}
+
+ntp_status ntp_calc_total_weight(ntp_ctx* ctx, const ntp_hit* hits, uint64_t n, double* area_acc, double* wl_acc,
+                                 double* abs_weight, double* total, int32_t on_device, void* stream) {
+    if (!ctx) return NTP_ERR_INVALID;
+    if (!ctx->have_targets || !ctx->have_medium || ctx->n_acc < 2) {
+        ctx->err = "ntp_calc_total_weight: targets, medium and wavelength acceptance must be set first";
+        return NTP_ERR_NOT_READY;
+    }
+    if (n == 0) return NTP_OK;
+    if (!hits) return invalid(ctx, "ntp_calc_total_weight: hits is NULL");
+    cudaSetDevice(ctx->device);
+    cudaStream_t st = on_device ? pick_stream(ctx, stream) : ctx->stream;
+    const ntp_hit* d_hits = nullptr;
+    ntp_status s = stage_hits(ctx, hits, n, on_device, st, &d_hits);
+    if (s != NTP_OK) return s;
+    double* outs[4] = {area_acc, wl_acc, abs_weight, total};
+    double* d_outs[4] = {area_acc, wl_acc, abs_weight, total};
+    if (!on_device) {
+        NTP_CUDA(ctx, ensure(ctx->d_stage2, ctx->stage2_bytes, 4 * sizeof(double) * n));
+        for (int k = 0; k < 4; ++k) d_outs[k] = outs[k] ? static_cast<double*>(ctx->d_stage2) + k * n : nullptr;
+    }
+    NTP_CUDA(ctx, ntp::launch_total_weight(hit_table(ctx), d_hits, n, ctx->d_abs_wl, ctx->d_abs_len, ctx->n_abs,
+                                           ctx->d_acc_wl, ctx->d_acc, ctx->n_acc, d_outs[0], d_outs[1],
+                                           d_outs[2], d_outs[3], st));
+    if (!on_device)
+        for (int k = 0; k < 4; ++k)
+            if (outs[k])
+                NTP_CUDA(ctx, cudaMemcpyAsync(outs[k], d_outs[k], sizeof(double) * n, cudaMemcpyDeviceToHost, st));
+    NTP_CUDA(ctx, cudaStreamSynchronize(st));
+    return NTP_OK;
+}
+
+ntp_status ntp_calc_time_residual(ntp_ctx* ctx, const ntp_hit* hits, uint64_t n, const float src[3], float n800,
+                                  double* tres, int32_t on_device, void* stream) {
+    if (!ctx) return NTP_ERR_INVALID;
+    if (!ctx->have_targets) {
+        ctx->err = "ntp_calc_time_residual: targets must be set first";
+        return NTP_ERR_NOT_READY;
+    }
+    if (n == 0) return NTP_OK;
+    if (!hits || !tres || !src) return invalid(ctx, "ntp_calc_time_residual: NULL argument");
+    if (!(n800 > 0.0f)) return invalid(ctx, "ntp_calc_time_residual: n800 must be > 0");
+    cudaSetDevice(ctx->device);
+    cudaStream_t st = on_device ? pick_stream(ctx, stream) : ctx->stream;
+    // tgeo per module, photon_prop_cuda.jl:913-914
+    std::vector<double> tgeo(ctx->n_tgt);
+    const double c_vac = 0.299792458;
+    for (int k = 0; k < ctx->n_tgt; ++k) {
+        const ntp_target& t = ctx->targets[k];
+        const float dx = src[0] - t.position[0], dy = src[1] - t.position[1], dz = src[2] - t.position[2];
+        const float distance = std::sqrt(dx * dx + dy * dy + dz * dz);
+        tgeo[k] = static_cast<double>(distance - t.radius) / (c_vac / static_cast<double>(n800));
+    }
+    NTP_CUDA(ctx, cudaMemcpyAsync(ctx->d_tgeo, tgeo.data(), sizeof(double) * tgeo.size(), cudaMemcpyHostToDevice, st));
+    const ntp_hit* d_hits = nullptr;
+    ntp_status s = stage_hits(ctx, hits, n, on_device, st, &d_hits);
+    if (s != NTP_OK) return s;
+    double* d_out = tres;
+    if (!on_device) {
+        NTP_CUDA(ctx, ensure(ctx->d_stage2, ctx->stage2_bytes, sizeof(double) * n));
+        d_out = static_cast<double*>(ctx->d_stage2);
+    }
+    NTP_CUDA(ctx, ntp::launch_time_residual(hit_table(ctx), d_hits, n, ctx->d_tgeo, d_out, st));
+    if (!on_device) NTP_CUDA(ctx, cudaMemcpyAsync(tres, d_out, sizeof(double) * n, cudaMemcpyDeviceToHost, st));
+    NTP_CUDA(ctx, cudaStreamSynchronize(st));
+    return NTP_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,146 @@
+// ntp_device.cuh -- device-side building blocks of the photon step law.
+//
+// Each function restates one piece of the reference (chrhck/NeutrinoTelescopes,
+// file:line given) for sm_103a in single precision.  Where the reference's
+// float arithmetic is ill-conditioned (sin of a scattering angle near the
+// forward pole computed as sqrt(1 - cos^2)), the same quantity is evaluated
+// in an algebraically identical, well-conditioned form; results agree with
+// the double-precision oracle instead of inheriting float cancellation.
+#pragma once
+
+#include <cstdint>
+#include <cuda_runtime.h>
+
+#include "../../include/ntp.h"
+
+namespace ntp {
+
+constexpr float kCVac = 0.299792458f;        // m/ns
+constexpr float kInvCVac = 3.3356409519815204f;  // ns/m
+constexpr unsigned kFull = 0xffffffffu;
+
+// Philox block indices (the "draw" word of the counter).  Photon k of source
+// s uses counter (draw, k_lo, k_hi, s) under key = seed.
+constexpr uint32_t kDrawInitA = 0;   // x: wavelength, y: azimuth, z: polar (isotropic), w: time / track position
+constexpr uint32_t kDrawInitB = 1;   // x: track-direction cos, y: track-direction azimuth
+constexpr uint32_t kDrawGamma0 = 2;  // attempt k of the gamma sampler: x, y -> normal, z -> accept
+constexpr int kGammaAttempts = 32;
+constexpr uint32_t kDrawStep0 = 64;  // step j: x: length, y: scatter cos, z: scatter azimuth, w: Rayleigh select
+
+// Philox4x32-10 (Salmon et al., SC'11).
+__device__ __forceinline__ uint4 philox4x32_10(uint4 c, uint2 k) {
+#pragma unroll
+    for (int r = 0; r < 10; ++r) {
+        if (r) {
+            k.x += 0x9E3779B9u;
+            k.y += 0xBB67AE85u;
+        }
+        const uint32_t lo0 = 0xD2511F53u * c.x, hi0 = __umulhi(0xD2511F53u, c.x);
+        const uint32_t lo1 = 0xCD9E8D57u * c.z, hi1 = __umulhi(0xCD9E8D57u, c.z);
+        c = make_uint4(hi1 ^ c.y ^ k.x, lo1, hi0 ^ c.w ^ k.y, lo0);
+    }
+    return c;
+}
+
+// Top 23 bits plus one half, times 2^-23: uniform on the open interval (0, 1),
+// exact in float; 1 - u01(w) is exact too.
+__device__ __forceinline__ float u01(uint32_t w) {
+    return (static_cast<float>(w >> 9) + 0.5f) * (1.0f / 8388608.0f);
+}
+
+struct V3 {
+    float x, y, z;
+};
+
+// rot_from_ez_fast, utils.jl:228-243: the rotation taking e_z to a, applied
+// to o.  At |a_z| == 1 the reference returns (o1, copysign(o2,a3),
+// copysign(o3,a3)); exact_pole switches to the true rotation there.
+__device__ __forceinline__ V3 rot_from_ez(V3 a, V3 o, bool exact_pole) {
+    if (fabsf(a.z) == 1.0f) {
+        if (exact_pole) return V3{o.x, a.z * o.y, a.z * o.z};
+        return V3{o.x, copysignf(o.y, a.z), copysignf(o.z, a.z)};
+    }
+    const float a1sq = a.x * a.x, a2sq = a.y * a.y;
+    const float fact = __fdividef(1.0f - a.z, a2sq + a1sq);
+    const float a1a2 = a.x * a.y;
+    V3 r;
+    r.x = fmaf(-a1sq, fact, 1.0f) * o.x - a1a2 * fact * o.y + a.x * o.z;
+    r.y = -a1a2 * fact * o.x + fmaf(-a2sq, fact, 1.0f) * o.y + a.y * o.z;
+    r.z = -a.x * o.x - a.y * o.y + a.z * o.z;
+    return r;
+}
+
+// Linear interpolation in a uniform table of float4 knots.
+__device__ __forceinline__ float4 interp_table(const float4* t, int n, float x0, float scale, float x) {
+    float pos = fminf(fmaxf((x - x0) * scale, 0.0f), static_cast<float>(n - 1));
+    int i = min(static_cast<int>(pos), n - 2);
+    const float f = pos - static_cast<float>(i);
+    const float4 a = t[i], b = t[i + 1];
+    return make_float4(fmaf(f, b.x - a.x, a.x), fmaf(f, b.y - a.y, a.y), fmaf(f, b.z - a.z, a.z),
+                       fmaf(f, b.w - a.w, a.w));
+}
+
+struct SpectrumView {
+    int kind;
+    int n;
+    const float* knots;  // shared memory
+    float p0, p1;        // INV_SQUARE: 1/wl_min, 1/wl_min - 1/wl_max ; MONOCHROMATIC: p0 = wavelength
+};
+
+// initialize_wavelength, photon_prop_cuda.jl:128-130 (the texture fetch of
+// spectrum.jl:102-103 is emulated in NTP_SPEC_TABLE_TEXTURE).
+__device__ __forceinline__ float sample_wavelength(const SpectrumView& s, float u) {
+    switch (s.kind) {
+    case NTP_SPEC_MONOCHROMATIC:
+        return s.p0;
+    case NTP_SPEC_TABLE_LINEAR: {
+        const float x = u * static_cast<float>(s.n - 1);
+        const int i = min(static_cast<int>(x), s.n - 2);
+        const float f = x - static_cast<float>(i);
+        const float k0 = s.knots[i], k1 = s.knots[i + 1];
+        return fmaf(f, k1 - k0, k0);
+    }
+    case NTP_SPEC_TABLE_TEXTURE: {
+        const float xb = fmaf(u, static_cast<float>(s.n), -0.5f);
+        const float fl = floorf(xb);
+        const int i = static_cast<int>(fl);
+        const float a = rintf((xb - fl) * 256.0f) * (1.0f / 256.0f);
+        const int i0 = min(max(i, 0), s.n - 1), i1 = min(max(i + 1, 0), s.n - 1);
+        return (1.0f - a) * s.knots[i0] + a * s.knots[i1];
+    }
+    default:  // NTP_SPEC_INV_SQUARE
+        return 1.0f / fmaf(-u, s.p1, s.p0);
+}
+}
+
+// One minus the Henyey-Greenstein cosine (cuda_hg_scattering_func,
+// photon_prop_cuda.jl:70-77).  With D = 1 + g(2 eta - 1), t = (1 - g^2)/D:
+//   cos = (1 + g^2 - t^2) / 2g    and    1 - cos = (1-g)(1-eta)(t + 1 - g) / D,
+// the second form keeps full relative precision for forward scatters.
+__device__ __forceinline__ float hg_one_minus_cos(float g, float one_m_g, float one_m_g2, float eta) {
+    const float D = fmaf(g, fmaf(2.0f, eta, -1.0f), 1.0f);
+    const float invD = 1.0f / D;
+    const float t = one_m_g2 * invD;
+    const float omc = one_m_g * (1.0f - eta) * (t + one_m_g) * invD;
+    return fminf(fmaxf(omc, 0.0f), 2.0f);
+}
+
+// Rayleigh (3/8)(1 + mu^2): exact CDF inverse, mu^3 + 3 mu = 8u - 4, by
+// Cardano in the form mu = sign(q)(A - 1/A), A = cbrt(|q| + sqrt(q^2 + 1)).
+__device__ __forceinline__ float rayleigh_cos(float u) {
+    const float q = fmaf(4.0f, u, -2.0f);
+    const float A = cbrtf(fabsf(q) + sqrtf(fmaf(q, q, 1.0f)));
+    const float mu = A - 1.0f / A;
+    return copysignf(mu, q);
+}
+
+// Direction from (1 - cos theta) and an azimuth uniform, as
+// sph_to_cart (utils.jl:105-115) with sin theta = sqrt(omc (2 - omc)).
+__device__ __forceinline__ V3 dir_from_omc(float omc, float u_phi) {
+    float sp, cp;
+    sincospif(2.0f * u_phi, &sp, &cp);
+    const float st = sqrtf(omc * (2.0f - omc));
+    return V3{cp * st, sp * st, 1.0f - omc};
+}
+
+}  // namespace ntp

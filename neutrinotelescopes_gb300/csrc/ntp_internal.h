@@ -1,0 +1,80 @@
+// ntp_internal.h -- shared declarations between the C ABI layer and the
+// kernels of libntp.so.  Not part of the public interface.
+#pragma once
+
+#include <cstdint>
+#include <string>
+#include <vector>
+
+#include <cuda_runtime.h>
+
+#include "../../include/ntp.h"
+
+namespace ntp {
+
+constexpr int kPropBlock = 256;      // threads per block of the propagation kernel
+constexpr int kMaxSmemTargets = 8192;  // targets staged in shared memory (20 B each)
+
+// Everything one launch of the propagation kernel reads.
+struct PropParams {
+    const ntp_source* sources;            // device
+    const unsigned long long* prefix;     // device, n_src + 1 exclusive photon offsets
+    int n_src;
+    unsigned long long total;             // photons over all sources
+
+    const float4* targets;                // device, (x, y, z, r^2)
+    const uint32_t* target_ids;           // device, module_id per target
+    int n_targets;
+    int targets_in_smem;                  // stage targets in shared memory
+
+    const float4* medium;                 // device, per knot (n, v_group, l_scatter, 0)
+    int n_medium;
+    float wl_min;
+    float medium_scale;                   // (n_medium - 1) / (wl_max - wl_min)
+
+    int spec_kind;
+    int n_spec;
+    const float* spec_knots;              // device
+    float spec_p0, spec_p1;
+
+    float hg_g;
+    float rayleigh_fraction;
+    int max_steps;
+    int hit_policy;
+    int exact_pole;
+    uint2 key;
+
+    ntp_hit* hits;                        // device
+    unsigned long long capacity;
+    unsigned long long* counters;         // device: [0] photons claimed, [1] hits, [2] photons done, [3] photon-steps
+    unsigned long long chunk;             // photons a warp claims at once
+};
+
+size_t prop_smem_bytes(const PropParams& p);
+cudaError_t launch_propagate(const PropParams& p, int grid, cudaStream_t stream);
+cudaError_t propagate_occupancy(const PropParams& p, int* blocks_per_sm);
+
+// Hit post-processing (make_hits / weights / time residual).
+struct HitTargetTable {
+    const uint2* sorted_ids;   // (module_id, target index), ascending module_id
+    int n_targets;
+    const float4* targets;     // (x, y, z, r^2)
+    const float* radius;       // float radius per target
+    const int* kind;           // ntp_target_kind per target
+    const int* n_pmts;
+    const int* pmt_offset;
+    const double* opening;     // PMT opening angle (rad) per target
+    const double* area_acc;    // area acceptance per target
+};
+
+cudaError_t launch_make_hits(const HitTargetTable& t, const ntp_hit* hits, unsigned long long n,
+                             const double* pmt_axes, int32_t* pmt_id, cudaStream_t stream);
+cudaError_t launch_total_weight(const HitTargetTable& t, const ntp_hit* hits, unsigned long long n,
+                                const float* abs_wl, const float* abs_len, int n_abs,
+                                const double* acc_wl, const double* acc, int n_acc,
+                                double* area_acc, double* wl_acc, double* abs_weight,
+                                double* total, cudaStream_t stream);
+cudaError_t launch_time_residual(const HitTargetTable& t, const ntp_hit* hits, unsigned long long n,
+                                 const double* tgeo, double* tres, cudaStream_t stream);
+
+}  // namespace ntp

@@ -1,0 +1,318 @@
+// propagate.cu -- the photon propagation kernel.
+//
+// Replaces cuda_propagate_photons! (chrhck/NeutrinoTelescopes,
+// src/photon_propagation/photon_prop_cuda.jl:402-506) and its launch loop
+// (:726-759).  Design for sm_103a:
+//   * persistent grid (a multiple of the SM count); each warp claims chunks of
+//     photon indices from a global counter and keeps its 32 lanes busy: a lane
+//     whose photon ended (hit or step cap) takes the next index of the chunk
+//     before the next step, so lanes never idle behind a long photon;
+//   * all randoms come from Philox4x32-10 in registers, one block per step,
+//     keyed by (draw, photon, source) so any photon can be replayed;
+//   * medium table, spectrum knots and targets sit in shared memory;
+//   * hits are written through one atomic per warp (ballot + popc) into an
+//     array of 64-byte records with 16-byte vector stores; the hit counter
+//     keeps counting past the capacity so the caller learns the exact size.
+#include <cuda_runtime.h>
+
+#include "ntp_device.cuh"
+#include "ntp_internal.h"
+
+namespace ntp {
+
+namespace {
+
+struct Photon {
+    V3 pos, dir, init_dir;
+    float time, wl, dist, sca_len, inv_vg;
+    uint32_t src;
+    uint32_t pk_lo, pk_hi;  // photon index within its source
+    int step;
+};
+
+__device__ __forceinline__ int source_of(const unsigned long long* prefix, int n_src,
+                                         unsigned long long gid) {
+    int lo = 0, hi = n_src - 1;
+    while (lo < hi) {
+        const int mid = (lo + hi + 1) >> 1;
+        if (__ldg(prefix + mid) <= gid) lo = mid;
+        else hi = mid - 1;
+    }
+    return lo;
+}
+
+// rand_gamma(shape, scale), utils.jl:267-294 (Marsaglia-Tsang, shape > 1),
+// the normal from Box-Muller on Philox words; at most kGammaAttempts tries.
+__device__ __noinline__ float rand_gamma(float shape, float scale, uint4 ctr, uint2 key) {
+    const float d = static_cast<float>(static_cast<double>(shape) - 1.0 / 3.0);
+    const float c = 1.0f / sqrtf(9.0f * d);
+    for (int k = 0; k < kGammaAttempts; ++k) {
+        ctr.x = kDrawGamma0 + static_cast<uint32_t>(k);
+        const uint4 r = philox4x32_10(ctr, key);
+        float s, cs;
+        sincospif(2.0f * u01(r.y), &s, &cs);
+        const float x = sqrtf(-2.0f * logf(u01(r.x))) * cs;
+        float v = fmaf(c, x, 1.0f);
+        if (v <= 0.0f) continue;
+        v = v * v * v;
+        const float u = u01(r.z);
+        const float xsq = x * x;
+        // the squeeze 1 - (1 + 0.0331 x^4) is never above u (utils.jl:286)
+        if (logf(u) < 0.5f * xsq + d * (1.0f - v + logf(v))) return d * v * scale;
+    }
+    return d * scale;
+}
+
+// initialize_photon_state methods, photon_prop_cuda.jl:133-200 and
+// sample_cherenkov_direction :107-125.
+__device__ __forceinline__ void init_photon(Photon& ph, const ntp_source* __restrict__ sources,
+                                         const PropParams& p, const SpectrumView& spec,
+                                         const float4* medium, unsigned long long gid, int s) {
+    const ntp_source* src = sources + s;
+    const unsigned long long pk = gid - __ldg(p.prefix + s);
+    ph.src = static_cast<uint32_t>(s);
+    ph.pk_lo = static_cast<uint32_t>(pk);
+    ph.pk_hi = static_cast<uint32_t>(pk >> 32);
+    const uint4 base = make_uint4(kDrawInitA, ph.pk_lo, ph.pk_hi, ph.src);
+    const uint4 A = philox4x32_10(base, p.key);
+
+    const int kind = __ldg(&src->kind);
+    ph.wl = sample_wavelength(spec, u01(A.x));
+    ph.pos = V3{__ldg(&src->position[0]), __ldg(&src->position[1]), __ldg(&src->position[2])};
+    ph.time = __ldg(&src->time);
+    const V3 sdir{__ldg(&src->direction[0]), __ldg(&src->direction[1]), __ldg(&src->direction[2])};
+    const float4 med = interp_table(medium, p.n_medium, p.wl_min, p.medium_scale, ph.wl);
+    bool cherenkov = false;
+
+    switch (kind) {
+    case NTP_SRC_POINT_ISOTROPIC:
+    case NTP_SRC_POINT_TIME_RANGE: {  // initialize_direction_isotropic :100-104
+        const float u = u01(A.z);     // cos = 2u - 1, 1 - cos = 2(1 - u)
+        ph.dir = dir_from_omc(2.0f * (1.0f - u), u01(A.y));
+        if (kind == NTP_SRC_POINT_TIME_RANGE) {
+            const float t1 = __ldg(&src->time_end);
+            ph.time = ph.time + u01(A.w) * (t1 - ph.time);
+        }
+        break;
+    }
+    case NTP_SRC_AXICONE: {  // :148-156
+        float st, ct, sp, cp;
+        sincosf(__ldg(&src->angle), &st, &ct);
+        sincospif(2.0f * u01(A.y), &sp, &cp);
+        ph.dir = rot_from_ez(sdir, V3{cp * st, sp * st, ct}, p.exact_pole);
+        break;
+    }
+    case NTP_SRC_PENCIL:  // :158-161
+        ph.dir = sdir;
+        break;
+    case NTP_SRC_EXTENDED_CHERENKOV: {  // :164-176
+        const float b = __ldg(&src->long_b);
+        const float long_pos =
+            rand_gamma(__ldg(&src->long_a), 1.0f / b, base, p.key) * __ldg(&src->long_lrad);
+        ph.pos = V3{fmaf(long_pos, sdir.x, ph.pos.x), fmaf(long_pos, sdir.y, ph.pos.y),
+                    fmaf(long_pos, sdir.z, ph.pos.z)};
+        ph.time = fmaf(long_pos, kInvCVac, ph.time);
+        cherenkov = true;
+        break;
+    }
+    case NTP_SRC_CHERENKOV_TRACK: {  // :190-200, direction as :178-188
+        const float along = u01(A.w) * __ldg(&src->length);
+        ph.pos = V3{fmaf(along, sdir.x, ph.pos.x), fmaf(along, sdir.y, ph.pos.y),
+                    fmaf(along, sdir.z, ph.pos.z)};
+        ph.time = fmaf(along, kInvCVac, ph.time);
+        cherenkov = true;
+        break;
+    }
+    default:  // NTP_SRC_POINT_CHERENKOV :178-188
+        cherenkov = true;
+        break;
+    }
+    if (cherenkov) {
+        // photon on the Cherenkov cone cos = 1/n(lambda) (medium.jl:309-311)
+        const float cos_c = 1.0f / med.x;
+        float sp, cp;
+        sincospif(2.0f * u01(A.y), &sp, &cp);
+        const float sin_c = sqrtf(fmaf(-cos_c, cos_c, 1.0f));
+        V3 d{cp * sin_c, sp * sin_c, cos_c};
+        // track smearing, sample_cherenkov_track_direction utils.jl:249-260:
+        // 1 - cos = (-log(1 - u I)/b)^(1/a), a = 0.39, b = 2.61
+        const uint4 B = philox4x32_10(make_uint4(kDrawInitB, ph.pk_lo, ph.pk_hi, ph.src), p.key);
+        const float I = 0.96729171f;  // 1 - exp(-2.61 * 2^0.39)
+        const float omc = fminf(powf(-log1pf(-u01(B.x) * I) * (1.0f / 2.61f),
+                                     1.0f / 0.39f),
+                                2.0f);
+        const V3 track = dir_from_omc(omc, u01(B.y));
+        d = rot_from_ez(track, d, p.exact_pole);
+        ph.dir = rot_from_ez(sdir, d, p.exact_pole);
+    }
+    ph.init_dir = ph.dir;
+    ph.dist = 0.0f;
+    ph.sca_len = med.z;
+    ph.inv_vg = 1.0f / med.y;
+    ph.step = 0;
+}
+
+__global__ void __launch_bounds__(kPropBlock, 3) propagate_kernel(const PropParams p) {
+    extern __shared__ float4 smem[];
+    float4* s_med = smem;
+    float4* s_tgt = s_med + p.n_medium;
+    uint32_t* s_tid = reinterpret_cast<uint32_t*>(s_tgt + (p.targets_in_smem ? p.n_targets : 0));
+    float* s_spec = reinterpret_cast<float*>(s_tid + (p.targets_in_smem ? p.n_targets : 0));
+
+    for (int i = threadIdx.x; i < p.n_medium; i += blockDim.x) s_med[i] = p.medium[i];
+    for (int i = threadIdx.x; i < p.n_spec; i += blockDim.x) s_spec[i] = p.spec_knots[i];
+    if (p.targets_in_smem) {
+        for (int i = threadIdx.x; i < p.n_targets; i += blockDim.x) {
+            s_tgt[i] = p.targets[i];
+            s_tid[i] = p.target_ids[i];
+        }
+    }
+    __syncthreads();
+    const float4* tg = p.targets_in_smem ? s_tgt : p.targets;
+    const uint32_t* tid = p.targets_in_smem ? s_tid : p.target_ids;
+
+    SpectrumView spec{p.spec_kind, p.n_spec, s_spec, p.spec_p0, p.spec_p1};
+    const float g = p.hg_g, one_m_g = 1.0f - g, one_m_g2 = fmaf(-g, g, 1.0f);
+    const unsigned lane = threadIdx.x & 31u;
+    const unsigned lt_mask = (1u << lane) - 1u;
+
+    unsigned long long c_next = 0, c_end = 0;  // warp-uniform chunk of photon indices
+    bool exhausted = false;
+    bool active = false;
+    unsigned long long done = 0, steps = 0;
+    Photon ph;
+
+    for (;;) {
+        const unsigned idle = __ballot_sync(kFull, !active);
+        if (idle && !exhausted) {
+            unsigned long long avail = c_end - c_next;
+            if (avail == 0) {
+                unsigned long long base = 0;
+                if (lane == 0) base = atomicAdd(p.counters, p.chunk);
+                base = __shfl_sync(kFull, base, 0);
+                if (base >= p.total) {
+                    exhausted = true;
+                } else {
+                    c_next = base;
+                    c_end = min(base + p.chunk, p.total);
+                    avail = c_end - c_next;
+                }
+            }
+            if (avail) {
+                const unsigned long long take = min(static_cast<unsigned long long>(__popc(idle)), avail);
+                const unsigned rank = __popc(idle & lt_mask);
+                if (!active && rank < take) {
+                    const unsigned long long gid = c_next + rank;
+                    init_photon(ph, p.sources, p, spec, s_med, gid, source_of(p.prefix, p.n_src, gid));
+                    active = true;
+                }
+                c_next += take;
+            }
+        }
+        if (!__any_sync(kFull, active)) break;
+
+        bool hit = false;
+        int hit_t = -1;
+        if (active) {
+            const uint4 r = philox4x32_10(
+                make_uint4(kDrawStep0 + static_cast<uint32_t>(ph.step), ph.pk_lo, ph.pk_hi, ph.src), p.key);
+            const float step = -logf(u01(r.x)) * ph.sca_len;
+            ++steps;
+
+            // check_intersection over the targets, photon_prop_cuda.jl:233-271, :460-468
+            float hit_d = step;
+            for (int t = 0; t < p.n_targets; ++t) {
+                const float4 T = tg[t];
+                const float dx = ph.pos.x - T.x, dy = ph.pos.y - T.y, dz = ph.pos.z - T.z;
+                const float a = ph.dir.x * dx + ph.dir.y * dy + ph.dir.z * dz;
+                const float pp = dx * dx + dy * dy + dz * dz;
+                const float b = fmaf(a, a, T.w - pp);
+                if (b >= 0.0f) {
+                    const float d = -a - sqrtf(b);
+                    if (d > 0.0f && d < step) {
+                        if (p.hit_policy == NTP_HIT_NEAREST) {
+                            if (d < hit_d) { hit_d = d; hit_t = t; }
+                        } else {
+                            hit_d = d;
+                            hit_t = t;
+                            break;
+                        }
+                    }
+                }
+            }
+            const float move = hit_t >= 0 ? hit_d : step;
+            ph.pos = V3{fmaf(ph.dir.x, move, ph.pos.x), fmaf(ph.dir.y, move, ph.pos.y),
+                        fmaf(ph.dir.z, move, ph.pos.z)};
+            ph.dist += move;
+            ph.time = fmaf(move, ph.inv_vg, ph.time);
+            if (hit_t >= 0) {
+                hit = true;
+            } else {
+                // update_direction, photon_prop_cuda.jl:204-222, phase function
+                // mixture Rayleigh / Henyey-Greenstein
+                const float eta = u01(r.y);
+                float omc;
+                if (u01(r.w) < p.rayleigh_fraction) omc = 1.0f - rayleigh_cos(eta);
+                else omc = hg_one_minus_cos(g, one_m_g, one_m_g2, eta);
+                ph.dir = rot_from_ez(ph.dir, dir_from_omc(omc, u01(r.z)), p.exact_pole);
+                if (++ph.step >= p.max_steps) {
+                    active = false;
+                    ++done;
+                }
+            }
+        }
+
+        const unsigned hm = __ballot_sync(kFull, hit);
+        if (hm) {
+            const int leader = __ffs(hm) - 1;
+            unsigned long long base = 0;
+            if (static_cast<int>(lane) == leader) base = atomicAdd(p.counters + 1, static_cast<unsigned long long>(__popc(hm)));
+            base = __shfl_sync(kFull, base, leader);
+            if (hit) {
+                const unsigned long long slot = base + __popc(hm & lt_mask);
+                if (slot < p.capacity) {
+                    float4* o = reinterpret_cast<float4*>(p.hits + slot);
+                    __stcs(o + 0, make_float4(ph.pos.x, ph.pos.y, ph.pos.z, ph.time));
+                    __stcs(o + 1, make_float4(ph.dir.x, ph.dir.y, ph.dir.z, ph.wl));
+                    __stcs(o + 2, make_float4(ph.init_dir.x, ph.init_dir.y, ph.init_dir.z, ph.dist));
+                    __stcs(reinterpret_cast<uint4*>(o + 3), make_uint4(tid[hit_t], ph.src, ph.pk_lo, ph.pk_hi));
+                }
+                active = false;
+                ++done;
+            }
+        }
+    }
+
+    // photons finished and photon-steps taken: one atomic per warp each
+    for (int off = 16; off > 0; off >>= 1) {
+        done += __shfl_down_sync(kFull, done, off);
+        steps += __shfl_down_sync(kFull, steps, off);
+    }
+    if (lane == 0 && done) atomicAdd(p.counters + 2, done);
+    if (lane == 0 && steps) atomicAdd(p.counters + 3, steps);
+}
+
+}  // namespace
+
+size_t prop_smem_bytes(const PropParams& p) {
+    size_t b = sizeof(float4) * static_cast<size_t>(p.n_medium);
+    if (p.targets_in_smem) b += (sizeof(float4) + sizeof(uint32_t)) * static_cast<size_t>(p.n_targets);
+    b += sizeof(float) * static_cast<size_t>(p.n_spec);
+    return b;
+}
+
+cudaError_t propagate_occupancy(const PropParams& p, int* blocks_per_sm) {
+    const size_t smem = prop_smem_bytes(p);
+    cudaError_t e = cudaFuncSetAttribute(propagate_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         static_cast<int>(smem));
+    if (e != cudaSuccess) return e;
+    return cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks_per_sm, propagate_kernel, kPropBlock, smem);
+}
+
+cudaError_t launch_propagate(const PropParams& p, int grid, cudaStream_t stream) {
+    const size_t smem = prop_smem_bytes(p);
+    propagate_kernel<<<grid, kPropBlock, smem, stream>>>(p);
+    return cudaGetLastError();
+}
+
+}  // namespace ntp

@@ -1,0 +1,57 @@
+"""Synthetic workloads of the benchmark and the tests, named by what they are.
+
+point_cone:      1e6 photons from the origin on a 41.2 degree cone around +z,
+                 1/lambda^2 spectrum on 300-600 nm, one 0.21 m sphere at
+                 (0, 0, 10 m), simple water (n 1.35, group index 1.39, absorption
+                 30 m at 400 nm, scattering 50 m, 0.85 HG(0.97) + 0.15 Rayleigh).
+cascade_string:  electromagnetic cascades, energy log-uniform 1e3-1e5 GeV,
+                 1.3e5 photons/GeV, gamma longitudinal profile a = 2 + 0.6 ln E,
+                 b = 0.63, radiation length 0.36 m, isotropic direction, vertex
+                 10 m from the string at a random azimuth and depth; a string of
+                 20 modules 15 m apart with 16 PMTs each (POM layout, 75 mm PMT
+                 diameter as the reference scripts use), PMT acceptance resampled
+                 to 31 knots on 300-600 nm; simple water.
+"""
+from __future__ import annotations
+
+import numpy as np
+
+from .detection import DetectionSphere, p_one_pmt_acc, string_of_modules
+from .lightyield import AxiconeEmitter, ExtendedCherenkovEmitter, LongitudinalParameterisation
+from .medium import make_simple_water
+from .photon_prop import PhotonPropSetup
+from .spectrum import InverseSquareSpectrum
+
+PMT_AREA = float(np.pi * (75e-3 / 2) ** 2)
+SEED_BASE = 0x5EED0000
+
+
+def point_cone_setup(photons: int = 1_000_000, **kw) -> PhotonPropSetup:
+    src = AxiconeEmitter((0.0, 0.0, 0.0), (0.0, 0.0, 1.0), 0.0, photons, float(np.deg2rad(41.2)))
+    tgt = DetectionSphere((0.0, 0.0, 10.0), 0.21, 16, PMT_AREA, 1)
+    return PhotonPropSetup([src], [tgt], make_simple_water(), InverseSquareSpectrum(300.0, 600.0), **kw)
+
+
+def cascade_sources(n: int, rng: np.random.Generator, e_min=1e3, e_max=1e5, photons_per_gev=1.3e5,
+                    string_z=(0.0, 285.0), distance=10.0, photon_scale=1.0):
+    out = []
+    for _ in range(n):
+        e = 10 ** rng.uniform(np.log10(e_min), np.log10(e_max))
+        ct = rng.uniform(-1, 1)
+        phi = rng.uniform(0, 2 * np.pi)
+        st = np.sqrt(1 - ct * ct)
+        direction = (st * np.cos(phi), st * np.sin(phi), ct)
+        az = rng.uniform(0, 2 * np.pi)
+        z = rng.uniform(string_z[0] + 50.0, string_z[1] - 50.0)
+        pos = (distance * np.cos(az), distance * np.sin(az), z)
+        lp = LongitudinalParameterisation(a=float(np.float32(2.0 + 0.6 * np.log(e))), b=0.63, lrad=0.36)
+        out.append(ExtendedCherenkovEmitter(pos, direction, 0.0, int(photons_per_gev * e * photon_scale), lp))
+    return out
+
+
+def cascade_string_setup(n_cascades: int = 4, seed: int = 1, photon_scale: float = 1.0, **kw) -> PhotonPropSetup:
+    rng = np.random.default_rng(seed)
+    targets = string_of_modules(20, 15.0, pmt_area=PMT_AREA)
+    srcs = cascade_sources(n_cascades, rng, photon_scale=photon_scale)
+    return PhotonPropSetup(srcs, targets, make_simple_water(), InverseSquareSpectrum(300.0, 600.0),
+                           wavelength_acceptance=p_one_pmt_acc.resampled(300.0, 600.0, 31), **kw)

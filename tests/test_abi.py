@@ -1,0 +1,62 @@
+"""The C ABI library: it loads without a GPU and exports every entry point
+include/ntp.h declares; the ctypes records match the header's sizes."""
+import ctypes as C
+import re
+from pathlib import Path
+
+import numpy as np
+import pytest
+
+from neutrinotelescopes_gb300 import _abi
+
+ROOT = Path(__file__).resolve().parents[1]
+
+
+def header_functions() -> set[str]:
+    text = (ROOT / "include" / "ntp.h").read_text()
+    text = re.sub(r"/\*.*?\*/", "", text, flags=re.S)
+    return set(re.findall(r"\b(ntp_[a-z_0-9]+)\s*\(", text))
+
+
+def test_header_matches_python_list():
+    assert header_functions() == set(_abi.EXPORTED)
+
+
+def test_library_exports_every_symbol():
+    lib = _abi.load_library()
+    for name in header_functions():
+        assert hasattr(lib, name), name
+    assert lib.ntp_abi_version() == _abi.NTP_ABI_VERSION
+
+
+def test_nm_lists_symbols():
+    import subprocess
+    out = subprocess.run(["nm", "-D", "--defined-only", str(_abi.LIB_PATH)], capture_output=True, text=True).stdout
+    exported = set(re.findall(r"\bT (ntp_\w+)", out))
+    assert header_functions() <= exported
+
+
+def test_record_layouts():
+    assert C.sizeof(_abi.NtpSource) == 64
+    assert C.sizeof(_abi.NtpTarget) == 48
+    assert _abi.HIT_DTYPE.itemsize == 64
+    assert _abi.HIT_DTYPE.fields["module_id"][1] == 48
+    assert _abi.HIT_DTYPE.fields["photon_index"][1] == 56
+    assert _abi.NtpSource.photons.offset == 32
+    assert _abi.NtpMediumDesc.hg_g.offset == 64
+
+
+def test_missing_library_fails_loudly(tmp_path):
+    with pytest.raises(RuntimeError, match="missing"):
+        _abi.load_library(tmp_path / "libntp.so")
+
+
+def test_create_without_gpu_reports_error():
+    import torch
+    if torch.cuda.is_available():
+        pytest.skip("a GPU is present")
+    lib = _abi.load_library()
+    ctx = C.c_void_p()
+    st = lib.ntp_create(0, C.byref(ctx))
+    assert st != _abi.NTP_OK and not ctx.value
+    assert lib.ntp_last_error(None)

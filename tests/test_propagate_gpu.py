@@ -1,0 +1,248 @@
+"""Parity of the CUDA propagation kernel with the CPU oracle, through the C ABI.
+
+Per-photon replay: the kernel and the double-precision oracle draw the same
+Philox stream, so every photon can be compared individually.  Tolerances:
+position, time and distance to 1e-4 relative (vector norm for positions),
+directions to 1e-4 absolute (unit vectors), wavelength to 1e-5 relative.
+A photon whose hit/miss decision falls within float rounding of the sphere
+edge or the step end can come out differently in float and double; at most
+0.5% of the hit photons (and at least 3 allowed) may differ in the set of
+hit photons.
+"""
+import ctypes as C
+import os
+
+import numpy as np
+import pytest
+
+import neutrinotelescopes_gb300 as nt
+from neutrinotelescopes_gb300 import _abi, workloads
+from neutrinotelescopes_gb300.photon_prop import pack_sources
+
+pytestmark = pytest.mark.gpu
+
+POS_RTOL = 1e-4
+DIR_ATOL = 1e-4
+WL_RTOL = 1e-5
+
+
+def gpu_hits(setup, seed=0):
+    h = nt.propagate_photons(setup, seed=seed, reference_columns=False)
+    return h.sorted_by_photon().records
+
+
+def compare_replay(g, o, min_hits=20):
+    assert len(o) >= min_hits, f"oracle found only {len(o)} hits"
+    kg = g["source_index"].astype(np.uint64) << np.uint64(40) | g["photon_index"]
+    ko = o["source_index"].astype(np.uint64) << np.uint64(40) | o["photon_index"]
+    common, ig, io = np.intersect1d(kg, ko, return_indices=True)
+    n_diff = len(kg) + len(ko) - 2 * len(common)
+    assert n_diff <= max(3, int(0.005 * len(ko))), f"{n_diff} photons differ in hit/miss out of {len(ko)}"
+    a, b = g[ig], o[io]
+    assert np.mean(a["module_id"] == b["module_id"]) >= 0.995
+    same = a["module_id"] == b["module_id"]
+    a, b = a[same], b[same]
+    dp = np.linalg.norm(a["position"].astype(np.float64) - b["position"], axis=1)
+    scale = np.maximum(np.linalg.norm(b["position"].astype(np.float64), axis=1), 1.0)
+    assert np.all(dp <= POS_RTOL * scale), f"max rel pos err {np.max(dp / scale):.3g}"
+    np.testing.assert_allclose(a["time"], b["time"], rtol=POS_RTOL, atol=1e-3)
+    np.testing.assert_allclose(a["dist_travelled"], b["dist_travelled"], rtol=POS_RTOL, atol=1e-4)
+    np.testing.assert_allclose(a["direction"], b["direction"], atol=DIR_ATOL, rtol=0)
+    np.testing.assert_allclose(a["initial_direction"], b["initial_direction"], atol=DIR_ATOL, rtol=0)
+    np.testing.assert_allclose(a["wavelength"], b["wavelength"], rtol=WL_RTOL)
+    return len(common)
+
+
+def iso_close_setup(photons=200_000, **kw):
+    src = nt.PointlikeIsotropicEmitter((0.0, 0.0, 0.0), 0.0, photons)
+    tgt = nt.DetectionSphere((0.0, 0.0, 5.0), 1.0, 16, workloads.PMT_AREA, 7)
+    return nt.PhotonPropSetup([src], [tgt], nt.make_simple_water(), nt.InverseSquareSpectrum(300.0, 600.0), **kw)
+
+
+def cascade_small_setup(photons=200_000, **kw):
+    m = nt.make_cascadia_medium_properties(0.99)
+    lp = nt.LongitudinalParameterisation.from_energy(1e4, m, nt.PEMinus)
+    src = nt.ExtendedCherenkovEmitter((4.0, 0.0, 140.0), (0.0, 0.6, 0.8), 0.0, photons, lp)
+    targets = nt.string_of_modules(20, 15.0, pmt_area=workloads.PMT_AREA)
+    return nt.PhotonPropSetup([src], targets, m, nt.CherenkovSpectrum((300.0, 800.0), 30, m), **kw)
+
+
+def mixed_setup(**kw):
+    srcs = [
+        nt.PencilEmitter((0.0, 0.0, -3.0), (0.0, 0.0, 1.0), 1.0, 30_000),
+        nt.PointlikeTimeRangeEmitter((0.5, 0.0, 0.0), (0.0, 20.0), 40_000),
+        nt.PointlikeCherenkovEmitter((0.0, -2.0, 0.0), (0.0, 0.8, 0.6), 0.0, 40_000),
+        nt.CherenkovTrackEmitter((1.0, 1.0, -5.0), (0.0, 0.0, 1.0), 0.0, 10.0, 40_000),
+        nt.AxiconeEmitter((0.0, 0.0, 0.0), (0.0, 0.0, 1.0), 0.0, 40_000, 0.7),
+    ]
+    targets = [nt.DetectionSphere((0.0, 0.0, 3.0), 0.8, 16, workloads.PMT_AREA, 11),
+               nt.DetectionSphere((0.0, 0.0, 6.0), 1.2, 16, workloads.PMT_AREA, 12),
+               nt.DetectionSphere((2.0, 1.0, 2.0), 0.7, 16, workloads.PMT_AREA, 13)]
+    m = nt.make_cascadia_medium_properties(0.99)
+    return nt.PhotonPropSetup(srcs, targets, m, nt.CherenkovSpectrum((300.0, 800.0), 30, m, semantics="linear"), **kw)
+
+
+@pytest.fixture(scope="module")
+def orc(oracle_lib):
+    return oracle_lib
+
+
+def test_replay_isotropic_close_sphere(orc):
+    s = iso_close_setup()
+    n = compare_replay(gpu_hits(s, seed=3), orc.propagate_f64(s, seed=3), min_hits=1000)
+    assert n > 1000
+
+
+def test_replay_point_cone(orc):
+    s = workloads.point_cone_setup(400_000)
+    compare_replay(gpu_hits(s, seed=11), orc.propagate_f64(s, seed=11), min_hits=1)
+
+
+def test_replay_cascade_on_pom_string(orc):
+    s = cascade_small_setup()
+    compare_replay(gpu_hits(s, seed=5), orc.propagate_f64(s, seed=5), min_hits=50)
+
+
+@pytest.mark.parametrize("policy,exact", [("first", False), ("nearest", False), ("first", True)])
+def test_replay_mixed_sources(orc, policy, exact):
+    s = mixed_setup(hit_policy=policy, exact_pole_rotation=exact)
+    compare_replay(gpu_hits(s, seed=17), orc.propagate_f64(s, seed=17), min_hits=1000)
+
+
+def test_axicone_pole_quirk_half_cone():
+    # rot_from_ez_fast at a = e_z (utils.jl:230-232): every photon of a cone about +z has y >= 0
+    src = nt.AxiconeEmitter((0.0, 0.0, 0.0), (0.0, 0.0, 1.0), 0.0, 100_000, 0.7)
+    tgt = nt.DetectionSphere((0.0, 0.0, 1.0), 0.9, 1, 1.0, 1)
+    s = nt.PhotonPropSetup([src], [tgt], nt.make_simple_water(), nt.Monochromatic(400.0))
+    h = gpu_hits(s)
+    first = h[h["dist_travelled"] < 0.5]  # unscattered, straight into the sphere
+    assert len(first) > 1000
+    assert np.all(first["initial_direction"][:, 1] >= 0)
+    s2 = nt.PhotonPropSetup([src], [tgt], nt.make_simple_water(), nt.Monochromatic(400.0), exact_pole_rotation=True)
+    h2 = gpu_hits(s2)
+    assert np.mean(h2["initial_direction"][:, 1] < 0) > 0.4
+
+
+def test_deterministic_rerun():
+    s = iso_close_setup(100_000)
+    a, b = gpu_hits(s, seed=9), gpu_hits(s, seed=9)
+    assert a.tobytes() == b.tobytes()
+    c = gpu_hits(s, seed=10)
+    assert len(c) != len(a) or c.tobytes() != a.tobytes()
+
+
+def test_overflow_reports_exact_count():
+    s = iso_close_setup(100_000)
+    full = gpu_hits(s, seed=4)
+    assert len(full) > 100
+    with pytest.raises(_abi.NtpError) as e:
+        nt.propagate_photons(s, seed=4, capacity=50)
+    assert e.value.status == _abi.NTP_ERR_OVERFLOW
+    lib, ctx = s.context()
+    out = np.zeros(50, dtype=_abi.HIT_DTYPE)
+    nh, ns = C.c_uint64(), C.c_uint64()
+    st = lib.ntp_propagate(ctx, pack_sources(s.sources), 1, 4, C.byref(s.prop_opts()), out.ctypes.data, 50, 0,
+                           C.byref(nh), C.byref(ns))
+    assert st == _abi.NTP_ERR_OVERFLOW and nh.value == len(full) and ns.value == 100_000
+    keys = set(zip(full["source_index"], full["photon_index"]))
+    assert all((r["source_index"], r["photon_index"]) in keys for r in out)
+
+
+def test_empty_and_no_target_inputs():
+    s = iso_close_setup(0)
+    h = nt.propagate_photons(s)
+    assert len(h) == 0 and h.n_photons_simulated == 0
+    src = nt.PointlikeIsotropicEmitter((0.0, 0.0, 0.0), 0.0, 50_000)
+    s2 = nt.PhotonPropSetup([src], [], nt.make_simple_water(), nt.Monochromatic(400.0))
+    h2 = nt.propagate_photons(s2)
+    assert len(h2) == 0 and h2.n_photons_simulated == 50_000
+
+
+def test_invalid_arguments():
+    s = iso_close_setup(1000)
+    lib, ctx = s.context()
+    srcs = pack_sources(s.sources)
+    srcs[0].kind = 99
+    nh, ns = C.c_uint64(), C.c_uint64()
+    out = np.zeros(10, dtype=_abi.HIT_DTYPE)
+    st = lib.ntp_propagate(ctx, srcs, 1, 0, None, out.ctypes.data, 10, 0, C.byref(nh), C.byref(ns))
+    assert st == _abi.NTP_ERR_INVALID and b"unknown kind" in lib.ntp_last_error(ctx)
+    bad = nt.PhotonPropSetup([nt.PointlikeIsotropicEmitter((0, 0, 0), 0.0, 10)],
+                             [nt.DetectionSphere((0, 0, 1), -1.0, 1, 1.0, 1)], nt.make_simple_water(),
+                             nt.Monochromatic(400.0))
+    with pytest.raises(_abi.NtpError):
+        nt.propagate_photons(bad)
+    dup = nt.PhotonPropSetup([nt.PointlikeIsotropicEmitter((0, 0, 0), 0.0, 10)],
+                             [nt.DetectionSphere((0, 0, 1), 0.2, 1, 1.0, 1), nt.DetectionSphere((0, 0, 2), 0.2, 1, 1.0, 1)],
+                             nt.make_simple_water(), nt.Monochromatic(400.0))
+    with pytest.raises(_abi.NtpError, match="duplicate module_id"):
+        nt.propagate_photons(dup)
+
+
+def test_run_stats_counts_steps():
+    s = iso_close_setup(100_000)
+    h = nt.propagate_photons(s, seed=1)
+    lib, ctx = s.context()
+    st = _abi.NtpRunStats()
+    assert lib.ntp_get_run_stats(ctx, C.byref(st)) == 0
+    assert st.photons == 100_000 and st.hits == len(h)
+    # photons that hit stop early; the others take all 15 steps
+    assert 100_000 * 1 <= st.photon_steps <= 100_000 * 15
+    assert st.photon_steps > (100_000 - len(h)) * 15
+
+
+def _chi2_counts(a, b, ids):
+    ca = np.array([np.sum(a == i) for i in ids], dtype=float)
+    cb = np.array([np.sum(b == i) for i in ids], dtype=float)
+    m = (ca + cb) > 0
+    return ca[m], cb[m]
+
+
+def test_statistics_against_float_mirror(orc):
+    # independent seeds: per-module counts within 4 sigma and arrival-time KS p > 0.01
+    from scipy import stats
+    s = cascade_small_setup(2_000_000)
+    g = gpu_hits(s, seed=101)
+    o = orc.propagate_f32(s, seed=202, threads=os.cpu_count() or 1)
+    ids = np.unique(np.concatenate([g["module_id"], o["module_id"]]))
+    ca, cb = _chi2_counts(g["module_id"], o["module_id"], ids)
+    z = (ca - cb) / np.sqrt(ca + cb)
+    assert np.all(np.abs(z) < 4.0), z
+    assert stats.ks_2samp(g["time"], o["time"]).pvalue > 0.01
+
+
+def test_make_hits_matches_oracle(orc):
+    s = cascade_small_setup(1_000_000)
+    h = nt.propagate_photons(s, seed=21, reference_columns=False)
+    R = nt.utils.random_rotation(np.random.default_rng(3))
+    lib, ctx = s.context()
+    recs = np.ascontiguousarray(h.records)
+    pmt = np.zeros(len(recs), dtype=np.int32)
+    assert lib.ntp_make_hits(ctx, recs.ctypes.data, len(recs), np.ascontiguousarray(R).ctypes.data_as(
+        C.POINTER(C.c_double)), pmt.ctypes.data, 0, None) == 0
+    want = orc.make_hits(recs, s, R)
+    np.testing.assert_array_equal(pmt, want)
+    assert np.any(pmt > 0)
+    sel = nt.make_hits_from_photons(h, s, R)
+    assert len(sel) == int(np.sum(want > 0)) and np.all(sel["pmt_id"] > 0)
+
+
+def test_total_weight_and_time_residual_match_oracle(orc):
+    s = cascade_small_setup(500_000)
+    h = nt.propagate_photons(s, seed=23, reference_columns=False)
+    nt.calc_total_weight(h, s)
+    want = orc.total_weight(h.records, s, nt.p_one_pmt_acc)
+    np.testing.assert_array_equal(h["area_acc"], want["area_acc"])
+    np.testing.assert_allclose(h["wl_acc"], want["wl_acc"], rtol=1e-12)
+    np.testing.assert_allclose(h["abs_weight"], want["abs_weight"], rtol=1e-6)
+    np.testing.assert_allclose(h["total_weight"], want["total_weight"], rtol=1e-6)
+    nt.calc_time_residual(h, s)
+    n800 = float(np.float32(s.medium.refractive_index(np.array([800.0]))[0]))
+    np.testing.assert_allclose(h["tres"], orc.time_residual(h.records, s, n800), rtol=1e-12, atol=1e-9)
+
+
+def test_single_target_column_swap():
+    s = iso_close_setup(50_000)
+    h = nt.propagate_photons(s, seed=2)
+    assert np.array_equal(h["direction"], h.records["initial_direction"])
+    assert np.array_equal(h["initial_direction"], h.records["direction"])
