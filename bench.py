@@ -54,6 +54,8 @@ def parse():
     ap.add_argument("--cpu-seconds", type=float, default=10.0, help="target length of the CPU baseline sample")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--e2e-steps", type=int, default=3)
+    ap.add_argument("--small", action="store_true",
+                    help="profiling case: one cascade at 1% of its photons, 64 MB hit buffer, 256 MB L2 flush")
     return ap.parse_args()
 
 
@@ -212,14 +214,17 @@ def main():
     from neutrinotelescopes_gb300.photon_prop import pack_sources
 
     torch.cuda.set_device(local)
-    setup = workloads.cascade_string_setup(N_CASCADES, WORKLOAD_SEED, device=local)
+    if args.small:
+        setup = workloads.cascade_string_setup(1, WORKLOAD_SEED, photon_scale=0.01, device=local)
+    else:
+        setup = workloads.cascade_string_setup(N_CASCADES, WORKLOAD_SEED, device=local)
     lib, ctx = setup.context()
     srcs = pack_sources(setup.sources)
     n_src = len(setup.sources)
     photons = sum(int(s.photons) for s in setup.sources)
-    cap = 1 << 24
+    cap = 1 << (20 if args.small else 24)
     hits = torch.empty((cap, 64), dtype=torch.uint8, device=f"cuda:{local}")
-    flush = torch.empty(512 << 20, dtype=torch.uint8, device=f"cuda:{local}")
+    flush = torch.empty((256 if args.small else 512) << 20, dtype=torch.uint8, device=f"cuda:{local}")
     stream = torch.cuda.current_stream()
     opts = setup.prop_opts(stream=stream.cuda_stream)
     nh, ns = C.c_uint64(), C.c_uint64()
@@ -273,15 +278,16 @@ def main():
         h = nt.propagate_photons(setup, seed=workloads.SEED_BASE + 500 + i, capacity=cap)
         e2e_t.append(time.perf_counter() - t0)
         e2e_hits.append(len(h))
-    e2e_val = photons * len(e2e_t) * world / max_over_ranks(sum(e2e_t), world)
+    e2e_val = photons * len(e2e_t) * world / max_over_ranks(sum(e2e_t), world) if e2e_t else None
     h2d = C.sizeof(_abi.NtpSource) * n_src + 8 * (n_src + 1)
-    d2h = int(statistics.mean(e2e_hits)) * 64 + 32
+    d2h = int(statistics.mean(e2e_hits)) * 64 + 32 if e2e_hits else 0
 
     out = {"metric": METRIC, "value": value, "unit": METRIC, "n_gpus": world, "steps": args.steps,
            "warmup": args.warmup, "ms_per_step": statistics.mean(ms), "higher_is_better": True,
            "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-           "config": {"workload": "cascade_string: 4 EM cascades 1e3-1e5 GeV (7.5e9 photons), 20 POM modules x 16 PMTs "
-                                  "on one string, simple water", "photons_per_step": photons,
+           "config": {"workload": ("cascade_string (small profiling case: 1 cascade at 1% of its photons)" if args.small
+                                   else "cascade_string: 4 EM cascades 1e3-1e5 GeV (7.5e9 photons), 20 POM modules "
+                                        "x 16 PMTs on one string, simple water"), "photons_per_step": photons,
                       "hits_per_step": int(statistics.mean(hit_counts)), "l2": "flushed between steps (512 MB write)",
                       "parallelism": f"replicas x{world}"},
            "roofline": roofline, "clocks": clocks,

@@ -148,7 +148,11 @@ enum ntp_hit_policy {
 enum ntp_prop_flags {
     /* rot_from_ez_fast (utils.jl:228-243) maps v to (v1, copysign(v2,a3), copysign(v3,a3))
        when |a3| == 1.  By default that is reproduced; this flag applies the true rotation. */
-    NTP_FLAG_EXACT_POLE_ROTATION = 1
+    NTP_FLAG_EXACT_POLE_ROTATION = 1,
+    /* Test every target at every step (the reference's linear scan,
+       photon_prop_cuda.jl:460-468) instead of culling by vertical columns;
+       the hits are the same either way. */
+    NTP_FLAG_PLAIN_SCAN = 2
 };
 
 typedef struct ntp_prop_opts {

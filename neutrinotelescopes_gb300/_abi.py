@@ -48,6 +48,7 @@ SPEC_INV_SQUARE = 3
 HIT_FIRST_IN_LIST = 0
 HIT_NEAREST = 1
 FLAG_EXACT_POLE_ROTATION = 1
+FLAG_PLAIN_SCAN = 2
 
 
 class NtpSource(C.Structure):

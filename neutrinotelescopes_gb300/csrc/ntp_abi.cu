@@ -50,6 +50,9 @@ struct ntp_ctx {
     int* d_pmtoff = nullptr;
     double* d_opening = nullptr;
     double* d_area = nullptr;
+    ntp::Column* d_cols = nullptr;  // vertical columns of targets (culling)
+    int* d_members = nullptr;
+    int n_cols = 0;
     double* d_axes = nullptr;  // PMT axes for the current orientation
     double* d_tgeo = nullptr;  // per-target tgeo for time residuals
 
@@ -195,6 +198,8 @@ void ntp_destroy(ntp_ctx* ctx) {
     dfree(ctx->d_area);
     dfree(ctx->d_axes);
     dfree(ctx->d_tgeo);
+    dfree(ctx->d_cols);
+    dfree(ctx->d_members);
     dfree(ctx->d_acc_wl);
     dfree(ctx->d_acc);
     dfree(ctx->d_counters);
@@ -333,7 +338,61 @@ ntp_status ntp_set_targets(ntp_ctx* ctx, const ntp_target* t, int32_t n, const f
     for (int i = 1; i < n; ++i)
         if (sorted[i].x == sorted[i - 1].x)
             return invalid(ctx, "ntp_set_targets: duplicate module_id " + std::to_string(sorted[i].x));
+    // vertical columns: targets with the same (x, y), sorted by z
+    std::vector<ntp::Column> cols;
+    std::vector<int> members;
+    {
+        std::vector<int> order(n);
+        for (int i = 0; i < n; ++i) order[i] = i;
+        std::sort(order.begin(), order.end(), [&](int a, int b) {
+            const ntp_target &A = t[a], &B = t[b];
+            if (A.position[0] != B.position[0]) return A.position[0] < B.position[0];
+            if (A.position[1] != B.position[1]) return A.position[1] < B.position[1];
+            if (A.position[2] != B.position[2]) return A.position[2] < B.position[2];
+            return a < b;
+        });
+        for (int i = 0; i < n;) {
+            int j = i;
+            while (j < n && t[order[j]].position[0] == t[order[i]].position[0] &&
+                   t[order[j]].position[1] == t[order[i]].position[1])
+                ++j;
+            ntp::Column c{};
+            c.cx = t[order[i]].position[0];
+            c.cy = t[order[i]].position[1];
+            c.first = static_cast<int>(members.size());
+            c.count = j - i;
+            c.z0 = t[order[i]].position[2];
+            c.z_last = t[order[j - 1]].position[2];
+            float rmax = 0.0f;
+            for (int k = i; k < j; ++k) {
+                rmax = std::max(rmax, t[order[k]].radius);
+                members.push_back(order[k]);
+            }
+            c.r_cull = rmax * (1.0f + 1e-6f) + 0.02f;
+            c.dz = 0.0f;
+            if (c.count > 1) {
+                const double step = (static_cast<double>(c.z_last) - c.z0) / (c.count - 1);
+                bool uniform = step > 0;
+                for (int k = i + 1; k < j && uniform; ++k) {
+                    const double want = c.z0 + step * (k - i);
+                    uniform = std::fabs(t[order[k]].position[2] - want) <= 1e-5 * std::max(1.0, std::fabs(want));
+                }
+                if (uniform) c.dz = static_cast<float>(step);
+            }
+            cols.push_back(c);
+            i = j;
+        }
+    }
+    const bool use_cols = n >= 4 && 2 * static_cast<int>(cols.size()) <= n && static_cast<int>(cols.size()) <= ntp::kMaxSmemColumns;
     cudaSetDevice(ctx->device);
+    dfree(ctx->d_cols);
+    dfree(ctx->d_members);
+    ctx->n_cols = 0;
+    if (use_cols) {
+        NTP_CUDA(ctx, dupload(ctx->d_cols, cols.data(), cols.size(), ctx->stream));
+        NTP_CUDA(ctx, dupload(ctx->d_members, members.data(), members.size(), ctx->stream));
+        ctx->n_cols = static_cast<int>(cols.size());
+    }
     NTP_CUDA(ctx, dupload(ctx->d_tgt, tg.data(), n, ctx->stream));
     NTP_CUDA(ctx, dupload(ctx->d_tgt_id, ids.data(), n, ctx->stream));
     NTP_CUDA(ctx, dupload(ctx->d_sorted, sorted.data(), n, ctx->stream));
@@ -436,6 +495,9 @@ ntp_status ntp_propagate(ntp_ctx* ctx, const ntp_source* sources, int32_t n_sour
     p.target_ids = ctx->d_tgt_id;
     p.n_targets = ctx->n_tgt;
     p.targets_in_smem = ctx->n_tgt <= ntp::kMaxSmemTargets ? 1 : 0;
+    p.columns = (ctx->n_cols > 0 && !(o.flags & NTP_FLAG_PLAIN_SCAN)) ? ctx->d_cols : nullptr;
+    p.members = ctx->d_members;
+    p.n_columns = ctx->n_cols;
     p.medium = ctx->d_med;
     p.n_medium = ctx->n_med;
     p.wl_min = ctx->wl_min;

@@ -53,14 +53,19 @@ struct V3 {
 };
 
 // rot_from_ez_fast, utils.jl:228-243: the rotation taking e_z to a, applied
-// to o.  At |a_z| == 1 the reference returns (o1, copysign(o2,a3),
+// to o.  At a = +-e_z the reference returns (o1, copysign(o2,a3),
 // copysign(o3,a3)); exact_pole switches to the true rotation there.
+// The reference tests |a3| == 1; here the pole is a1^2 + a2^2 == 0.  The two
+// agree for every exact +-e_z, but a scattered direction whose z component
+// rounds to 1.0f in single precision while x, y are not zero keeps its
+// transverse part here (the general formula stays bounded: a_i^2 fact <=
+// 1 - a3), as the same step in double precision does.
 __device__ __forceinline__ V3 rot_from_ez(V3 a, V3 o, bool exact_pole) {
-    if (fabsf(a.z) == 1.0f) {
-        if (exact_pole) return V3{o.x, a.z * o.y, a.z * o.z};
+    const float a1sq = a.x * a.x, a2sq = a.y * a.y;
+    if (a1sq + a2sq == 0.0f) {
+        if (exact_pole) return V3{o.x, copysignf(1.0f, a.z) * o.y, copysignf(1.0f, a.z) * o.z};
         return V3{o.x, copysignf(o.y, a.z), copysignf(o.z, a.z)};
     }
-    const float a1sq = a.x * a.x, a2sq = a.y * a.y;
     const float fact = __fdividef(1.0f - a.z, a2sq + a1sq);
     const float a1a2 = a.x * a.y;
     V3 r;

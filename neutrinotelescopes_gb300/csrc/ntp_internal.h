@@ -14,6 +14,20 @@ namespace ntp {
 
 constexpr int kPropBlock = 256;      // threads per block of the propagation kernel
 constexpr int kMaxSmemTargets = 8192;  // targets staged in shared memory (20 B each)
+constexpr int kMaxSmemColumns = 2048;  // columns staged in shared memory (32 B each)
+
+// A vertical column of targets sharing (x, y): the unit of the geometric
+// culling.  Members are target indices sorted by z.
+struct Column {
+    float cx, cy;  // axis
+    float r_cull;  // largest member radius plus a rounding margin
+    float z0;      // z of the lowest member
+    float dz;      // uniform member spacing, 0 if not uniform
+    int first;     // offset of the members in the member list
+    int count;
+    float z_last;  // z of the highest member
+};
+static_assert(sizeof(Column) == 32, "Column is 32 bytes");
 
 // Everything one launch of the propagation kernel reads.
 struct PropParams {
@@ -26,6 +40,10 @@ struct PropParams {
     const uint32_t* target_ids;           // device, module_id per target
     int n_targets;
     int targets_in_smem;                  // stage targets in shared memory
+
+    const Column* columns;                // device; nullptr = scan every target
+    const int* members;                   // device, target indices grouped by column
+    int n_columns;
 
     const float4* medium;                 // device, per knot (n, v_group, l_scatter, 0)
     int n_medium;

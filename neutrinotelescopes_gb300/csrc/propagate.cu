@@ -63,6 +63,78 @@ __device__ __noinline__ float rand_gamma(float shape, float scale, uint4 ctr, ui
     return d * scale;
 }
 
+// check_intersection(::Spherical, ...), photon_prop_cuda.jl:233-271: the
+// segment pos + t dir, 0 < t < step, enters the sphere (x, y, z, r^2) at t = d.
+__device__ __forceinline__ bool sphere_hit(const float4 T, const V3 pos, const V3 dir, float step, float& d) {
+    const float dx = pos.x - T.x, dy = pos.y - T.y, dz = pos.z - T.z;
+    const float a = dir.x * dx + dir.y * dy + dir.z * dz;
+    const float pp = dx * dx + dy * dy + dz * dz;
+    const float b = fmaf(a, a, T.w - pp);
+    if (b >= 0.0f) {
+        d = -a - sqrtf(b);
+        return d > 0.0f && d < step;
+    }
+    return false;
+}
+
+// Tests the members of one vertical column that the segment can reach.  The
+// culling is conservative: the horizontal distance of the segment from the
+// column axis is compared with r_cull^2 plus the rounding envelope of the
+// single-precision sphere test (which grows as step^2), and the z range is
+// padded by r_cull and one member; every member it keeps goes through the
+// same sphere_hit as the plain scan.  Among the hits it keeps the first in
+// target-list order (or the nearest), as the plain scan does.
+__device__ __forceinline__ void column_candidates(const Column& C, const int* __restrict__ mem,
+                                                  const float4* __restrict__ tg, const V3 pos, const V3 dir,
+                                                  float step, int policy, int& hit_t, float& hit_d) {
+    const float px = pos.x - C.cx, py = pos.y - C.cy;
+    const float dd = dir.x * dir.x + dir.y * dir.y;
+    const float rc2 = fmaf(4e-7f * step, step, C.r_cull * C.r_cull);
+    float t0 = 0.0f, t1 = step;
+    if (dd > 1e-12f) {
+        const float inv_dd = 1.0f / dd;
+        const float ts = -(px * dir.x + py * dir.y) * inv_dd;  // closest approach to the axis
+        float m;
+        if (ts <= 0.0f) {
+            m = px * px + py * py;
+        } else if (ts >= step) {
+            const float ex = fmaf(step, dir.x, px), ey = fmaf(step, dir.y, py);
+            m = ex * ex + ey * ey;
+        } else {
+            const float cr = px * dir.y - py * dir.x;
+            m = cr * cr * inv_dd;
+        }
+        if (m > rc2) return;
+        const float cr = px * dir.y - py * dir.x;
+        const float h = sqrtf(fmaxf(rc2 - cr * cr * inv_dd, 0.0f) * inv_dd);
+        t0 = fmaxf(ts - h, 0.0f);
+        t1 = fminf(ts + h, step);
+    } else if (px * px + py * py > rc2) {
+        return;
+    }
+    const float za = fmaf(t0, dir.z, pos.z), zb = fmaf(t1, dir.z, pos.z);
+    const float zlo = fminf(za, zb) - C.r_cull, zhi = fmaxf(za, zb) + C.r_cull;
+    if (zhi < C.z0 - C.r_cull || zlo > C.z_last + C.r_cull) return;
+    int k0 = 0, k1 = C.count - 1;
+    if (C.dz > 0.0f) {
+        const float inv = 1.0f / C.dz;
+        k0 = max(k0, static_cast<int>(floorf(fmaxf((zlo - C.z0) * inv, -1.0f))) - 1);
+        k1 = min(k1, static_cast<int>(ceilf(fminf((zhi - C.z0) * inv, static_cast<float>(C.count)))) + 1);
+    }
+    for (int k = k0; k <= k1; ++k) {
+        const int t = mem[C.first + k];
+        const float4 T = tg[t];
+        if (C.dz <= 0.0f && (T.z < zlo - 1.0f || T.z > zhi + 1.0f)) continue;
+        float d;
+        if (sphere_hit(T, pos, dir, step, d)) {
+            if (policy == NTP_HIT_NEAREST ? d < hit_d : (hit_t < 0 || t < hit_t)) {
+                hit_d = d;
+                hit_t = t;
+            }
+        }
+    }
+}
+
 // initialize_photon_state methods, photon_prop_cuda.jl:133-200 and
 // sample_cherenkov_direction :107-125.
 __device__ __forceinline__ void init_photon(Photon& ph, const ntp_source* __restrict__ sources,
@@ -153,23 +225,31 @@ __device__ __forceinline__ void init_photon(Photon& ph, const ntp_source* __rest
 }
 
 __global__ void __launch_bounds__(kPropBlock, 3) propagate_kernel(const PropParams p) {
+    // shared memory: medium knots | targets | module ids | columns | members | spectrum knots
     extern __shared__ float4 smem[];
+    const int nt_s = p.targets_in_smem ? p.n_targets : 0;
+    const int nc_s = p.targets_in_smem && p.columns ? p.n_columns : 0;
     float4* s_med = smem;
     float4* s_tgt = s_med + p.n_medium;
-    uint32_t* s_tid = reinterpret_cast<uint32_t*>(s_tgt + (p.targets_in_smem ? p.n_targets : 0));
-    float* s_spec = reinterpret_cast<float*>(s_tid + (p.targets_in_smem ? p.n_targets : 0));
+    Column* s_col = reinterpret_cast<Column*>(s_tgt + nt_s);
+    uint32_t* s_tid = reinterpret_cast<uint32_t*>(s_col + nc_s);
+    int* s_mem = reinterpret_cast<int*>(s_tid + nt_s);
+    float* s_spec = reinterpret_cast<float*>(s_mem + (nc_s ? nt_s : 0));
 
     for (int i = threadIdx.x; i < p.n_medium; i += blockDim.x) s_med[i] = p.medium[i];
     for (int i = threadIdx.x; i < p.n_spec; i += blockDim.x) s_spec[i] = p.spec_knots[i];
-    if (p.targets_in_smem) {
-        for (int i = threadIdx.x; i < p.n_targets; i += blockDim.x) {
-            s_tgt[i] = p.targets[i];
-            s_tid[i] = p.target_ids[i];
-        }
+    for (int i = threadIdx.x; i < nt_s; i += blockDim.x) {
+        s_tgt[i] = p.targets[i];
+        s_tid[i] = p.target_ids[i];
     }
+    for (int i = threadIdx.x; i < nc_s; i += blockDim.x) s_col[i] = p.columns[i];
+    if (nc_s)
+        for (int i = threadIdx.x; i < nt_s; i += blockDim.x) s_mem[i] = p.members[i];
     __syncthreads();
     const float4* tg = p.targets_in_smem ? s_tgt : p.targets;
     const uint32_t* tid = p.targets_in_smem ? s_tid : p.target_ids;
+    const Column* cols = p.columns ? (nc_s ? s_col : p.columns) : nullptr;
+    const int* mem = nc_s ? s_mem : p.members;
 
     SpectrumView spec{p.spec_kind, p.n_spec, s_spec, p.spec_p0, p.spec_p1};
     const float g = p.hg_g, one_m_g = 1.0f - g, one_m_g2 = fmaf(-g, g, 1.0f);
@@ -221,15 +301,13 @@ __global__ void __launch_bounds__(kPropBlock, 3) propagate_kernel(const PropPara
 
             // check_intersection over the targets, photon_prop_cuda.jl:233-271, :460-468
             float hit_d = step;
-            for (int t = 0; t < p.n_targets; ++t) {
-                const float4 T = tg[t];
-                const float dx = ph.pos.x - T.x, dy = ph.pos.y - T.y, dz = ph.pos.z - T.z;
-                const float a = ph.dir.x * dx + ph.dir.y * dy + ph.dir.z * dz;
-                const float pp = dx * dx + dy * dy + dz * dz;
-                const float b = fmaf(a, a, T.w - pp);
-                if (b >= 0.0f) {
-                    const float d = -a - sqrtf(b);
-                    if (d > 0.0f && d < step) {
+            if (cols) {
+                for (int c = 0; c < p.n_columns; ++c)
+                    column_candidates(cols[c], mem, tg, ph.pos, ph.dir, step, p.hit_policy, hit_t, hit_d);
+            } else {
+                for (int t = 0; t < p.n_targets; ++t) {
+                    float d;
+                    if (sphere_hit(tg[t], ph.pos, ph.dir, step, d)) {
                         if (p.hit_policy == NTP_HIT_NEAREST) {
                             if (d < hit_d) { hit_d = d; hit_t = t; }
                         } else {
@@ -296,7 +374,11 @@ __global__ void __launch_bounds__(kPropBlock, 3) propagate_kernel(const PropPara
 
 size_t prop_smem_bytes(const PropParams& p) {
     size_t b = sizeof(float4) * static_cast<size_t>(p.n_medium);
-    if (p.targets_in_smem) b += (sizeof(float4) + sizeof(uint32_t)) * static_cast<size_t>(p.n_targets);
+    if (p.targets_in_smem) {
+        b += (sizeof(float4) + sizeof(uint32_t)) * static_cast<size_t>(p.n_targets);
+        if (p.columns)
+            b += sizeof(Column) * static_cast<size_t>(p.n_columns) + sizeof(int) * static_cast<size_t>(p.n_targets);
+    }
     b += sizeof(float) * static_cast<size_t>(p.n_spec);
     return b;
 }

@@ -83,7 +83,9 @@ class PhotonPropSetup:
     ``hit_policy`` ('first' = first target in list order, as the reference;
     'nearest'), ``exact_pole_rotation`` (apply the true rotation where the
     reference's rot_from_ez_fast uses copysign at |a_z| = 1), ``device`` and
-    ``wavelength_acceptance`` (PMT acceptance table; default assets/PMTAcc.csv).
+    ``wavelength_acceptance`` (PMT acceptance table; default assets/PMTAcc.csv)
+    and ``plain_scan`` (test every target at every step instead of culling by
+    vertical columns; same hits, slower).
     """
 
     sources: list
@@ -96,6 +98,7 @@ class PhotonPropSetup:
     device: int = 0
     medium_knots: int = 1024
     wavelength_acceptance: object = None
+    plain_scan: bool = False
     _ctx: object = field(default=None, init=False, repr=False)
     _uploaded: tuple = field(default=(), init=False, repr=False)
 
@@ -166,7 +169,8 @@ class PhotonPropSetup:
         return _abi.NtpPropOpts(
             max_steps=self.max_steps,
             hit_policy=_abi.HIT_FIRST_IN_LIST if self.hit_policy == "first" else _abi.HIT_NEAREST,
-            flags=_abi.FLAG_EXACT_POLE_ROTATION if self.exact_pole_rotation else 0,
+            flags=(_abi.FLAG_EXACT_POLE_ROTATION if self.exact_pole_rotation else 0)
+            | (_abi.FLAG_PLAIN_SCAN if self.plain_scan else 0),
             stream=stream,
         )
 

@@ -109,6 +109,20 @@ def test_replay_mixed_sources(orc, policy, exact):
     compare_replay(gpu_hits(s, seed=17), orc.propagate_f64(s, seed=17), min_hits=1000)
 
 
+def test_column_culling_matches_plain_scan():
+    # culling by vertical columns keeps exactly the hits of the full scan
+    for policy in ("first", "nearest"):
+        a = cascade_small_setup(400_000, hit_policy=policy)
+        b = cascade_small_setup(400_000, hit_policy=policy, plain_scan=True)
+        ha, hb = gpu_hits(a, seed=8), gpu_hits(b, seed=8)
+        assert len(ha) > 100
+        assert ha.tobytes() == hb.tobytes()
+    s = workloads.cascade_string_setup(2, photon_scale=2e-4)
+    t = workloads.cascade_string_setup(2, photon_scale=2e-4, plain_scan=True)
+    ha, hb = gpu_hits(s, seed=3), gpu_hits(t, seed=3)
+    assert len(ha) > 100 and ha.tobytes() == hb.tobytes()
+
+
 def test_axicone_pole_quirk_half_cone():
     # rot_from_ez_fast at a = e_z (utils.jl:230-232): every photon of a cone about +z has y >= 0
     src = nt.AxiconeEmitter((0.0, 0.0, 0.0), (0.0, 0.0, 1.0), 0.0, 100_000, 0.7)
