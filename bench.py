@@ -36,13 +36,16 @@ METRIC = "photons/s"
 # Philox4x32-10 block (10 rounds x 6 integer ops + 10 for counter / uniform
 # conversion), about 50 FP32 operations for the step length, phase function,
 # rotation and position / time update, 5 special-function operations (log,
-# sin, cos, sqrt, reciprocal), and 12 FP32 operations per sphere tested.
+# sin, cos, sqrt, reciprocal), and 12 FP32 operations for the one geometric
+# test a step needs on this detector (the closest approach of the segment to
+# the single string; a sphere test only follows when the segment passes within
+# a module radius, which is rare enough not to count).
 OPS_BASE = 70 + 50 + 5
-OPS_PER_TARGET = 12
+OPS_PER_GEOMETRY_TEST = 12
 
 
-def algo_ops_per_step(n_targets: int) -> int:
-    return OPS_BASE + OPS_PER_TARGET * n_targets
+def algo_ops_per_step(n_strings: int) -> int:
+    return OPS_BASE + OPS_PER_GEOMETRY_TEST * n_strings
 
 
 def parse():
@@ -260,7 +263,8 @@ def main():
     clocks = clk.summary()
 
     # roofline of the propagation kernel: algorithmic lane-ops / kernel time
-    ops_step = algo_ops_per_step(len(setup.targets))
+    n_strings = len({(float(t.position[0]), float(t.position[1])) for t in setup.targets})
+    ops_step = algo_ops_per_step(n_strings)
     achieved = sum(steps_taken) * ops_step / (sum(ms) / 1e3) / 1e9
     sm_mhz = clocks.get("sm_mhz") or 2070.0
     peak = 152 * 4 * 32 * sm_mhz * 1e6 / 1e9  # lane-instructions issued per second at the sampled clock

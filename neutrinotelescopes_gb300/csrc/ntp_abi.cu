@@ -6,6 +6,7 @@
 #include <algorithm>
 #include <cmath>
 #include <cstdio>
+#include <cstdlib>
 #include <cstring>
 #include <mutex>
 #include <string>
@@ -528,6 +529,8 @@ ntp_status ntp_propagate(ntp_ctx* ctx, const ntp_source* sources, int32_t n_sour
     unsigned long long chunk = total / (warps * 8);
     chunk = std::max<unsigned long long>(32, std::min<unsigned long long>(4096, chunk));
     p.chunk = (chunk + 31) / 32 * 32;
+    p.refill_min = 8;
+    if (const char* env = std::getenv("NTP_REFILL_MIN")) p.refill_min = std::max(1, std::min(32, std::atoi(env)));
 
     NTP_CUDA(ctx, ntp::launch_propagate(p, grid, st));
     NTP_CUDA(ctx, cudaMemcpyAsync(ctx->h_counters, ctx->d_counters, 4 * sizeof(unsigned long long),

@@ -35,9 +35,11 @@ __device__ __forceinline__ uint4 philox4x32_10(uint4 c, uint2 k) {
             k.x += 0x9E3779B9u;
             k.y += 0xBB67AE85u;
         }
-        const uint32_t lo0 = 0xD2511F53u * c.x, hi0 = __umulhi(0xD2511F53u, c.x);
-        const uint32_t lo1 = 0xCD9E8D57u * c.z, hi1 = __umulhi(0xCD9E8D57u, c.z);
-        c = make_uint4(hi1 ^ c.y ^ k.x, lo1, hi0 ^ c.w ^ k.y, lo0);
+        // one 32x32->64 wide multiply each
+        const unsigned long long p0 = static_cast<unsigned long long>(0xD2511F53u) * c.x;
+        const unsigned long long p1 = static_cast<unsigned long long>(0xCD9E8D57u) * c.z;
+        c = make_uint4(static_cast<uint32_t>(p1 >> 32) ^ c.y ^ k.x, static_cast<uint32_t>(p1),
+                       static_cast<uint32_t>(p0 >> 32) ^ c.w ^ k.y, static_cast<uint32_t>(p0));
     }
     return c;
 }
@@ -118,24 +120,42 @@ __device__ __forceinline__ float sample_wavelength(const SpectrumView& s, float 
 }
 }
 
+// Fast single-precision helpers for the per-step arithmetic.  Their errors
+// (a few ulp relative, or ~4e-7 absolute for the sine and cosine) are far
+// below the 1e-4 per-photon agreement the propagation is held to.
+__device__ __forceinline__ float fast_rcp(float x) { return __fdividef(1.0f, x); }
+
+// sqrt(x) for x >= 0 from the reciprocal square root (exact 0 at 0)
+__device__ __forceinline__ float fast_sqrt(float x) { return x > 0.0f ? x * rsqrtf(x) : 0.0f; }
+
+// (sin, cos)(2 pi u) for u in (0, 1): the hardware sine / cosine on the
+// argument moved to [-pi, pi), where their absolute error is below 2^-21.
+__device__ __forceinline__ void sincos_2pi(float u, float* s, float* c) {
+    const float x = 6.283185307179586f * (u - 0.5f);
+    *s = -__sinf(x);
+    *c = -__cosf(x);
+}
+
 // One minus the Henyey-Greenstein cosine (cuda_hg_scattering_func,
 // photon_prop_cuda.jl:70-77).  With D = 1 + g(2 eta - 1), t = (1 - g^2)/D:
 //   cos = (1 + g^2 - t^2) / 2g    and    1 - cos = (1-g)(1-eta)(t + 1 - g) / D,
 // the second form keeps full relative precision for forward scatters.
 __device__ __forceinline__ float hg_one_minus_cos(float g, float one_m_g, float one_m_g2, float eta) {
     const float D = fmaf(g, fmaf(2.0f, eta, -1.0f), 1.0f);
-    const float invD = 1.0f / D;
+    const float invD = fast_rcp(D);
     const float t = one_m_g2 * invD;
     const float omc = one_m_g * (1.0f - eta) * (t + one_m_g) * invD;
     return fminf(fmaxf(omc, 0.0f), 2.0f);
 }
 
 // Rayleigh (3/8)(1 + mu^2): exact CDF inverse, mu^3 + 3 mu = 8u - 4, by
-// Cardano in the form mu = sign(q)(A - 1/A), A = cbrt(|q| + sqrt(q^2 + 1)).
+// Cardano in the form mu = sign(q)(A - 1/A), A = cbrt(|q| + sqrt(q^2 + 1)),
+// the cube root as 2^(log2(x)/3) on x in [1, 2 + sqrt 5].
 __device__ __forceinline__ float rayleigh_cos(float u) {
     const float q = fmaf(4.0f, u, -2.0f);
-    const float A = cbrtf(fabsf(q) + sqrtf(fmaf(q, q, 1.0f)));
-    const float mu = A - 1.0f / A;
+    const float x = fabsf(q) + fast_sqrt(fmaf(q, q, 1.0f));
+    const float A = exp2f(__log2f(x) * (1.0f / 3.0f));
+    const float mu = A - fast_rcp(A);
     return copysignf(mu, q);
 }
 
@@ -143,8 +163,8 @@ __device__ __forceinline__ float rayleigh_cos(float u) {
 // sph_to_cart (utils.jl:105-115) with sin theta = sqrt(omc (2 - omc)).
 __device__ __forceinline__ V3 dir_from_omc(float omc, float u_phi) {
     float sp, cp;
-    sincospif(2.0f * u_phi, &sp, &cp);
-    const float st = sqrtf(omc * (2.0f - omc));
+    sincos_2pi(u_phi, &sp, &cp);
+    const float st = fast_sqrt(omc * (2.0f - omc));
     return V3{cp * st, sp * st, 1.0f - omc};
 }
 

@@ -66,6 +66,7 @@ struct PropParams {
     unsigned long long capacity;
     unsigned long long* counters;         // device: [0] photons claimed, [1] hits, [2] photons done, [3] photon-steps
     unsigned long long chunk;             // photons a warp claims at once
+    int refill_min;                       // idle lanes a warp gathers before it initialises new photons
 };
 
 size_t prop_smem_bytes(const PropParams& p);

@@ -43,22 +43,22 @@ __device__ __forceinline__ int source_of(const unsigned long long* prefix, int n
 
 // rand_gamma(shape, scale), utils.jl:267-294 (Marsaglia-Tsang, shape > 1),
 // the normal from Box-Muller on Philox words; at most kGammaAttempts tries.
-__device__ __noinline__ float rand_gamma(float shape, float scale, uint4 ctr, uint2 key) {
-    const float d = static_cast<float>(static_cast<double>(shape) - 1.0 / 3.0);
-    const float c = 1.0f / sqrtf(9.0f * d);
+__device__ __forceinline__ float rand_gamma(float shape, float scale, uint4 ctr, uint2 key) {
+    const float d = shape - (1.0f / 3.0f);
+    const float c = rsqrtf(9.0f * d);
     for (int k = 0; k < kGammaAttempts; ++k) {
         ctr.x = kDrawGamma0 + static_cast<uint32_t>(k);
         const uint4 r = philox4x32_10(ctr, key);
         float s, cs;
-        sincospif(2.0f * u01(r.y), &s, &cs);
-        const float x = sqrtf(-2.0f * logf(u01(r.x))) * cs;
+        sincos_2pi(u01(r.y), &s, &cs);
+        const float x = fast_sqrt(-2.0f * __logf(u01(r.x))) * cs;
         float v = fmaf(c, x, 1.0f);
         if (v <= 0.0f) continue;
         v = v * v * v;
         const float u = u01(r.z);
         const float xsq = x * x;
         // the squeeze 1 - (1 + 0.0331 x^4) is never above u (utils.jl:286)
-        if (logf(u) < 0.5f * xsq + d * (1.0f - v + logf(v))) return d * v * scale;
+        if (__logf(u) < 0.5f * xsq + d * (1.0f - v + __logf(v))) return d * v * scale;
     }
     return d * scale;
 }
@@ -160,7 +160,7 @@ __device__ __forceinline__ void init_photon(Photon& ph, const ntp_source* __rest
     case NTP_SRC_POINT_ISOTROPIC:
     case NTP_SRC_POINT_TIME_RANGE: {  // initialize_direction_isotropic :100-104
         const float u = u01(A.z);     // cos = 2u - 1, 1 - cos = 2(1 - u)
-        ph.dir = dir_from_omc(2.0f * (1.0f - u), u01(A.y));
+        ph.dir = dir_from_omc(2.0f * (1.0f - u), u01(A.y));  // sin = sqrt(omc (2 - omc)) = 2 sqrt(u (1 - u))
         if (kind == NTP_SRC_POINT_TIME_RANGE) {
             const float t1 = __ldg(&src->time_end);
             ph.time = ph.time + u01(A.w) * (t1 - ph.time);
@@ -170,7 +170,7 @@ __device__ __forceinline__ void init_photon(Photon& ph, const ntp_source* __rest
     case NTP_SRC_AXICONE: {  // :148-156
         float st, ct, sp, cp;
         sincosf(__ldg(&src->angle), &st, &ct);
-        sincospif(2.0f * u01(A.y), &sp, &cp);
+        sincos_2pi(u01(A.y), &sp, &cp);
         ph.dir = rot_from_ez(sdir, V3{cp * st, sp * st, ct}, p.exact_pole);
         break;
     }
@@ -201,18 +201,17 @@ __device__ __forceinline__ void init_photon(Photon& ph, const ntp_source* __rest
     }
     if (cherenkov) {
         // photon on the Cherenkov cone cos = 1/n(lambda) (medium.jl:309-311)
-        const float cos_c = 1.0f / med.x;
+        const float cos_c = fast_rcp(med.x);
         float sp, cp;
-        sincospif(2.0f * u01(A.y), &sp, &cp);
-        const float sin_c = sqrtf(fmaf(-cos_c, cos_c, 1.0f));
+        sincos_2pi(u01(A.y), &sp, &cp);
+        const float sin_c = fast_sqrt(fmaf(-cos_c, cos_c, 1.0f));
         V3 d{cp * sin_c, sp * sin_c, cos_c};
         // track smearing, sample_cherenkov_track_direction utils.jl:249-260:
         // 1 - cos = (-log(1 - u I)/b)^(1/a), a = 0.39, b = 2.61
         const uint4 B = philox4x32_10(make_uint4(kDrawInitB, ph.pk_lo, ph.pk_hi, ph.src), p.key);
         const float I = 0.96729171f;  // 1 - exp(-2.61 * 2^0.39)
-        const float omc = fminf(powf(-log1pf(-u01(B.x) * I) * (1.0f / 2.61f),
-                                     1.0f / 0.39f),
-                                2.0f);
+        const float base = -log1pf(-u01(B.x) * I) * (1.0f / 2.61f);
+        const float omc = fminf(exp2f(__log2f(base) * (1.0f / 0.39f)), 2.0f);
         const V3 track = dir_from_omc(omc, u01(B.y));
         d = rot_from_ez(track, d, p.exact_pole);
         ph.dir = rot_from_ez(sdir, d, p.exact_pole);
@@ -220,7 +219,7 @@ __device__ __forceinline__ void init_photon(Photon& ph, const ntp_source* __rest
     ph.init_dir = ph.dir;
     ph.dist = 0.0f;
     ph.sca_len = med.z;
-    ph.inv_vg = 1.0f / med.y;
+    ph.inv_vg = fast_rcp(med.y);
     ph.step = 0;
 }
 
@@ -263,8 +262,11 @@ __global__ void __launch_bounds__(kPropBlock, 3) propagate_kernel(const PropPara
     Photon ph;
 
     for (;;) {
+        // refill idle lanes in batches of at least refill_min (or when every
+        // lane is idle), so the divergent initialisation runs for many lanes
+        // at once instead of for one or two in almost every iteration
         const unsigned idle = __ballot_sync(kFull, !active);
-        if (idle && !exhausted) {
+        if (!exhausted && (idle == kFull || __popc(idle) >= p.refill_min)) {
             unsigned long long avail = c_end - c_next;
             if (avail == 0) {
                 unsigned long long base = 0;
@@ -296,7 +298,7 @@ __global__ void __launch_bounds__(kPropBlock, 3) propagate_kernel(const PropPara
         if (active) {
             const uint4 r = philox4x32_10(
                 make_uint4(kDrawStep0 + static_cast<uint32_t>(ph.step), ph.pk_lo, ph.pk_hi, ph.src), p.key);
-            const float step = -logf(u01(r.x)) * ph.sca_len;
+            const float step = -__logf(u01(r.x)) * ph.sca_len;
             ++steps;
 
             // check_intersection over the targets, photon_prop_cuda.jl:233-271, :460-468

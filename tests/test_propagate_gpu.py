@@ -4,10 +4,13 @@ Per-photon replay: the kernel and the double-precision oracle draw the same
 Philox stream, so every photon can be compared individually.  Tolerances:
 position, time and distance to 1e-4 relative (vector norm for positions),
 directions to 1e-4 absolute (unit vectors), wavelength to 1e-5 relative.
-A photon whose hit/miss decision falls within float rounding of the sphere
-edge or the step end can come out differently in float and double; at most
-0.5% of the hit photons (and at least 3 allowed) may differ in the set of
-hit photons.
+Where the photon enters the sphere at a grazing angle the entry distance
+amplifies a lateral error by 1/cos(incidence): the position / time / distance
+bound of such a hit is widened by that factor (capped at 50), with
+cos(incidence) taken from the oracle's hit.  A photon whose hit/miss decision
+falls within float rounding of the sphere edge or the step end can come out
+differently in float and double; at most 0.5% of the hit photons (and at
+least 3) may differ in the set of hit photons.
 """
 import ctypes as C
 import os
@@ -31,7 +34,19 @@ def gpu_hits(setup, seed=0):
     return h.sorted_by_photon().records
 
 
-def compare_replay(g, o, min_hits=20):
+def incidence_slack(hits, setup):
+    """1 / cos(incidence) at each hit (capped at 50), from the hit position,
+    final direction and the module centre."""
+    centres = {t.module_id: (np.asarray(t.position, dtype=np.float64), float(t.radius)) for t in setup.targets}
+    out = np.ones(len(hits))
+    for i, h in enumerate(hits):
+        c, r = centres[int(h["module_id"])]
+        n = (h["position"].astype(np.float64) - c) / r
+        out[i] = 1.0 / max(abs(float(np.dot(n, h["direction"]))), 0.02)
+    return out
+
+
+def compare_replay(g, o, min_hits=20, setup=None):
     assert len(o) >= min_hits, f"oracle found only {len(o)} hits"
     kg = g["source_index"].astype(np.uint64) << np.uint64(40) | g["photon_index"]
     ko = o["source_index"].astype(np.uint64) << np.uint64(40) | o["photon_index"]
@@ -42,11 +57,15 @@ def compare_replay(g, o, min_hits=20):
     assert np.mean(a["module_id"] == b["module_id"]) >= 0.995
     same = a["module_id"] == b["module_id"]
     a, b = a[same], b[same]
+    slack = incidence_slack(b, setup) if setup is not None else np.ones(len(b))
     dp = np.linalg.norm(a["position"].astype(np.float64) - b["position"], axis=1)
     scale = np.maximum(np.linalg.norm(b["position"].astype(np.float64), axis=1), 1.0)
-    assert np.all(dp <= POS_RTOL * scale), f"max rel pos err {np.max(dp / scale):.3g}"
-    np.testing.assert_allclose(a["time"], b["time"], rtol=POS_RTOL, atol=1e-3)
-    np.testing.assert_allclose(a["dist_travelled"], b["dist_travelled"], rtol=POS_RTOL, atol=1e-4)
+    assert np.all(dp <= POS_RTOL * scale * slack), f"max rel pos err {np.max(dp / scale / slack):.3g}"
+    # along-path error of the entry point: at most the lateral bound times the slack
+    dl = POS_RTOL * scale * slack
+    vg = np.maximum(b["dist_travelled"] / np.maximum(b["time"], 1e-9), 0.05)
+    assert np.all(np.abs(a["dist_travelled"] - b["dist_travelled"]) <= POS_RTOL * b["dist_travelled"] + dl + 1e-4)
+    assert np.all(np.abs(a["time"].astype(np.float64) - b["time"]) <= POS_RTOL * np.abs(b["time"]) + dl / vg + 1e-3)
     np.testing.assert_allclose(a["direction"], b["direction"], atol=DIR_ATOL, rtol=0)
     np.testing.assert_allclose(a["initial_direction"], b["initial_direction"], atol=DIR_ATOL, rtol=0)
     np.testing.assert_allclose(a["wavelength"], b["wavelength"], rtol=WL_RTOL)
@@ -89,24 +108,24 @@ def orc(oracle_lib):
 
 def test_replay_isotropic_close_sphere(orc):
     s = iso_close_setup()
-    n = compare_replay(gpu_hits(s, seed=3), orc.propagate_f64(s, seed=3), min_hits=1000)
+    n = compare_replay(gpu_hits(s, seed=3), orc.propagate_f64(s, seed=3), min_hits=1000, setup=s)
     assert n > 1000
 
 
 def test_replay_point_cone(orc):
     s = workloads.point_cone_setup(400_000)
-    compare_replay(gpu_hits(s, seed=11), orc.propagate_f64(s, seed=11), min_hits=1)
+    compare_replay(gpu_hits(s, seed=11), orc.propagate_f64(s, seed=11), min_hits=1, setup=s)
 
 
 def test_replay_cascade_on_pom_string(orc):
     s = cascade_small_setup()
-    compare_replay(gpu_hits(s, seed=5), orc.propagate_f64(s, seed=5), min_hits=50)
+    compare_replay(gpu_hits(s, seed=5), orc.propagate_f64(s, seed=5), min_hits=50, setup=s)
 
 
 @pytest.mark.parametrize("policy,exact", [("first", False), ("nearest", False), ("first", True)])
 def test_replay_mixed_sources(orc, policy, exact):
     s = mixed_setup(hit_policy=policy, exact_pole_rotation=exact)
-    compare_replay(gpu_hits(s, seed=17), orc.propagate_f64(s, seed=17), min_hits=1000)
+    compare_replay(gpu_hits(s, seed=17), orc.propagate_f64(s, seed=17), min_hits=1000, setup=s)
 
 
 def test_column_culling_matches_plain_scan():
