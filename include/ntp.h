@@ -207,6 +207,31 @@ ntp_status ntp_propagate(ntp_ctx* ctx, const ntp_source* sources, int32_t n_sour
                          ntp_hit* hits, uint64_t capacity, int32_t hits_on_device,
                          uint64_t* n_hits, uint64_t* n_photons_simulated);
 
+/* ntp_propagate without any allocation.  This entry point has no counterpart
+   in the reference.  It is for callers that cannot call cudaMalloc: a data-
+   taking or trigger process that reserves its device memory at start-up and
+   must not allocate afterwards (cudaMalloc synchronises the device and can
+   fail on fragmented memory), or a host framework whose device buffers all
+   come from its own pool.  Such a caller owns the output hit buffer (device
+   memory, 16-byte aligned) and passes the inputs as host descriptors, as for
+   ntp_set_medium / ntp_set_spectrum / ntp_set_targets / ntp_propagate; no
+   context is needed.  The kernel's scratch (counters, source table and prefix
+   sums, medium, spectrum and target tables) lives in a fixed 256 KiB device
+   array inside the library, so the call allocates nothing.  Limits: at most
+   1024 sources, 4096 targets, NTP_MAX_MEDIUM_KNOTS medium knots and
+   NTP_MAX_SPECTRUM_KNOTS spectrum knots; more is rejected with
+   NTP_ERR_INVALID.  The scratch is shared by all calls on a device: calls
+   that overlap on the GPU race and must be serialised by the caller.  The
+   first call on a device looks up the scratch address on that device (the
+   current device); make that first call before any stream capture.  Uses
+   opts->stream (NULL = the legacy default stream) and returns once the hit
+   count is known; the error text is ntp_last_error(NULL). */
+ntp_status ntp_propagate_noalloc(const ntp_medium_desc* medium, const ntp_spectrum_desc* spectrum,
+                                 const ntp_target* targets, int32_t n_targets,
+                                 const ntp_source* sources, int32_t n_sources, uint64_t seed,
+                                 const ntp_prop_opts* opts, ntp_hit* hits, uint64_t capacity,
+                                 uint64_t* n_hits, uint64_t* n_photons_simulated);
+
 /* Counters of the last ntp_propagate on this context (no reference
    counterpart beyond n_ph_sim of photon_prop_cuda.jl:758). */
 typedef struct ntp_run_stats {

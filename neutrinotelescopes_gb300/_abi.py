@@ -158,6 +158,7 @@ EXPORTED = (
     "ntp_set_spectrum",
     "ntp_set_targets",
     "ntp_propagate",
+    "ntp_propagate_noalloc",
     "ntp_get_run_stats",
     "ntp_make_hits",
     "ntp_calc_total_weight",
@@ -183,12 +184,16 @@ def _declare(lib: C.CDLL) -> None:
     lib.ntp_set_targets.argtypes = [vp, C.POINTER(NtpTarget), i32, C.POINTER(C.c_float), i32]
     lib.ntp_propagate.argtypes = [vp, C.POINTER(NtpSource), i32, u64, C.POINTER(NtpPropOpts), vp, u64, i32,
                                   C.POINTER(u64), C.POINTER(u64)]
+    lib.ntp_propagate_noalloc.argtypes = [C.POINTER(NtpMediumDesc), C.POINTER(NtpSpectrumDesc), C.POINTER(NtpTarget),
+                                          i32, C.POINTER(NtpSource), i32, u64, C.POINTER(NtpPropOpts), vp, u64,
+                                          C.POINTER(u64), C.POINTER(u64)]
     lib.ntp_get_run_stats.argtypes = [vp, C.POINTER(NtpRunStats)]
     lib.ntp_make_hits.argtypes = [vp, vp, u64, C.POINTER(C.c_double), vp, i32, vp]
     lib.ntp_calc_total_weight.argtypes = [vp, vp, u64, vp, vp, vp, vp, i32, vp]
     lib.ntp_set_wavelength_acceptance.argtypes = [vp, C.POINTER(C.c_double), C.POINTER(C.c_double), i32]
     lib.ntp_calc_time_residual.argtypes = [vp, vp, u64, C.POINTER(C.c_float), C.c_float, vp, i32, vp]
-    for name in ("ntp_set_medium", "ntp_set_spectrum", "ntp_set_targets", "ntp_propagate", "ntp_get_run_stats",
+    for name in ("ntp_set_medium", "ntp_set_spectrum", "ntp_set_targets", "ntp_propagate", "ntp_propagate_noalloc",
+                 "ntp_get_run_stats",
                  "ntp_make_hits",
                  "ntp_calc_total_weight", "ntp_set_wavelength_acceptance", "ntp_calc_time_residual"):
         getattr(lib, name).restype = C.c_int

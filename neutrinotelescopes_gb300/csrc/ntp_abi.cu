@@ -79,6 +79,8 @@ struct ntp_ctx {
     size_t stage2_bytes = 0;
 };
 
+const char* ntp_noalloc_last_error();
+
 namespace {
 
 std::string g_create_error;
@@ -213,7 +215,11 @@ void ntp_destroy(ntp_ctx* ctx) {
     delete ctx;
 }
 
-const char* ntp_last_error(const ntp_ctx* ctx) { return ctx ? ctx->err.c_str() : g_create_error.c_str(); }
+const char* ntp_last_error(const ntp_ctx* ctx) {
+    if (ctx) return ctx->err.c_str();
+    const char* na = ntp_noalloc_last_error();  // set when the last ntp_propagate_noalloc on this thread failed
+    return na[0] ? na : g_create_error.c_str();
+}
 
 ntp_status ntp_set_medium(ntp_ctx* ctx, const ntp_medium_desc* m) {
     if (!ctx) return NTP_ERR_INVALID;
