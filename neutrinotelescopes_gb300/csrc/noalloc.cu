@@ -223,6 +223,8 @@ extern "C" ntp_status ntp_propagate_noalloc(const ntp_medium_desc* m, const ntp_
     p.columns = nullptr;
     p.members = nullptr;
     p.n_columns = 0;
+    p.cell_start = nullptr;
+    p.cell_items = nullptr;
     p.medium = reinterpret_cast<const float4*>(base + kOffMedium);
     p.n_medium = m->n_knots;
     p.wl_min = m->wl_min;

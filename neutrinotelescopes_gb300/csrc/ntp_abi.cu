@@ -54,6 +54,10 @@ struct ntp_ctx {
     ntp::Column* d_cols = nullptr;  // vertical columns of targets (culling)
     int* d_members = nullptr;
     int n_cols = 0;
+    int* d_cell_start = nullptr;    // 2-D grid over the columns
+    int* d_cell_items = nullptr;
+    int grid_nx = 0, grid_ny = 0, n_cell_items = 0;
+    float grid_x0 = 0, grid_y0 = 0, grid_h = 0;
     double* d_axes = nullptr;  // PMT axes for the current orientation
     double* d_tgeo = nullptr;  // per-target tgeo for time residuals
 
@@ -203,6 +207,8 @@ void ntp_destroy(ntp_ctx* ctx) {
     dfree(ctx->d_tgeo);
     dfree(ctx->d_cols);
     dfree(ctx->d_members);
+    dfree(ctx->d_cell_start);
+    dfree(ctx->d_cell_items);
     dfree(ctx->d_acc_wl);
     dfree(ctx->d_acc);
     dfree(ctx->d_counters);
@@ -395,10 +401,60 @@ ntp_status ntp_set_targets(ntp_ctx* ctx, const ntp_target* t, int32_t n, const f
     dfree(ctx->d_cols);
     dfree(ctx->d_members);
     ctx->n_cols = 0;
+    dfree(ctx->d_cell_start);
+    dfree(ctx->d_cell_items);
+    ctx->grid_nx = ctx->grid_ny = ctx->n_cell_items = 0;
     if (use_cols) {
         NTP_CUDA(ctx, dupload(ctx->d_cols, cols.data(), cols.size(), ctx->stream));
         NTP_CUDA(ctx, dupload(ctx->d_members, members.data(), members.size(), ctx->stream));
         ctx->n_cols = static_cast<int>(cols.size());
+    }
+    if (use_cols && static_cast<int>(cols.size()) >= ntp::kGridMinColumns) {
+        // cells of side h over the axes' bounding box; each column goes into
+        // every cell its culling disk, widened by 0.5 m, overlaps
+        const float margin = 0.5f;
+        double x0 = 1e30, y0 = 1e30, x1 = -1e30, y1 = -1e30, rmax = 0;
+        for (const auto& c : cols) {
+            x0 = std::min(x0, static_cast<double>(c.cx));
+            x1 = std::max(x1, static_cast<double>(c.cx));
+            y0 = std::min(y0, static_cast<double>(c.cy));
+            y1 = std::max(y1, static_cast<double>(c.cy));
+            rmax = std::max(rmax, static_cast<double>(c.r_cull));
+        }
+        const double pad = rmax + margin + 1.0;
+        x0 -= pad; y0 -= pad; x1 += pad; y1 += pad;
+        double h = std::sqrt((x1 - x0) * (y1 - y0) / (4.0 * cols.size()));
+        h = std::max(h, 2.0 * (rmax + margin));
+        int nx = static_cast<int>(std::ceil((x1 - x0) / h)), ny = static_cast<int>(std::ceil((y1 - y0) / h));
+        while (static_cast<long long>(nx) * ny > 65536) {
+            h *= 1.5;
+            nx = static_cast<int>(std::ceil((x1 - x0) / h));
+            ny = static_cast<int>(std::ceil((y1 - y0) / h));
+        }
+        std::vector<std::vector<int>> cells(static_cast<size_t>(nx) * ny);
+        for (int ci = 0; ci < static_cast<int>(cols.size()); ++ci) {
+            const double r = cols[ci].r_cull + margin;
+            const int ax = std::max(0, static_cast<int>(std::floor((cols[ci].cx - r - x0) / h)));
+            const int bx = std::min(nx - 1, static_cast<int>(std::floor((cols[ci].cx + r - x0) / h)));
+            const int ay = std::max(0, static_cast<int>(std::floor((cols[ci].cy - r - y0) / h)));
+            const int by = std::min(ny - 1, static_cast<int>(std::floor((cols[ci].cy + r - y0) / h)));
+            for (int iy = ay; iy <= by; ++iy)
+                for (int ix = ax; ix <= bx; ++ix) cells[static_cast<size_t>(iy) * nx + ix].push_back(ci);
+        }
+        std::vector<int> start(cells.size() + 1, 0), items;
+        for (size_t c = 0; c < cells.size(); ++c) {
+            start[c] = static_cast<int>(items.size());
+            items.insert(items.end(), cells[c].begin(), cells[c].end());
+        }
+        start[cells.size()] = static_cast<int>(items.size());
+        NTP_CUDA(ctx, dupload(ctx->d_cell_start, start.data(), start.size(), ctx->stream));
+        NTP_CUDA(ctx, dupload(ctx->d_cell_items, items.data(), items.size(), ctx->stream));
+        ctx->grid_nx = nx;
+        ctx->grid_ny = ny;
+        ctx->n_cell_items = static_cast<int>(items.size());
+        ctx->grid_x0 = static_cast<float>(x0);
+        ctx->grid_y0 = static_cast<float>(y0);
+        ctx->grid_h = static_cast<float>(h);
     }
     NTP_CUDA(ctx, dupload(ctx->d_tgt, tg.data(), n, ctx->stream));
     NTP_CUDA(ctx, dupload(ctx->d_tgt_id, ids.data(), n, ctx->stream));
@@ -505,6 +561,14 @@ ntp_status ntp_propagate(ntp_ctx* ctx, const ntp_source* sources, int32_t n_sour
     p.columns = (ctx->n_cols > 0 && !(o.flags & NTP_FLAG_PLAIN_SCAN)) ? ctx->d_cols : nullptr;
     p.members = ctx->d_members;
     p.n_columns = ctx->n_cols;
+    p.cell_start = p.columns ? ctx->d_cell_start : nullptr;
+    p.cell_items = ctx->d_cell_items;
+    p.grid_nx = ctx->grid_nx;
+    p.grid_ny = ctx->grid_ny;
+    p.n_cell_items = ctx->n_cell_items;
+    p.grid_x0 = ctx->grid_x0;
+    p.grid_y0 = ctx->grid_y0;
+    p.grid_h = ctx->grid_h;
     p.medium = ctx->d_med;
     p.n_medium = ctx->n_med;
     p.wl_min = ctx->wl_min;

@@ -15,6 +15,8 @@ namespace ntp {
 constexpr int kPropBlock = 256;      // threads per block of the propagation kernel
 constexpr int kMaxSmemTargets = 8192;  // targets staged in shared memory (20 B each)
 constexpr int kMaxSmemColumns = 2048;  // columns staged in shared memory (32 B each)
+constexpr int kMaxSmemGridInts = 16384; // grid offsets + items staged in shared memory (4 B each)
+constexpr int kGridMinColumns = 9;      // below this many columns every column is tested
 
 // A vertical column of targets sharing (x, y): the unit of the geometric
 // culling.  Members are target indices sorted by z.
@@ -44,6 +46,14 @@ struct PropParams {
     const Column* columns;                // device; nullptr = scan every target
     const int* members;                   // device, target indices grouped by column
     int n_columns;
+
+    // 2-D grid over the column axes (used when cell_start != nullptr): cell
+    // (ix, iy) lists the columns whose culling disk, widened by a margin,
+    // overlaps it; a step walks the cells its horizontal projection crosses.
+    const int* cell_start;                // device, nx * ny + 1 offsets into cell_items
+    const int* cell_items;                // device, column indices
+    int grid_nx, grid_ny, n_cell_items;
+    float grid_x0, grid_y0, grid_h;
 
     const float4* medium;                 // device, per knot (n, v_group, l_scatter, 0)
     int n_medium;

@@ -138,6 +138,62 @@ __device__ __forceinline__ void column_candidates(const Column& C, const int* __
     }
 }
 
+// Walks the cells of the column grid that the horizontal projection of the
+// segment pos + t dir, 0 <= t <= step, crosses (Amanatides-Woo), testing the
+// columns listed in each.  A column listed in several visited cells is
+// tested more than once, which does not change the result.  The walk is
+// bounded by nx + ny + 2 cells.
+__device__ __forceinline__ void grid_candidates(const PropParams& p, const int* __restrict__ cstart,
+                                                const int* __restrict__ citems, const Column* __restrict__ cols,
+                                                const int* __restrict__ mem, const float4* __restrict__ tg,
+                                                const V3 pos, const V3 dir, float step, int& hit_t, float& hit_d) {
+    const float h = p.grid_h, inv_h = 1.0f / h;
+    const float x1 = p.grid_x0 + h * static_cast<float>(p.grid_nx);
+    const float y1 = p.grid_y0 + h * static_cast<float>(p.grid_ny);
+    // clip the segment to the grid box
+    float t_in = 0.0f, t_out = step;
+    if (dir.x != 0.0f) {
+        const float ta = (p.grid_x0 - pos.x) / dir.x, tb = (x1 - pos.x) / dir.x;
+        t_in = fmaxf(t_in, fminf(ta, tb));
+        t_out = fminf(t_out, fmaxf(ta, tb));
+    } else if (pos.x < p.grid_x0 || pos.x > x1) {
+        return;
+    }
+    if (dir.y != 0.0f) {
+        const float ta = (p.grid_y0 - pos.y) / dir.y, tb = (y1 - pos.y) / dir.y;
+        t_in = fmaxf(t_in, fminf(ta, tb));
+        t_out = fminf(t_out, fmaxf(ta, tb));
+    } else if (pos.y < p.grid_y0 || pos.y > y1) {
+        return;
+    }
+    if (!(t_in <= t_out)) return;
+    const float sx = fmaf(t_in, dir.x, pos.x), sy = fmaf(t_in, dir.y, pos.y);
+    int ix = min(max(static_cast<int>(floorf((sx - p.grid_x0) * inv_h)), 0), p.grid_nx - 1);
+    int iy = min(max(static_cast<int>(floorf((sy - p.grid_y0) * inv_h)), 0), p.grid_ny - 1);
+    const int stx = dir.x > 0.0f ? 1 : -1, sty = dir.y > 0.0f ? 1 : -1;
+    const float inf = __int_as_float(0x7f800000);
+    float tmx = dir.x != 0.0f ? (p.grid_x0 + h * static_cast<float>(ix + (dir.x > 0.0f)) - pos.x) / dir.x : inf;
+    float tmy = dir.y != 0.0f ? (p.grid_y0 + h * static_cast<float>(iy + (dir.y > 0.0f)) - pos.y) / dir.y : inf;
+    const float tdx = dir.x != 0.0f ? h / fabsf(dir.x) : inf;
+    const float tdy = dir.y != 0.0f ? h / fabsf(dir.y) : inf;
+    for (int guard = p.grid_nx + p.grid_ny + 2; guard > 0; --guard) {
+        const int c = iy * p.grid_nx + ix;
+        for (int k = cstart[c]; k < cstart[c + 1]; ++k)
+            column_candidates(cols[citems[k]], mem, tg, pos, dir, step, p.hit_policy, hit_t, hit_d);
+        if (tmx < tmy) {
+            if (tmx > t_out) break;
+            ix += stx;
+            if (ix < 0 || ix >= p.grid_nx) break;
+            tmx += tdx;
+        } else {
+            if (tmy > t_out) break;
+            iy += sty;
+            if (iy < 0 || iy >= p.grid_ny) break;
+            tmy += tdy;
+        }
+    }
+}
+
 // initialize_photon_state methods, photon_prop_cuda.jl:133-200 and
 // sample_cherenkov_direction :107-125.
 __device__ __forceinline__ void init_photon(Photon& ph, const ntp_source* __restrict__ sources,
@@ -237,7 +293,11 @@ __global__ void __launch_bounds__(kPropBlock, kMinBlocks) propagate_kernel(const
     Column* s_col = reinterpret_cast<Column*>(s_tgt + nt_s);
     uint32_t* s_tid = reinterpret_cast<uint32_t*>(s_col + nc_s);
     int* s_mem = reinterpret_cast<int*>(s_tid + nt_s);
-    float* s_spec = reinterpret_cast<float*>(s_mem + (nc_s ? nt_s : 0));
+    const bool grid_s = nc_s && p.cell_start && (p.grid_nx * p.grid_ny + 1 + p.n_cell_items) <= kMaxSmemGridInts;
+    const int ng_s = grid_s ? p.grid_nx * p.grid_ny + 1 : 0;
+    int* s_cstart = s_mem + (nc_s ? nt_s : 0);
+    int* s_citems = s_cstart + ng_s;
+    float* s_spec = reinterpret_cast<float*>(s_citems + (grid_s ? p.n_cell_items : 0));
 
     for (int i = threadIdx.x; i < p.n_medium; i += blockDim.x) s_med[i] = p.medium[i];
     for (int i = threadIdx.x; i < p.n_spec; i += blockDim.x) s_spec[i] = p.spec_knots[i];
@@ -248,7 +308,13 @@ __global__ void __launch_bounds__(kPropBlock, kMinBlocks) propagate_kernel(const
     for (int i = threadIdx.x; i < nc_s; i += blockDim.x) s_col[i] = p.columns[i];
     if (nc_s)
         for (int i = threadIdx.x; i < nt_s; i += blockDim.x) s_mem[i] = p.members[i];
+    if (grid_s) {
+        for (int i = threadIdx.x; i < ng_s; i += blockDim.x) s_cstart[i] = p.cell_start[i];
+        for (int i = threadIdx.x; i < p.n_cell_items; i += blockDim.x) s_citems[i] = p.cell_items[i];
+    }
     __syncthreads();
+    const int* cstart = grid_s ? s_cstart : p.cell_start;
+    const int* citems = grid_s ? s_citems : p.cell_items;
     const float4* tg = p.targets_in_smem ? s_tgt : p.targets;
     const uint32_t* tid = p.targets_in_smem ? s_tid : p.target_ids;
     const Column* cols = p.columns ? (nc_s ? s_col : p.columns) : nullptr;
@@ -306,7 +372,9 @@ __global__ void __launch_bounds__(kPropBlock, kMinBlocks) propagate_kernel(const
 
             // check_intersection over the targets, photon_prop_cuda.jl:233-271, :460-468
             float hit_d = step;
-            if (cols) {
+            if (cols && cstart) {
+                grid_candidates(p, cstart, citems, cols, mem, tg, ph.pos, ph.dir, step, hit_t, hit_d);
+            } else if (cols) {
                 for (int c = 0; c < p.n_columns; ++c)
                     column_candidates(cols[c], mem, tg, ph.pos, ph.dir, step, p.hit_policy, hit_t, hit_d);
             } else {
@@ -385,8 +453,11 @@ size_t prop_smem_bytes(const PropParams& p) {
     size_t b = sizeof(float4) * static_cast<size_t>(p.n_medium);
     if (p.targets_in_smem) {
         b += (sizeof(float4) + sizeof(uint32_t)) * static_cast<size_t>(p.n_targets);
-        if (p.columns)
+        if (p.columns) {
             b += sizeof(Column) * static_cast<size_t>(p.n_columns) + sizeof(int) * static_cast<size_t>(p.n_targets);
+            const long long g = p.cell_start ? static_cast<long long>(p.grid_nx) * p.grid_ny + 1 + p.n_cell_items : 0;
+            if (p.cell_start && g <= kMaxSmemGridInts) b += sizeof(int) * static_cast<size_t>(g);
+        }
     }
     b += sizeof(float) * static_cast<size_t>(p.n_spec);
     return b;

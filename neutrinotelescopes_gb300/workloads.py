@@ -4,6 +4,10 @@ point_cone:      1e6 photons from the origin on a 41.2 degree cone around +z,
                  1/lambda^2 spectrum on 300-600 nm, one 0.21 m sphere at
                  (0, 0, 10 m), simple water (n 1.35, group index 1.39, absorption
                  30 m at 400 nm, scattering 50 m, 0.85 HG(0.97) + 0.15 Rayleigh).
+string_grid:     nx x ny vertical strings spaced `spacing` m on a square grid,
+                 n_modules per string spaced dz m (the serving detector is
+                 10 x 10 strings, 50 m, 20 modules 15 m apart; the hybrid
+                 detector 100 strings x 80 modules).
 cascade_string:  electromagnetic cascades, energy log-uniform 1e3-1e5 GeV,
                  1.3e5 photons/GeV, gamma longitudinal profile a = 2 + 0.6 ln E,
                  b = 0.63, radiation length 0.36 m, isotropic direction, vertex
@@ -55,3 +59,16 @@ def cascade_string_setup(n_cascades: int = 4, seed: int = 1, photon_scale: float
     srcs = cascade_sources(n_cascades, rng, photon_scale=photon_scale)
     return PhotonPropSetup(srcs, targets, make_simple_water(), InverseSquareSpectrum(300.0, 600.0),
                            wavelength_acceptance=p_one_pmt_acc.resampled(300.0, 600.0, 31), **kw)
+
+
+def string_grid(nx: int = 10, ny: int = 10, spacing: float = 50.0, n_modules: int = 20, dz: float = 15.0,
+                z0: float = 0.0):
+    """MultiPMTDetector modules of nx * ny strings centred on x = y = 0, module ids 1..N."""
+    targets = []
+    for j in range(ny):
+        for i in range(nx):
+            x = (i - (nx - 1) / 2) * spacing
+            y = (j - (ny - 1) / 2) * spacing
+            targets += string_of_modules(n_modules, dz, x=x, y=y, z_start=z0, pmt_area=PMT_AREA,
+                                         id_offset=len(targets))
+    return targets

@@ -142,6 +142,23 @@ def test_column_culling_matches_plain_scan():
     assert len(ha) > 100 and ha.tobytes() == hb.tobytes()
 
 
+def test_grid_culling_matches_plain_scan_on_string_grid():
+    # 10 x 10 strings, 20 modules each: the 2-D grid walk keeps exactly the hits of the full scan
+    targets = workloads.string_grid(10, 10, 50.0, 20, 15.0)
+    rng = np.random.default_rng(5)
+    srcs = workloads.cascade_sources(3, rng, photon_scale=2e-4, string_z=(0.0, 285.0), distance=8.0)
+    m = nt.make_simple_water()
+    for policy in ("first", "nearest"):
+        a = nt.PhotonPropSetup(srcs, targets, m, nt.InverseSquareSpectrum(300.0, 600.0), hit_policy=policy)
+        b = nt.PhotonPropSetup(srcs, targets, m, nt.InverseSquareSpectrum(300.0, 600.0), hit_policy=policy,
+                               plain_scan=True)
+        ha, hb = gpu_hits(a, seed=21), gpu_hits(b, seed=21)
+        assert len(ha) > 100
+        assert ha.tobytes() == hb.tobytes()
+        a.close()
+        b.close()
+
+
 def test_axicone_pole_quirk_half_cone():
     # rot_from_ez_fast at a = e_z (utils.jl:230-232): every photon of a cone about +z has y >= 0
     src = nt.AxiconeEmitter((0.0, 0.0, 0.0), (0.0, 0.0, 1.0), 0.0, 100_000, 0.7)
