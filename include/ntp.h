@@ -276,6 +276,71 @@ ntp_status ntp_calc_time_residual(ntp_ctx* ctx, const ntp_hit* hits, uint64_t n_
                                   const float source_position[3], float n800,
                                   double* tres, int32_t buffers_on_device, void* stream);
 
+/* ------------------------------------------------------------------ serving
+ * Continuous-batching event server (no reference counterpart; the reference
+ * runs one propagate_photons per event, photon_prop_cuda.jl:804-817).  Each
+ * event is one source; its photons draw from the Philox stream of its
+ * event_id, so an event's hits do not depend on which events share its batch.
+ * Hits stay on the device in an arena of hbm_budget_bytes: an event is
+ * admitted (FIFO) when a batch slot is free and its hit reservation fits in
+ * the arena, and keeps its hits there until ntp_server_release.  Admitted
+ * events are packed into one propagation launch per batch (a CUDA graph
+ * replayed with new parameters); two batch slots on two streams let a new
+ * batch start while the previous one drains.  An event whose hits exceed its
+ * reservation is re-run alone with the exact size (same hits).  The server
+ * uses the medium, spectrum and targets of its context, which must not change
+ * while the server exists. */
+typedef struct ntp_server ntp_server;
+
+typedef struct ntp_server_config {
+    uint64_t hbm_budget_bytes;      /* hit arena size (64 bytes per hit)                     */
+    uint64_t seed;                  /* Philox key of every event                             */
+    int32_t max_events_per_batch;   /* <= 65536                                              */
+    int32_t max_steps;              /* scatter steps per photon (15 in the reference)        */
+    int32_t hit_policy;             /* enum ntp_hit_policy                                   */
+    int32_t flags;                  /* enum ntp_prop_flags                                   */
+    double reserve_hits_per_photon; /* initial hit reservation per photon                    */
+    uint64_t min_reserve_hits;      /* smallest reservation of an event                      */
+    uint64_t max_batch_photons;     /* photons per batch before it is closed                 */
+} ntp_server_config;
+
+typedef struct ntp_event_result {
+    uint32_t event_id;
+    int32_t status;         /* NTP_OK, or NTP_ERR_NOMEM if the event can never fit the arena */
+    uint64_t n_hits;
+    uint64_t n_photons;
+    const ntp_hit* hits;    /* device pointer into the arena, valid until ntp_server_release */
+    double t_submit;        /* seconds on the server's clock                                */
+    double t_launch;        /* launch of the batch that produced the hits                   */
+    double t_done;          /* completion observed by ntp_server_poll                       */
+    int32_t reruns;         /* re-runs after a reservation overflow                         */
+    int32_t batch_events;   /* events in that batch                                          */
+} ntp_event_result;
+
+typedef struct ntp_server_stats {
+    uint64_t queued, running, completed, released;
+    uint64_t batches, photons;
+    uint64_t arena_hits, arena_reserved_hits;
+    double clock;           /* the server's clock now (seconds)                             */
+} ntp_server_stats;
+
+ntp_status ntp_server_create(ntp_ctx* ctx, const ntp_server_config* config, ntp_server** out);
+void ntp_server_destroy(ntp_server* server);
+/* Queues one event (stamped with the submit time). */
+ntp_status ntp_server_submit(ntp_server* server, uint32_t event_id, const ntp_source* source);
+/* Advances the loop (collects finished batches, admits queued events, launches
+   batches) and returns up to max finished events in out, waiting up to
+   timeout_us for one if none is ready.  Returns the number written, or -1
+   on a CUDA error (text in ntp_last_error of the server's context). */
+int32_t ntp_server_poll(ntp_server* server, ntp_event_result* out, int32_t max, int32_t timeout_us);
+/* Copies up to max of a finished event's hits from the arena into host
+   memory; *n receives the event's hit count. */
+ntp_status ntp_server_copy_hits(ntp_server* server, uint32_t event_id, ntp_hit* host_dst, uint64_t max,
+                                uint64_t* n);
+/* Frees an event's hits in the arena. */
+ntp_status ntp_server_release(ntp_server* server, uint32_t event_id);
+ntp_status ntp_server_get_stats(const ntp_server* server, ntp_server_stats* out);
+
 #ifdef __cplusplus
 }
 #endif

@@ -128,6 +128,49 @@ class NtpRunStats(C.Structure):
     ]
 
 
+class NtpServerConfig(C.Structure):
+    _fields_ = [
+        ("hbm_budget_bytes", C.c_uint64),
+        ("seed", C.c_uint64),
+        ("max_events_per_batch", C.c_int32),
+        ("max_steps", C.c_int32),
+        ("hit_policy", C.c_int32),
+        ("flags", C.c_int32),
+        ("reserve_hits_per_photon", C.c_double),
+        ("min_reserve_hits", C.c_uint64),
+        ("max_batch_photons", C.c_uint64),
+    ]
+
+
+class NtpEventResult(C.Structure):
+    _fields_ = [
+        ("event_id", C.c_uint32),
+        ("status", C.c_int32),
+        ("n_hits", C.c_uint64),
+        ("n_photons", C.c_uint64),
+        ("hits", C.c_void_p),
+        ("t_submit", C.c_double),
+        ("t_launch", C.c_double),
+        ("t_done", C.c_double),
+        ("reruns", C.c_int32),
+        ("batch_events", C.c_int32),
+    ]
+
+
+class NtpServerStats(C.Structure):
+    _fields_ = [
+        ("queued", C.c_uint64),
+        ("running", C.c_uint64),
+        ("completed", C.c_uint64),
+        ("released", C.c_uint64),
+        ("batches", C.c_uint64),
+        ("photons", C.c_uint64),
+        ("arena_hits", C.c_uint64),
+        ("arena_reserved_hits", C.c_uint64),
+        ("clock", C.c_double),
+    ]
+
+
 assert C.sizeof(NtpSource) == 64
 assert C.sizeof(NtpTarget) == 48
 
@@ -164,6 +207,13 @@ EXPORTED = (
     "ntp_calc_total_weight",
     "ntp_set_wavelength_acceptance",
     "ntp_calc_time_residual",
+    "ntp_server_create",
+    "ntp_server_destroy",
+    "ntp_server_submit",
+    "ntp_server_poll",
+    "ntp_server_copy_hits",
+    "ntp_server_release",
+    "ntp_server_get_stats",
 )
 
 _lib = None
@@ -192,6 +242,18 @@ def _declare(lib: C.CDLL) -> None:
     lib.ntp_calc_total_weight.argtypes = [vp, vp, u64, vp, vp, vp, vp, i32, vp]
     lib.ntp_set_wavelength_acceptance.argtypes = [vp, C.POINTER(C.c_double), C.POINTER(C.c_double), i32]
     lib.ntp_calc_time_residual.argtypes = [vp, vp, u64, C.POINTER(C.c_float), C.c_float, vp, i32, vp]
+    lib.ntp_server_create.argtypes = [vp, C.POINTER(NtpServerConfig), C.POINTER(vp)]
+    lib.ntp_server_destroy.argtypes = [vp]
+    lib.ntp_server_destroy.restype = None
+    lib.ntp_server_submit.argtypes = [vp, C.c_uint32, C.POINTER(NtpSource)]
+    lib.ntp_server_poll.argtypes = [vp, C.POINTER(NtpEventResult), i32, i32]
+    lib.ntp_server_poll.restype = i32
+    lib.ntp_server_copy_hits.argtypes = [vp, C.c_uint32, vp, u64, C.POINTER(u64)]
+    lib.ntp_server_release.argtypes = [vp, C.c_uint32]
+    lib.ntp_server_get_stats.argtypes = [vp, C.POINTER(NtpServerStats)]
+    for name in ("ntp_server_create", "ntp_server_submit", "ntp_server_copy_hits", "ntp_server_release",
+                 "ntp_server_get_stats"):
+        getattr(lib, name).restype = C.c_int
     for name in ("ntp_set_medium", "ntp_set_spectrum", "ntp_set_targets", "ntp_propagate", "ntp_propagate_noalloc",
                  "ntp_get_run_stats",
                  "ntp_make_hits",

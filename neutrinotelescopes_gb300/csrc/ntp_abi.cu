@@ -136,6 +136,49 @@ bool finite(float x) { return std::isfinite(x); }
 
 cudaStream_t pick_stream(ntp_ctx* ctx, void* s) { return s ? static_cast<cudaStream_t>(s) : ctx->stream; }
 
+}  // namespace
+
+namespace ntp {
+
+bool fill_world_params(const ntp_ctx* ctx, PropParams& p) {
+    if (!ctx->have_medium || !ctx->have_spec || !ctx->have_targets) return false;
+    p.targets = ctx->d_tgt;
+    p.target_ids = ctx->d_tgt_id;
+    p.n_targets = ctx->n_tgt;
+    p.targets_in_smem = ctx->n_tgt <= kMaxSmemTargets ? 1 : 0;
+    p.columns = ctx->n_cols > 0 ? ctx->d_cols : nullptr;
+    p.members = ctx->d_members;
+    p.n_columns = ctx->n_cols;
+    p.cell_start = p.columns ? ctx->d_cell_start : nullptr;
+    p.cell_items = ctx->d_cell_items;
+    p.grid_nx = ctx->grid_nx;
+    p.grid_ny = ctx->grid_ny;
+    p.n_cell_items = ctx->n_cell_items;
+    p.grid_x0 = ctx->grid_x0;
+    p.grid_y0 = ctx->grid_y0;
+    p.grid_h = ctx->grid_h;
+    p.medium = ctx->d_med;
+    p.n_medium = ctx->n_med;
+    p.wl_min = ctx->wl_min;
+    p.medium_scale = static_cast<float>(ctx->n_med - 1) / (ctx->wl_max - ctx->wl_min);
+    p.spec_kind = ctx->spec_kind;
+    p.n_spec = ctx->n_spec;
+    p.spec_knots = ctx->d_spec;
+    p.spec_p0 = ctx->spec_p0;
+    p.spec_p1 = ctx->spec_p1;
+    p.hg_g = ctx->hg_g;
+    p.rayleigh_fraction = ctx->f_ray;
+    return true;
+}
+
+int ctx_device(const ntp_ctx* ctx) { return ctx->device; }
+int ctx_num_sms(const ntp_ctx* ctx) { return ctx->num_sms; }
+void set_ctx_error(ntp_ctx* ctx, const char* msg) { ctx->err = msg; }
+
+}  // namespace ntp
+
+namespace {
+
 ntp::HitTargetTable hit_table(const ntp_ctx* ctx) {
     ntp::HitTargetTable t;
     t.sorted_ids = ctx->d_sorted;

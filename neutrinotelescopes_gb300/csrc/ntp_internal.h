@@ -72,6 +72,18 @@ struct PropParams {
     int exact_pole;
     uint2 key;
 
+    // Philox stream word per source (nullptr: the source index).  The serving
+    // loop passes event ids, so an event draws the same photons whatever
+    // batch it is simulated in.
+    const uint32_t* src_stream;
+
+    // Per-source output (serving): when src_hit_count != nullptr, hits of
+    // source s go to hits[src_hit_base[s] + k] for k < src_hit_cap[s], with
+    // src_hit_count[s] counting every hit of s (exact even past the cap).
+    unsigned long long* src_hit_count;
+    const unsigned long long* src_hit_base;
+    const unsigned long long* src_hit_cap;
+
     ntp_hit* hits;                        // device
     unsigned long long capacity;
     unsigned long long* counters;         // device: [0] photons claimed, [1] hits, [2] photons done, [3] photon-steps
@@ -82,6 +94,15 @@ struct PropParams {
 size_t prop_smem_bytes(const PropParams& p);
 cudaError_t launch_propagate(const PropParams& p, int grid, cudaStream_t stream);
 cudaError_t propagate_occupancy(const PropParams& p, int* blocks_per_sm);
+// the kernel launch_propagate uses (for CUDA-graph kernel-node updates)
+const void* propagate_kernel_fn();
+
+// Medium / spectrum / target part of the kernel parameters from a context
+// whose tables are set (ntp_abi.cu); returns false if a table is missing.
+bool fill_world_params(const ntp_ctx* ctx, PropParams& p);
+int ctx_device(const ntp_ctx* ctx);
+int ctx_num_sms(const ntp_ctx* ctx);
+void set_ctx_error(ntp_ctx* ctx, const char* msg);
 
 // Hit post-processing (make_hits / weights / time residual).
 struct HitTargetTable {

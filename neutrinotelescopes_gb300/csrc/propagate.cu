@@ -30,6 +30,7 @@ struct Photon {
     uint32_t src;
     uint32_t pk_lo, pk_hi;  // photon index within its source
     int step;
+    int slot;               // index of the source in this launch
 };
 
 __device__ __forceinline__ int source_of(const unsigned long long* prefix, int n_src,
@@ -201,7 +202,8 @@ __device__ __forceinline__ void init_photon(Photon& ph, const ntp_source* __rest
                                          const float4* medium, unsigned long long gid, int s) {
     const ntp_source* src = sources + s;
     const unsigned long long pk = gid - __ldg(p.prefix + s);
-    ph.src = static_cast<uint32_t>(s);
+    ph.src = p.src_stream ? __ldg(p.src_stream + s) : static_cast<uint32_t>(s);
+    ph.slot = s;
     ph.pk_lo = static_cast<uint32_t>(pk);
     ph.pk_hi = static_cast<uint32_t>(pk >> 32);
     const uint4 base = make_uint4(kDrawInitA, ph.pk_lo, ph.pk_hi, ph.src);
@@ -418,19 +420,35 @@ __global__ void __launch_bounds__(kPropBlock, kMinBlocks) propagate_kernel(const
         }
 
         if (hit) {
-            // one atomic for the lanes of this warp that hit in this step
-            const unsigned hm = __activemask();
+            // one atomic for the lanes of this warp that hit in this step (per
+            // source in the per-source output mode)
+            const unsigned act = __activemask();
+            const unsigned hm = p.src_hit_count ? __match_any_sync(act, ph.slot) : act;
             const int leader = __ffs(hm) - 1;
             unsigned long long base = 0;
-            if (static_cast<int>(lane) == leader) base = atomicAdd(p.counters + 1, static_cast<unsigned long long>(__popc(hm)));
+            if (static_cast<int>(lane) == leader) {
+                const unsigned long long n = static_cast<unsigned long long>(__popc(hm));
+                if (p.src_hit_count) {
+                    base = atomicAdd(p.src_hit_count + ph.slot, n);
+                    atomicAdd(p.counters + 1, n);
+                } else {
+                    base = atomicAdd(p.counters + 1, n);
+                }
+            }
             base = __shfl_sync(hm, base, leader);
-            const unsigned long long slot = base + __popc(hm & lt_mask);
-            if (slot < p.capacity) {
+            unsigned long long slot = base + __popc(hm & lt_mask);
+            bool room = slot < p.capacity;
+            if (p.src_hit_count) {
+                room = slot < __ldg(p.src_hit_cap + ph.slot);
+                slot += __ldg(p.src_hit_base + ph.slot);
+            }
+            if (room) {
                 float4* o = reinterpret_cast<float4*>(p.hits + slot);
                 __stcs(o + 0, make_float4(ph.pos.x, ph.pos.y, ph.pos.z, ph.time));
                 __stcs(o + 1, make_float4(ph.dir.x, ph.dir.y, ph.dir.z, ph.wl));
                 __stcs(o + 2, make_float4(ph.init_dir.x, ph.init_dir.y, ph.init_dir.z, ph.dist));
-                __stcs(reinterpret_cast<uint4*>(o + 3), make_uint4(tid[hit_t], ph.src, ph.pk_lo, ph.pk_hi));
+                __stcs(reinterpret_cast<uint4*>(o + 3),
+                       make_uint4(tid[hit_t], p.src_stream ? ph.src : static_cast<uint32_t>(ph.slot), ph.pk_lo, ph.pk_hi));
             }
             active = false;
             ++done;
@@ -483,6 +501,11 @@ static cudaError_t occupancy_of(const PropParams& p, int* blocks_per_sm) {
 
 cudaError_t propagate_occupancy(const PropParams& p, int* blocks_per_sm) {
     return use_four_blocks() ? occupancy_of<4>(p, blocks_per_sm) : occupancy_of<3>(p, blocks_per_sm);
+}
+
+const void* propagate_kernel_fn() {
+    return use_four_blocks() ? reinterpret_cast<const void*>(&propagate_kernel<4>)
+                             : reinterpret_cast<const void*>(&propagate_kernel<3>);
 }
 
 cudaError_t launch_propagate(const PropParams& p, int grid, cudaStream_t stream) {
