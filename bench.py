@@ -57,6 +57,8 @@ def parse():
     ap.add_argument("--cpu-seconds", type=float, default=10.0, help="target length of the CPU baseline sample")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--e2e-steps", type=int, default=3)
+    ap.add_argument("--serving-requests", type=int, default=4096,
+                    help="requests of the serving measurement (0 = skip)")
     ap.add_argument("--small", action="store_true",
                     help="profiling case: one cascade at 1% of its photons, 64 MB hit buffer, 256 MB L2 flush")
     return ap.parse_args()
@@ -116,6 +118,58 @@ class ClockSampler:
                     reasons.add(name)
         return {"sm_mhz": statistics.median(r[0] for r in loaded), "sm_max_mhz": max(r[1] for r in rows),
                 "power_w_max": pmax, "samples": len(loaded), "reasons": sorted(reasons)}
+
+
+def serving_bench(n_requests: int, budget_bytes: int = 120 * 10 ** 9) -> dict:
+    """Serving workload: n_requests cascade events (1e4-1e8 photons, Poisson
+    arrivals at 200/s) on the 10 x 10 string detector, through the
+    continuous-batching server with a 120 GB hit arena.  Two passes: all
+    requests at once (throughput, events/s), then the arrivals replayed in
+    real time (latency p50 / p99 at 200/s)."""
+    import numpy as np
+    from neutrinotelescopes_gb300 import workloads
+    from neutrinotelescopes_gb300.serving import EventServer
+    reqs = workloads.serving_requests(n_requests)
+    setup = workloads.serving_setup()
+    photons = sum(r[2].photons for r in reqs)
+    out = {"workload": f"{n_requests} cascade events, photons log-uniform 1e4-1e8 ({photons:.3g} in total), vertex "
+                       "uniform in a 100 m cube, 10 x 10 strings x 20 modules, hits kept on the device",
+           "hbm_budget_bytes": budget_bytes}
+    # saturated: every request queued at t = 0
+    srv = EventServer(setup, hbm_budget_bytes=budget_bytes, seed=workloads.SEED_BASE + 2)
+    for _, eid, src in reqs:
+        srv.submit(eid, src)
+    t0 = srv.stats().clock
+    res = srv.run_all()
+    t1 = max(r.t_done for r in res)
+    st = srv.stats()
+    out["saturated"] = {"events_per_s": len(res) / (t1 - t0), "photons_per_s": photons / (t1 - t0),
+                        "batches": st.batches, "reruns": int(sum(r.reruns for r in res)),
+                        "hits": int(sum(r.n_hits for r in res)), "seconds": t1 - t0}
+    srv.close()
+    # real time: arrivals replayed on the server clock, results released on completion
+    srv = EventServer(setup, hbm_budget_bytes=budget_bytes, seed=workloads.SEED_BASE + 2)
+    start = srv.stats().clock
+    i, lat, done = 0, [], 0
+    while done < len(reqs):
+        now = srv.stats().clock - start
+        while i < len(reqs) and reqs[i][0] <= now:
+            srv.submit(reqs[i][1], reqs[i][2])
+            i += 1
+        wait_us = int(max(0.0, min(1e-3, (reqs[i][0] - now) if i < len(reqs) else 1e-3)) * 1e6)
+        for r in srv.poll(wait_us):
+            lat.append(r.t_done - r.t_submit)
+            srv.release(r.event_id)
+            done += 1
+    span = srv.stats().clock - start
+    lat = np.array(lat)
+    out["realtime"] = {"arrival_rate_hz": 200.0, "events_per_s": len(lat) / span,
+                       "latency_p50_ms": float(np.percentile(lat, 50) * 1e3),
+                       "latency_p99_ms": float(np.percentile(lat, 99) * 1e3),
+                       "latency_max_ms": float(lat.max() * 1e3), "batches": srv.stats().batches}
+    srv.close()
+    setup.close()
+    return out
 
 
 def dist_setup():
@@ -297,11 +351,16 @@ def main():
            "roofline": roofline, "clocks": clocks,
            "e2e": {"value": e2e_val, "unit": METRIC, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
            "gpu_launches": args.steps}
+    setup.close()
+    del hits, flush
+    torch.cuda.empty_cache()
+    if args.serving_requests > 0 and not args.small:
+        out["serving"] = serving_bench(args.serving_requests)
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
-        out["cpu_baseline"] = cpu_baseline(setup, args.cpu_seconds, os.cpu_count() or 1)
+        out["cpu_baseline"] = cpu_baseline(workloads.cascade_string_setup(N_CASCADES, WORKLOAD_SEED),
+                                           args.cpu_seconds, os.cpu_count() or 1)
     if rank == 0:
         print(json.dumps(out))
-    setup.close()
     if world > 1:
         import torch.distributed as dist
         dist.destroy_process_group()

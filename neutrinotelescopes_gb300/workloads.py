@@ -72,3 +72,34 @@ def string_grid(nx: int = 10, ny: int = 10, spacing: float = 50.0, n_modules: in
             targets += string_of_modules(n_modules, dz, x=x, y=y, z_start=z0, pmt_area=PMT_AREA,
                                          id_offset=len(targets))
     return targets
+
+
+def serving_requests(n: int = 4096, seed: int = 2, rate_hz: float = 200.0, ph_lo: float = 1e4, ph_hi: float = 1e8,
+                     cube: float = 100.0, centre=(0.0, 0.0, 142.5), photons_per_gev: float = 1.3e5):
+    """Event requests of the serving workload: Poisson arrivals at rate_hz,
+    photon counts log-uniform in [ph_lo, ph_hi], cascades (gamma profile a =
+    2 + 0.6 ln E with E = photons / photons_per_gev, clamped to E >= 1 GeV so
+    that a >= 2, b = 0.63, radiation length 0.36 m), isotropic direction,
+    vertex uniform in a cube of side ``cube`` around ``centre``.
+    Returns [(arrival_time_s, event_id, source)]."""
+    rng = np.random.default_rng(seed)
+    t = np.cumsum(rng.exponential(1.0 / rate_hz, n))
+    out = []
+    for i in range(n):
+        photons = int(10 ** rng.uniform(np.log10(ph_lo), np.log10(ph_hi)))
+        e = max(photons / photons_per_gev, 1.0)
+        ct = rng.uniform(-1, 1)
+        phi = rng.uniform(0, 2 * np.pi)
+        st = np.sqrt(1 - ct * ct)
+        pos = tuple(c + rng.uniform(-cube / 2, cube / 2) for c in centre)
+        lp = LongitudinalParameterisation(a=float(np.float32(2.0 + 0.6 * np.log(e))), b=0.63, lrad=0.36)
+        src = ExtendedCherenkovEmitter(pos, (st * np.cos(phi), st * np.sin(phi), ct), 0.0, photons, lp)
+        out.append((float(t[i]), i + 1, src))
+    return out
+
+
+def serving_setup(**kw) -> PhotonPropSetup:
+    """The serving detector: 10 x 10 strings, 50 m apart, 20 modules 15 m apart, simple water."""
+    return PhotonPropSetup([], string_grid(10, 10, 50.0, 20, 15.0), make_simple_water(),
+                           InverseSquareSpectrum(300.0, 600.0),
+                           wavelength_acceptance=p_one_pmt_acc.resampled(300.0, 600.0, 31), **kw)
