@@ -136,7 +136,10 @@ def serving_bench(n_requests: int, budget_bytes: int = 120 * 10 ** 9) -> dict:
                        "uniform in a 100 m cube, 10 x 10 strings x 20 modules, hits kept on the device",
            "hbm_budget_bytes": budget_bytes}
     # saturated: every request queued at t = 0
-    srv = EventServer(setup, hbm_budget_bytes=budget_bytes, seed=workloads.SEED_BASE + 2)
+    kw = dict(hbm_budget_bytes=budget_bytes, seed=workloads.SEED_BASE + 2, reserve_hits_per_photon=5e-3,
+              min_reserve_hits=4096, max_batch_photons=200_000_000)
+    out["server"] = {k: v for k, v in kw.items() if k != "seed"}
+    srv = EventServer(setup, **kw)
     for _, eid, src in reqs:
         srv.submit(eid, src)
     t0 = srv.stats().clock
@@ -148,7 +151,7 @@ def serving_bench(n_requests: int, budget_bytes: int = 120 * 10 ** 9) -> dict:
                         "hits": int(sum(r.n_hits for r in res)), "seconds": t1 - t0}
     srv.close()
     # real time: arrivals replayed on the server clock, results released on completion
-    srv = EventServer(setup, hbm_budget_bytes=budget_bytes, seed=workloads.SEED_BASE + 2)
+    srv = EventServer(setup, **kw)
     start = srv.stats().clock
     i, lat, done = 0, [], 0
     while done < len(reqs):

@@ -157,6 +157,7 @@ bool fill_world_params(const ntp_ctx* ctx, PropParams& p) {
     p.grid_x0 = ctx->grid_x0;
     p.grid_y0 = ctx->grid_y0;
     p.grid_h = ctx->grid_h;
+    p.grid_inv_h = ctx->grid_h > 0 ? 1.0f / ctx->grid_h : 0.0f;
     p.medium = ctx->d_med;
     p.n_medium = ctx->n_med;
     p.wl_min = ctx->wl_min;
@@ -464,10 +465,19 @@ ntp_status ntp_set_targets(ntp_ctx* ctx, const ntp_target* t, int32_t n, const f
             y1 = std::max(y1, static_cast<double>(c.cy));
             rmax = std::max(rmax, static_cast<double>(c.r_cull));
         }
-        const double pad = rmax + margin + 1.0;
-        x0 -= pad; y0 -= pad; x1 += pad; y1 += pad;
-        double h = std::sqrt((x1 - x0) * (y1 - y0) / (4.0 * cols.size()));
-        h = std::max(h, 2.0 * (rmax + margin));
+        // cell side: the median distance from a column to its nearest
+        // neighbour (about one column per cell), grid shifted so that a
+        // regular lattice of strings sits at cell centres
+        std::vector<double> nn(cols.size(), 1e30);
+        for (size_t a = 0; a < cols.size(); ++a)
+            for (size_t b = 0; b < cols.size(); ++b)
+                if (a != b) {
+                    const double dx = cols[a].cx - cols[b].cx, dy = cols[a].cy - cols[b].cy;
+                    nn[a] = std::min(nn[a], std::sqrt(dx * dx + dy * dy));
+                }
+        std::nth_element(nn.begin(), nn.begin() + nn.size() / 2, nn.end());
+        double h = std::max(nn[nn.size() / 2], 2.0 * (rmax + margin));
+        x0 -= h / 2; y0 -= h / 2; x1 += h / 2; y1 += h / 2;
         int nx = static_cast<int>(std::ceil((x1 - x0) / h)), ny = static_cast<int>(std::ceil((y1 - y0) / h));
         while (static_cast<long long>(nx) * ny > 65536) {
             h *= 1.5;
@@ -597,32 +607,11 @@ ntp_status ntp_propagate(ntp_ctx* ctx, const ntp_source* sources, int32_t n_sour
     p.prefix = ctx->d_prefix;
     p.n_src = n_sources;
     p.total = total;
-    p.targets = ctx->d_tgt;
-    p.target_ids = ctx->d_tgt_id;
-    p.n_targets = ctx->n_tgt;
-    p.targets_in_smem = ctx->n_tgt <= ntp::kMaxSmemTargets ? 1 : 0;
-    p.columns = (ctx->n_cols > 0 && !(o.flags & NTP_FLAG_PLAIN_SCAN)) ? ctx->d_cols : nullptr;
-    p.members = ctx->d_members;
-    p.n_columns = ctx->n_cols;
-    p.cell_start = p.columns ? ctx->d_cell_start : nullptr;
-    p.cell_items = ctx->d_cell_items;
-    p.grid_nx = ctx->grid_nx;
-    p.grid_ny = ctx->grid_ny;
-    p.n_cell_items = ctx->n_cell_items;
-    p.grid_x0 = ctx->grid_x0;
-    p.grid_y0 = ctx->grid_y0;
-    p.grid_h = ctx->grid_h;
-    p.medium = ctx->d_med;
-    p.n_medium = ctx->n_med;
-    p.wl_min = ctx->wl_min;
-    p.medium_scale = static_cast<float>(ctx->n_med - 1) / (ctx->wl_max - ctx->wl_min);
-    p.spec_kind = ctx->spec_kind;
-    p.n_spec = ctx->n_spec;
-    p.spec_knots = ctx->d_spec;
-    p.spec_p0 = ctx->spec_p0;
-    p.spec_p1 = ctx->spec_p1;
-    p.hg_g = ctx->hg_g;
-    p.rayleigh_fraction = ctx->f_ray;
+    ntp::fill_world_params(ctx, p);
+    if (o.flags & NTP_FLAG_PLAIN_SCAN) {
+        p.columns = nullptr;
+        p.cell_start = nullptr;
+    }
     p.max_steps = o.max_steps;
     p.hit_policy = o.hit_policy;
     p.exact_pole = (o.flags & NTP_FLAG_EXACT_POLE_ROTATION) ? 1 : 0;

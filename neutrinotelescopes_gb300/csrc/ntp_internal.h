@@ -53,7 +53,7 @@ struct PropParams {
     const int* cell_start;                // device, nx * ny + 1 offsets into cell_items
     const int* cell_items;                // device, column indices
     int grid_nx, grid_ny, n_cell_items;
-    float grid_x0, grid_y0, grid_h;
+    float grid_x0, grid_y0, grid_h, grid_inv_h;
 
     const float4* medium;                 // device, per knot (n, v_group, l_scatter, 0)
     int n_medium;

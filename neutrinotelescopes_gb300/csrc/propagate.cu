@@ -80,32 +80,44 @@ __device__ __forceinline__ bool sphere_hit(const float4 T, const V3 pos, const V
     return false;
 }
 
+// Per-step quantities of the column tests.
+struct SegmentView {
+    V3 pos, dir;
+    float step;
+    float dd;       // dir.x^2 + dir.y^2
+    float slack2;   // rounding envelope of the float sphere test, grows as step^2
+};
+
+__device__ __forceinline__ SegmentView make_segment(const V3 pos, const V3 dir, float step) {
+    return SegmentView{pos, dir, step, dir.x * dir.x + dir.y * dir.y, 4e-7f * step * step};
+}
+
 // Tests the members of one vertical column that the segment can reach.  The
 // culling is conservative: the horizontal distance of the segment from the
 // column axis is compared with r_cull^2 plus the rounding envelope of the
-// single-precision sphere test (which grows as step^2), and the z range is
-// padded by r_cull and one member; every member it keeps goes through the
-// same sphere_hit as the plain scan.  Among the hits it keeps the first in
-// target-list order (or the nearest), as the plain scan does.
+// single-precision sphere test, and the z range is padded by r_cull and one
+// member; every member it keeps goes through the same sphere_hit as the plain
+// scan.  Among the hits it keeps the first in target-list order (or the
+// nearest), as the plain scan does.  The cheapest test comes first: the
+// distance of the column axis from the infinite line.
 __device__ __forceinline__ void column_candidates(const Column& C, const int* __restrict__ mem,
-                                                  const float4* __restrict__ tg, const V3 pos, const V3 dir,
-                                                  float step, int policy, int& hit_t, float& hit_d) {
+                                                  const float4* __restrict__ tg, const SegmentView& sg,
+                                                  int policy, int& hit_t, float& hit_d) {
+    const V3 pos = sg.pos, dir = sg.dir;
+    const float step = sg.step, dd = sg.dd;
     const float px = pos.x - C.cx, py = pos.y - C.cy;
-    const float dd = dir.x * dir.x + dir.y * dir.y;
-    const float rc2 = fmaf(4e-7f * step, step, C.r_cull * C.r_cull);
+    const float rc2 = fmaf(C.r_cull, C.r_cull, sg.slack2);
     float t0 = 0.0f, t1 = step;
     if (dd > 1e-12f) {
-        // closest approach to the axis at ts = -(p.d)/dd, tested without dividing
-        const float pd = -(px * dir.x + py * dir.y);  // ts * dd
-        const float cr = px * dir.y - py * dir.x;     // perpendicular distance * sqrt(dd)
-        bool far;
+        const float cr = px * dir.y - py * dir.x;  // perpendicular distance * sqrt(dd)
+        if (cr * cr > rc2 * dd) return;            // the line passes wide of the axis
+        const float pd = -(px * dir.x + py * dir.y);  // closest approach at ts = pd / dd
+        bool far = false;
         if (pd <= 0.0f) {
             far = px * px + py * py > rc2;
         } else if (pd >= step * dd) {
             const float ex = fmaf(step, dir.x, px), ey = fmaf(step, dir.y, py);
             far = ex * ex + ey * ey > rc2;
-        } else {
-            far = cr * cr > rc2 * dd;
         }
         if (far) return;
         const float inv_dd = 1.0f / dd;
@@ -147,21 +159,26 @@ __device__ __forceinline__ void column_candidates(const Column& C, const int* __
 __device__ __forceinline__ void grid_candidates(const PropParams& p, const int* __restrict__ cstart,
                                                 const int* __restrict__ citems, const Column* __restrict__ cols,
                                                 const int* __restrict__ mem, const float4* __restrict__ tg,
-                                                const V3 pos, const V3 dir, float step, int& hit_t, float& hit_d) {
-    const float h = p.grid_h, inv_h = 1.0f / h;
+                                                const SegmentView& sg, int& hit_t, float& hit_d) {
+    const V3 pos = sg.pos, dir = sg.dir;
+    const float step = sg.step;
+    const float h = p.grid_h, inv_h = p.grid_inv_h;
     const float x1 = p.grid_x0 + h * static_cast<float>(p.grid_nx);
     const float y1 = p.grid_y0 + h * static_cast<float>(p.grid_ny);
+    // reciprocal direction components (0 components never cross a cell wall)
+    const float inf = __int_as_float(0x7f800000);
+    const float rx = dir.x != 0.0f ? fast_rcp(dir.x) : inf, ry = dir.y != 0.0f ? fast_rcp(dir.y) : inf;
     // clip the segment to the grid box
     float t_in = 0.0f, t_out = step;
     if (dir.x != 0.0f) {
-        const float ta = (p.grid_x0 - pos.x) / dir.x, tb = (x1 - pos.x) / dir.x;
+        const float ta = (p.grid_x0 - pos.x) * rx, tb = (x1 - pos.x) * rx;
         t_in = fmaxf(t_in, fminf(ta, tb));
         t_out = fminf(t_out, fmaxf(ta, tb));
     } else if (pos.x < p.grid_x0 || pos.x > x1) {
         return;
     }
     if (dir.y != 0.0f) {
-        const float ta = (p.grid_y0 - pos.y) / dir.y, tb = (y1 - pos.y) / dir.y;
+        const float ta = (p.grid_y0 - pos.y) * ry, tb = (y1 - pos.y) * ry;
         t_in = fmaxf(t_in, fminf(ta, tb));
         t_out = fminf(t_out, fmaxf(ta, tb));
     } else if (pos.y < p.grid_y0 || pos.y > y1) {
@@ -172,15 +189,13 @@ __device__ __forceinline__ void grid_candidates(const PropParams& p, const int* 
     int ix = min(max(static_cast<int>(floorf((sx - p.grid_x0) * inv_h)), 0), p.grid_nx - 1);
     int iy = min(max(static_cast<int>(floorf((sy - p.grid_y0) * inv_h)), 0), p.grid_ny - 1);
     const int stx = dir.x > 0.0f ? 1 : -1, sty = dir.y > 0.0f ? 1 : -1;
-    const float inf = __int_as_float(0x7f800000);
-    float tmx = dir.x != 0.0f ? (p.grid_x0 + h * static_cast<float>(ix + (dir.x > 0.0f)) - pos.x) / dir.x : inf;
-    float tmy = dir.y != 0.0f ? (p.grid_y0 + h * static_cast<float>(iy + (dir.y > 0.0f)) - pos.y) / dir.y : inf;
-    const float tdx = dir.x != 0.0f ? h / fabsf(dir.x) : inf;
-    const float tdy = dir.y != 0.0f ? h / fabsf(dir.y) : inf;
+    float tmx = dir.x != 0.0f ? (p.grid_x0 + h * static_cast<float>(ix + (dir.x > 0.0f)) - pos.x) * rx : inf;
+    float tmy = dir.y != 0.0f ? (p.grid_y0 + h * static_cast<float>(iy + (dir.y > 0.0f)) - pos.y) * ry : inf;
+    const float tdx = h * fabsf(rx), tdy = h * fabsf(ry);
     for (int guard = p.grid_nx + p.grid_ny + 2; guard > 0; --guard) {
         const int c = iy * p.grid_nx + ix;
         for (int k = cstart[c]; k < cstart[c + 1]; ++k)
-            column_candidates(cols[citems[k]], mem, tg, pos, dir, step, p.hit_policy, hit_t, hit_d);
+            column_candidates(cols[citems[k]], mem, tg, sg, p.hit_policy, hit_t, hit_d);
         if (tmx < tmy) {
             if (tmx > t_out) break;
             ix += stx;
@@ -374,11 +389,14 @@ __global__ void __launch_bounds__(kPropBlock, kMinBlocks) propagate_kernel(const
 
             // check_intersection over the targets, photon_prop_cuda.jl:233-271, :460-468
             float hit_d = step;
-            if (cols && cstart) {
-                grid_candidates(p, cstart, citems, cols, mem, tg, ph.pos, ph.dir, step, hit_t, hit_d);
-            } else if (cols) {
-                for (int c = 0; c < p.n_columns; ++c)
-                    column_candidates(cols[c], mem, tg, ph.pos, ph.dir, step, p.hit_policy, hit_t, hit_d);
+            if (cols) {
+                const SegmentView sg = make_segment(ph.pos, ph.dir, step);
+                if (cstart) {
+                    grid_candidates(p, cstart, citems, cols, mem, tg, sg, hit_t, hit_d);
+                } else {
+                    for (int c = 0; c < p.n_columns; ++c)
+                        column_candidates(cols[c], mem, tg, sg, p.hit_policy, hit_t, hit_d);
+                }
             } else {
                 for (int t = 0; t < p.n_targets; ++t) {
                     float d;

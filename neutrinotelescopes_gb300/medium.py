@@ -128,14 +128,20 @@ class MediumProperties:
         raise NotImplementedError
 
     def tabulate(self, wl_min: float, wl_max: float, n_knots: int = DEFAULT_TABLE_KNOTS) -> MediumTables:
+        """Knot tables on [wl_min, wl_max]; a medium whose per-photon
+        quantities do not vary with wavelength gets 2 knots (exact)."""
         wl = np.linspace(wl_min, wl_max, n_knots)
         awl, alen = self.absorption_table()
+        tabs = [np.asarray(f(wl), dtype=np.float32) for f in
+                (self.refractive_index, self.group_velocity, self.scattering_length)]
+        if all(np.all(t == t[0]) for t in tabs):
+            tabs = [t[:1].repeat(2) for t in tabs]
         return MediumTables(
             wl_min=float(wl_min),
             wl_max=float(wl_max),
-            ref_index=np.asarray(self.refractive_index(wl), dtype=np.float32),
-            group_velocity=np.asarray(self.group_velocity(wl), dtype=np.float32),
-            scattering_length=np.asarray(self.scattering_length(wl), dtype=np.float32),
+            ref_index=tabs[0],
+            group_velocity=tabs[1],
+            scattering_length=tabs[2],
             abs_wavelength=np.asarray(awl, dtype=np.float32),
             abs_length=np.asarray(alen, dtype=np.float32),
             hg_g=float(self.mean_scattering_angle),
