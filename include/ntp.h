@@ -276,6 +276,45 @@ ntp_status ntp_calc_time_residual(ntp_ctx* ctx, const ntp_hit* hits, uint64_t n_
                                   const float source_position[3], float n800,
                                   double* tres, int32_t buffers_on_device, void* stream);
 
+/* Per-PMT reduction of a hit set in double precision (no single reference
+   counterpart: it fuses make_hits_from_photons, calc_total_weight! and
+   calc_time_residual!, photon_prop_cuda.jl:850-924, with the per-(module,
+   PMT) grouping of pmt_frontend/pipeline.jl:104-116).  For every hit on a
+   PMT: weight_sum[k][j] += total weight, hit_count[k][j] += 1 and, with
+   n_bins > 0, time_hist[k][j][bin] += total weight, where k is the target's
+   index in ntp_set_targets, j the 0-based PMT and the binned time either the
+   hit time or the time residual.  Outputs are zeroed first; any may be NULL
+   except that time_hist is needed when n_bins > 0. */
+typedef struct ntp_summary_spec {
+    int32_t max_pmts;          /* PMT slots per target; >= every target's PMT count       */
+    int32_t n_bins;            /* time-histogram bins over [t_min, t_max), 0 for none     */
+    float t_min;               /* ns                                                      */
+    float t_max;
+    int32_t use_time_residual; /* 1: bin time - tgeo(module) as calc_time_residual!        */
+    float source_position[3];  /* for the time residual                                   */
+    float n800;                /* refractive index at 800 nm, for the time residual       */
+} ntp_summary_spec;
+
+ntp_status ntp_pmt_summary(ntp_ctx* ctx, const ntp_hit* hits, uint64_t n_hits, const double orientation[9],
+                           const ntp_summary_spec* spec, double* weight_sum, double* hit_count, double* time_hist,
+                           int32_t buffers_on_device, void* stream);
+
+/* resample_simulation (pmt_frontend/pipeline.jl:86-116) with per_pmt = true:
+   hits grouped by (module, PMT) with pmt_id from ntp_make_hits (0 = none) and
+   weight from ntp_calc_total_weight; per group N = min(Poisson(sum(weight) *
+   downsample), number of hits with weight > 0), then N hits drawn without
+   replacement with probability proportional to weight.  Outputs, grouped by
+   group g = target_index * max_pmts + pmt_id - 1 in increasing g: out_group,
+   out_time (the input time, or the hit time when time is NULL) and out_hit
+   (index of the drawn hit); any output may be NULL.  The random draws are
+   keyed by seed and by each hit's (source_index, photon_index), so the
+   result does not depend on the order of the hits.  *n_out receives the
+   total; above capacity nothing is written and NTP_ERR_OVERFLOW returned. */
+ntp_status ntp_resample(ntp_ctx* ctx, const ntp_hit* hits, uint64_t n_hits, const int32_t* pmt_id,
+                        const double* weight, const double* time, int32_t max_pmts, double downsample,
+                        uint64_t seed, int32_t* out_group, double* out_time, uint64_t* out_hit,
+                        uint64_t capacity, uint64_t* n_out, int32_t buffers_on_device, void* stream);
+
 /* ------------------------------------------------------------------ serving
  * Continuous-batching event server (no reference counterpart; the reference
  * runs one propagate_photons per event, photon_prop_cuda.jl:804-817).  Each

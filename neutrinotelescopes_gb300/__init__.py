@@ -19,7 +19,7 @@ from .lightyield import (AxiconeEmitter, CherenkovTrackEmitter, ExtendedCherenko
 from .medium import (MediumProperties, SimpleWater, WaterProperties, make_cascadia_medium_properties,
                      make_simple_water)
 from .photon_prop import (HitTable, PhotonHit, PhotonPropSetup, calc_time_residual, calc_total_weight,
-                          make_hits_from_photons, propagate_photons)
+                          make_hits_from_photons, pmt_summary, propagate_photons, resample_simulation)
 from .spectrum import (CherenkovSpectrum, InverseSquareSpectrum, Monochromatic, frank_tamm, frank_tamm_inverted_cdf,
                        frank_tamm_norm)
 

@@ -171,6 +171,18 @@ class NtpServerStats(C.Structure):
     ]
 
 
+class NtpSummarySpec(C.Structure):
+    _fields_ = [
+        ("max_pmts", C.c_int32),
+        ("n_bins", C.c_int32),
+        ("t_min", C.c_float),
+        ("t_max", C.c_float),
+        ("use_time_residual", C.c_int32),
+        ("source_position", C.c_float * 3),
+        ("n800", C.c_float),
+    ]
+
+
 assert C.sizeof(NtpSource) == 64
 assert C.sizeof(NtpTarget) == 48
 
@@ -207,6 +219,8 @@ EXPORTED = (
     "ntp_calc_total_weight",
     "ntp_set_wavelength_acceptance",
     "ntp_calc_time_residual",
+    "ntp_pmt_summary",
+    "ntp_resample",
     "ntp_server_create",
     "ntp_server_destroy",
     "ntp_server_submit",
@@ -242,6 +256,12 @@ def _declare(lib: C.CDLL) -> None:
     lib.ntp_calc_total_weight.argtypes = [vp, vp, u64, vp, vp, vp, vp, i32, vp]
     lib.ntp_set_wavelength_acceptance.argtypes = [vp, C.POINTER(C.c_double), C.POINTER(C.c_double), i32]
     lib.ntp_calc_time_residual.argtypes = [vp, vp, u64, C.POINTER(C.c_float), C.c_float, vp, i32, vp]
+    lib.ntp_pmt_summary.argtypes = [vp, vp, u64, C.POINTER(C.c_double), C.POINTER(NtpSummarySpec), vp, vp, vp, i32,
+                                    vp]
+    lib.ntp_pmt_summary.restype = C.c_int
+    lib.ntp_resample.argtypes = [vp, vp, u64, vp, vp, vp, i32, C.c_double, u64, vp, vp, vp, u64, C.POINTER(u64),
+                                 i32, vp]
+    lib.ntp_resample.restype = C.c_int
     lib.ntp_server_create.argtypes = [vp, C.POINTER(NtpServerConfig), C.POINTER(vp)]
     lib.ntp_server_destroy.argtypes = [vp]
     lib.ntp_server_destroy.restype = None

@@ -81,6 +81,8 @@ struct ntp_ctx {
     size_t stage_bytes = 0;
     void* d_stage2 = nullptr;
     size_t stage2_bytes = 0;
+    void* d_scratch = nullptr;  // resampling work arrays
+    size_t scratch_bytes = 0;
 };
 
 const char* ntp_noalloc_last_error();
@@ -260,6 +262,7 @@ void ntp_destroy(ntp_ctx* ctx) {
     dfree(ctx->d_prefix);
     if (ctx->d_stage) cudaFree(ctx->d_stage);
     if (ctx->d_stage2) cudaFree(ctx->d_stage2);
+    if (ctx->d_scratch) cudaFree(ctx->d_scratch);
     if (ctx->h_counters) cudaFreeHost(ctx->h_counters);
     if (ctx->stream) cudaStreamDestroy(ctx->stream);
     delete ctx;
@@ -678,6 +681,40 @@ static ntp_status stage_hits(ntp_ctx* ctx, const ntp_hit* hits, uint64_t n, int 
     return NTP_OK;
 }
 
+// PMT axes for an orientation: orientation * sph_to_cart(theta, phi), the
+// spherical step in float as the coordinates are Float32 (detection.jl:60-70).
+static ntp_status upload_axes(ntp_ctx* ctx, const double orientation[9], cudaStream_t st) {
+    const int npc = static_cast<int>(ctx->pmt_coords.size() / 2);
+    if (npc == 0) return NTP_OK;
+    std::vector<double> axes(3 * static_cast<size_t>(npc));
+    for (int j = 0; j < npc; ++j) {
+        const float th = ctx->pmt_coords[2 * j], ph = ctx->pmt_coords[2 * j + 1];
+        const float s_t = sinf(th), c_t = cosf(th), s_p = sinf(ph), c_p = cosf(ph);
+        const double v[3] = {static_cast<double>(c_p * s_t), static_cast<double>(s_p * s_t), static_cast<double>(c_t)};
+        for (int r = 0; r < 3; ++r)
+            axes[3 * j + r] = orientation[3 * r] * v[0] + orientation[3 * r + 1] * v[1] + orientation[3 * r + 2] * v[2];
+    }
+    NTP_CUDA(ctx, cudaMemcpyAsync(ctx->d_axes, axes.data(), sizeof(double) * axes.size(), cudaMemcpyHostToDevice, st));
+    NTP_CUDA(ctx, cudaStreamSynchronize(st));
+    return NTP_OK;
+}
+
+// tgeo per target, photon_prop_cuda.jl:913-914
+static ntp_status upload_tgeo(ntp_ctx* ctx, const float src[3], float n800, cudaStream_t st) {
+    std::vector<double> tgeo(ctx->n_tgt);
+    const double c_vac = 0.299792458;
+    for (int k = 0; k < ctx->n_tgt; ++k) {
+        const ntp_target& t = ctx->targets[k];
+        const float dx = src[0] - t.position[0], dy = src[1] - t.position[1], dz = src[2] - t.position[2];
+        const float distance = std::sqrt(dx * dx + dy * dy + dz * dz);
+        tgeo[k] = static_cast<double>(distance - t.radius) / (c_vac / static_cast<double>(n800));
+    }
+    if (!tgeo.empty())
+        NTP_CUDA(ctx, cudaMemcpyAsync(ctx->d_tgeo, tgeo.data(), sizeof(double) * tgeo.size(), cudaMemcpyHostToDevice, st));
+    NTP_CUDA(ctx, cudaStreamSynchronize(st));
+    return NTP_OK;
+}
+
 ntp_status ntp_make_hits(ntp_ctx* ctx, const ntp_hit* hits, uint64_t n, const double orientation[9],
                          int32_t* pmt_id, int32_t on_device, void* stream) {
     if (!ctx) return NTP_ERR_INVALID;
@@ -689,23 +726,8 @@ ntp_status ntp_make_hits(ntp_ctx* ctx, const ntp_hit* hits, uint64_t n, const do
     if (!hits || !pmt_id || !orientation) return invalid(ctx, "ntp_make_hits: NULL argument");
     cudaSetDevice(ctx->device);
     cudaStream_t st = on_device ? pick_stream(ctx, stream) : ctx->stream;
-    // PMT axes: orientation * sph_to_cart(theta, phi), the spherical step in
-    // float as the coordinates are Float32 (detection.jl:60-70)
-    const int npc = static_cast<int>(ctx->pmt_coords.size() / 2);
-    if (npc > 0) {
-        std::vector<double> axes(3 * static_cast<size_t>(npc));
-        for (int j = 0; j < npc; ++j) {
-            const float th = ctx->pmt_coords[2 * j], ph = ctx->pmt_coords[2 * j + 1];
-            const float s_t = sinf(th), c_t = cosf(th), s_p = sinf(ph), c_p = cosf(ph);
-            const double v[3] = {static_cast<double>(c_p * s_t), static_cast<double>(s_p * s_t),
-                                 static_cast<double>(c_t)};
-            for (int r = 0; r < 3; ++r)
-                axes[3 * j + r] = orientation[3 * r] * v[0] + orientation[3 * r + 1] * v[1] + orientation[3 * r + 2] * v[2];
-        }
-        NTP_CUDA(ctx, cudaMemcpyAsync(ctx->d_axes, axes.data(), sizeof(double) * axes.size(),
-                                      cudaMemcpyHostToDevice, st));
-        NTP_CUDA(ctx, cudaStreamSynchronize(st));
-    }
+    ntp_status sa = upload_axes(ctx, orientation, st);
+    if (sa != NTP_OK) return sa;
     const ntp_hit* d_hits = nullptr;
     ntp_status s = stage_hits(ctx, hits, n, on_device, st, &d_hits);
     if (s != NTP_OK) return s;
@@ -753,6 +775,167 @@ ntp_status ntp_calc_total_weight(ntp_ctx* ctx, const ntp_hit* hits, uint64_t n, 
     return NTP_OK;
 }
 
+ntp_status ntp_pmt_summary(ntp_ctx* ctx, const ntp_hit* hits, uint64_t n, const double orientation[9],
+                           const ntp_summary_spec* spec, double* wsum, double* count, double* hist,
+                           int32_t on_device, void* stream) {
+    if (!ctx) return NTP_ERR_INVALID;
+    if (!ctx->have_targets || !ctx->have_medium || ctx->n_acc < 2) {
+        ctx->err = "ntp_pmt_summary: targets, medium and wavelength acceptance must be set first";
+        return NTP_ERR_NOT_READY;
+    }
+    if (!spec || !orientation) return invalid(ctx, "ntp_pmt_summary: NULL argument");
+    int need = 1;
+    for (const auto& t : ctx->targets) need = std::max(need, t.kind == NTP_TARGET_MULTI_PMT ? t.n_pmts : 1);
+    if (spec->max_pmts < need) return invalid(ctx, "ntp_pmt_summary: max_pmts is below a target's PMT count");
+    if (spec->n_bins < 0 || (spec->n_bins > 0 && (!hist || !(spec->t_max > spec->t_min))))
+        return invalid(ctx, "ntp_pmt_summary: need t_max > t_min and time_hist when n_bins > 0");
+    if (spec->use_time_residual && !(spec->n800 > 0.0f)) return invalid(ctx, "ntp_pmt_summary: n800 must be > 0");
+    if (n > 0 && !hits) return invalid(ctx, "ntp_pmt_summary: hits is NULL");
+    cudaSetDevice(ctx->device);
+    cudaStream_t st = on_device ? pick_stream(ctx, stream) : ctx->stream;
+    const size_t slots = static_cast<size_t>(ctx->n_tgt) * spec->max_pmts;
+    const size_t nb = static_cast<size_t>(spec->n_bins);
+    double* outs[3] = {wsum, count, hist};
+    const size_t sizes[3] = {slots, slots, slots * nb};
+    double* d_outs[3] = {wsum, count, hist};
+    if (!on_device) {
+        NTP_CUDA(ctx, ensure(ctx->d_stage2, ctx->stage2_bytes, sizeof(double) * (sizes[0] + sizes[1] + sizes[2] + 1)));
+        double* base = static_cast<double*>(ctx->d_stage2);
+        d_outs[0] = base;
+        d_outs[1] = base + sizes[0];
+        d_outs[2] = base + sizes[0] + sizes[1];
+    }
+    // outputs not wanted by the caller still receive the sums (scratch)
+    for (int k = 0; k < 3; ++k)
+        if (sizes[k] && d_outs[k]) NTP_CUDA(ctx, cudaMemsetAsync(d_outs[k], 0, sizeof(double) * sizes[k], st));
+    if (n > 0) {
+        ntp_status s0 = upload_axes(ctx, orientation, st);
+        if (s0 != NTP_OK) return s0;
+        if (spec->use_time_residual) {
+            s0 = upload_tgeo(ctx, spec->source_position, spec->n800, st);
+            if (s0 != NTP_OK) return s0;
+        }
+        const ntp_hit* d_hits = nullptr;
+        s0 = stage_hits(ctx, hits, n, on_device, st, &d_hits);
+        if (s0 != NTP_OK) return s0;
+        if (!d_outs[0] || !d_outs[1]) {  // device call with NULL outputs: give them scratch
+            NTP_CUDA(ctx, ensure(ctx->d_stage2, ctx->stage2_bytes, sizeof(double) * 2 * slots));
+            double* base = static_cast<double*>(ctx->d_stage2);
+            if (!d_outs[0]) { d_outs[0] = base; NTP_CUDA(ctx, cudaMemsetAsync(base, 0, sizeof(double) * slots, st)); }
+            if (!d_outs[1]) { d_outs[1] = base + slots; NTP_CUDA(ctx, cudaMemsetAsync(base + slots, 0, sizeof(double) * slots, st)); }
+        }
+        NTP_CUDA(ctx, ntp::launch_pmt_summary(hit_table(ctx), d_hits, n, ctx->d_axes, ctx->d_abs_wl, ctx->d_abs_len,
+                                              ctx->n_abs, ctx->d_acc_wl, ctx->d_acc, ctx->n_acc, ctx->d_tgeo,
+                                              spec->use_time_residual, spec->max_pmts, spec->n_bins, spec->t_min,
+                                              spec->t_max, d_outs[0], d_outs[1], d_outs[2], st));
+    }
+    if (!on_device)
+        for (int k = 0; k < 3; ++k)
+            if (outs[k] && sizes[k])
+                NTP_CUDA(ctx, cudaMemcpyAsync(outs[k], d_outs[k], sizeof(double) * sizes[k], cudaMemcpyDeviceToHost, st));
+    NTP_CUDA(ctx, cudaStreamSynchronize(st));
+    return NTP_OK;
+}
+
+ntp_status ntp_resample(ntp_ctx* ctx, const ntp_hit* hits, uint64_t n, const int32_t* pmt_id, const double* weight,
+                        const double* time, int32_t max_pmts, double downsample, uint64_t seed, int32_t* out_group,
+                        double* out_time, uint64_t* out_hit, uint64_t capacity, uint64_t* n_out, int32_t on_device,
+                        void* stream) {
+    if (!ctx) return NTP_ERR_INVALID;
+    if (n_out) *n_out = 0;
+    if (!ctx->have_targets) {
+        ctx->err = "ntp_resample: targets must be set first";
+        return NTP_ERR_NOT_READY;
+    }
+    if (max_pmts < 1 || !(downsample >= 0.0)) return invalid(ctx, "ntp_resample: need max_pmts >= 1, downsample >= 0");
+    if (n > 0 && (!hits || !pmt_id || !weight)) return invalid(ctx, "ntp_resample: NULL input");
+    const long long G = static_cast<long long>(ctx->n_tgt) * max_pmts;
+    if (G > (1ll << 26)) return invalid(ctx, "ntp_resample: too many (module, PMT) groups");
+    if (n == 0 || G == 0) return NTP_OK;
+    cudaSetDevice(ctx->device);
+    cudaStream_t st = on_device ? pick_stream(ctx, stream) : ctx->stream;
+    const uint2 key = make_uint2(static_cast<uint32_t>(seed), static_cast<uint32_t>(seed >> 32));
+    // inputs on the device
+    const ntp_hit* d_hits = nullptr;
+    ntp_status s0 = stage_hits(ctx, hits, n, on_device, st, &d_hits);
+    if (s0 != NTP_OK) return s0;
+    // scratch: group i32[n] | order u64[n] | okey u64[n] | pmt i32[n] | w f64[n] | t f64[n] |
+    //          wsum f64[G] | npos, nall, nsel, fill u64[G] | start, out_start u64[G+1]
+    const size_t nn = n, g = static_cast<size_t>(G);
+    size_t off = 0;
+    auto take = [&](size_t bytes) { size_t o = off; off += (bytes + 255) / 256 * 256; return o; };
+    const size_t o_group = take(4 * nn), o_order = take(8 * nn), o_okey = take(8 * nn);
+    const size_t o_pmt = on_device ? 0 : take(4 * nn), o_w = on_device ? 0 : take(8 * nn);
+    const size_t o_t = (on_device || !time) ? 0 : take(8 * nn);
+    const size_t o_wsum = take(8 * g), o_npos = take(8 * g), o_nall = take(8 * g), o_nsel = take(8 * g);
+    const size_t o_fill = take(8 * g), o_start = take(8 * (g + 1)), o_ostart = take(8 * (g + 1));
+    NTP_CUDA(ctx, ensure(ctx->d_scratch, ctx->scratch_bytes, off));
+    unsigned char* sc = static_cast<unsigned char*>(ctx->d_scratch);
+    const int32_t* d_pmt = pmt_id;
+    const double* d_w = weight;
+    const double* d_t = time;
+    if (!on_device) {
+        NTP_CUDA(ctx, cudaMemcpyAsync(sc + o_pmt, pmt_id, 4 * nn, cudaMemcpyHostToDevice, st));
+        NTP_CUDA(ctx, cudaMemcpyAsync(sc + o_w, weight, 8 * nn, cudaMemcpyHostToDevice, st));
+        d_pmt = reinterpret_cast<const int32_t*>(sc + o_pmt);
+        d_w = reinterpret_cast<const double*>(sc + o_w);
+        if (time) {
+            NTP_CUDA(ctx, cudaMemcpyAsync(sc + o_t, time, 8 * nn, cudaMemcpyHostToDevice, st));
+            d_t = reinterpret_cast<const double*>(sc + o_t);
+        }
+    }
+    auto u64p = [&](size_t o) { return reinterpret_cast<unsigned long long*>(sc + o); };
+    int32_t* d_group = reinterpret_cast<int32_t*>(sc + o_group);
+    double* d_wsum = reinterpret_cast<double*>(sc + o_wsum);
+    NTP_CUDA(ctx, cudaMemsetAsync(sc + o_wsum, 0, o_start - o_wsum, st));  // wsum, npos, nall, nsel, fill
+    NTP_CUDA(ctx, ntp::launch_resample_group(d_hits, n, d_pmt, d_w, ctx->d_sorted, ctx->n_tgt, max_pmts, d_group,
+                                             d_wsum, u64p(o_npos), u64p(o_nall), st));
+    NTP_CUDA(ctx, ntp::launch_resample_draw(static_cast<int>(G), d_wsum, u64p(o_npos), downsample, key,
+                                            u64p(o_nsel), st));
+    // bucket offsets and output offsets (prefix sums on the host)
+    std::vector<unsigned long long> nall(g), nsel(g), start(g + 1), ostart(g + 1);
+    NTP_CUDA(ctx, cudaMemcpyAsync(nall.data(), u64p(o_nall), 8 * g, cudaMemcpyDeviceToHost, st));
+    NTP_CUDA(ctx, cudaMemcpyAsync(nsel.data(), u64p(o_nsel), 8 * g, cudaMemcpyDeviceToHost, st));
+    NTP_CUDA(ctx, cudaStreamSynchronize(st));
+    start[0] = ostart[0] = 0;
+    for (size_t i = 0; i < g; ++i) {
+        start[i + 1] = start[i] + nall[i];
+        ostart[i + 1] = ostart[i] + nsel[i];
+    }
+    const unsigned long long total = ostart[g];
+    if (n_out) *n_out = total;
+    if (total > capacity) {
+        ctx->err = "ntp_resample: output capacity " + std::to_string(capacity) + " below " + std::to_string(total);
+        return NTP_ERR_OVERFLOW;
+    }
+    if (total == 0) return NTP_OK;
+    NTP_CUDA(ctx, cudaMemcpyAsync(u64p(o_start), start.data(), 8 * (g + 1), cudaMemcpyHostToDevice, st));
+    NTP_CUDA(ctx, cudaMemcpyAsync(u64p(o_ostart), ostart.data(), 8 * (g + 1), cudaMemcpyHostToDevice, st));
+    NTP_CUDA(ctx, ntp::launch_resample_bucket(d_hits, n, d_group, d_w, key, u64p(o_start), u64p(o_fill),
+                                              u64p(o_order), u64p(o_okey), st));
+    // outputs (staged for host buffers)
+    int32_t* d_og = out_group;
+    double* d_ot = out_time;
+    unsigned long long* d_oh = reinterpret_cast<unsigned long long*>(out_hit);
+    if (!on_device || !out_group || !out_time || !out_hit) {
+        NTP_CUDA(ctx, ensure(ctx->d_stage2, ctx->stage2_bytes, 24 * total));
+        unsigned char* b = static_cast<unsigned char*>(ctx->d_stage2);
+        if (!on_device || !d_og) d_og = reinterpret_cast<int32_t*>(b);
+        if (!on_device || !d_ot) d_ot = reinterpret_cast<double*>(b + 8 * total);
+        if (!on_device || !d_oh) d_oh = reinterpret_cast<unsigned long long*>(b + 16 * total);
+    }
+    NTP_CUDA(ctx, ntp::launch_resample_select(static_cast<int>(G), d_hits, d_t, u64p(o_start), u64p(o_nall),
+                                              u64p(o_nsel), u64p(o_ostart), u64p(o_order), u64p(o_okey), d_og, d_ot,
+                                              d_oh, st));
+    if (!on_device) {
+        if (out_group) NTP_CUDA(ctx, cudaMemcpyAsync(out_group, d_og, 4 * total, cudaMemcpyDeviceToHost, st));
+        if (out_time) NTP_CUDA(ctx, cudaMemcpyAsync(out_time, d_ot, 8 * total, cudaMemcpyDeviceToHost, st));
+        if (out_hit) NTP_CUDA(ctx, cudaMemcpyAsync(out_hit, d_oh, 8 * total, cudaMemcpyDeviceToHost, st));
+    }
+    NTP_CUDA(ctx, cudaStreamSynchronize(st));
+    return NTP_OK;
+}
+
 ntp_status ntp_calc_time_residual(ntp_ctx* ctx, const ntp_hit* hits, uint64_t n, const float src[3], float n800,
                                   double* tres, int32_t on_device, void* stream) {
     if (!ctx) return NTP_ERR_INVALID;
@@ -765,16 +948,8 @@ ntp_status ntp_calc_time_residual(ntp_ctx* ctx, const ntp_hit* hits, uint64_t n,
     if (!(n800 > 0.0f)) return invalid(ctx, "ntp_calc_time_residual: n800 must be > 0");
     cudaSetDevice(ctx->device);
     cudaStream_t st = on_device ? pick_stream(ctx, stream) : ctx->stream;
-    // tgeo per module, photon_prop_cuda.jl:913-914
-    std::vector<double> tgeo(ctx->n_tgt);
-    const double c_vac = 0.299792458;
-    for (int k = 0; k < ctx->n_tgt; ++k) {
-        const ntp_target& t = ctx->targets[k];
-        const float dx = src[0] - t.position[0], dy = src[1] - t.position[1], dz = src[2] - t.position[2];
-        const float distance = std::sqrt(dx * dx + dy * dy + dz * dz);
-        tgeo[k] = static_cast<double>(distance - t.radius) / (c_vac / static_cast<double>(n800));
-    }
-    NTP_CUDA(ctx, cudaMemcpyAsync(ctx->d_tgeo, tgeo.data(), sizeof(double) * tgeo.size(), cudaMemcpyHostToDevice, st));
+    ntp_status sg = upload_tgeo(ctx, src, n800, st);
+    if (sg != NTP_OK) return sg;
     const ntp_hit* d_hits = nullptr;
     ntp_status s = stage_hits(ctx, hits, n, on_device, st, &d_hits);
     if (s != NTP_OK) return s;

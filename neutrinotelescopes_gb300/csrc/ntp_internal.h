@@ -124,6 +124,25 @@ cudaError_t launch_total_weight(const HitTargetTable& t, const ntp_hit* hits, un
                                 const double* acc_wl, const double* acc, int n_acc,
                                 double* area_acc, double* wl_acc, double* abs_weight,
                                 double* total, cudaStream_t stream);
+cudaError_t launch_pmt_summary(const HitTargetTable& t, const ntp_hit* hits, unsigned long long n, const double* axes,
+                               const float* abs_wl, const float* abs_len, int n_abs, const double* acc_wl,
+                               const double* acc, int n_acc, const double* tgeo, int use_tres, int max_pmts,
+                               int n_bins, double t_min, double t_max, double* wsum, double* count, double* hist,
+                               cudaStream_t stream);
+// resample_simulation passes (resample.cu)
+cudaError_t launch_resample_group(const ntp_hit* hits, unsigned long long n, const int32_t* pmt, const double* w,
+                                  const uint2* sorted_ids, int n_targets, int max_pmts, int32_t* group, double* wsum,
+                                  unsigned long long* npos, unsigned long long* nall, cudaStream_t st);
+cudaError_t launch_resample_draw(int n_groups, const double* wsum, const unsigned long long* npos, double downsample,
+                                 uint2 key, unsigned long long* nsel, cudaStream_t st);
+cudaError_t launch_resample_bucket(const ntp_hit* hits, unsigned long long n, const int32_t* group, const double* w,
+                                   uint2 key, const unsigned long long* start, unsigned long long* fill,
+                                   unsigned long long* order, unsigned long long* okey, cudaStream_t st);
+cudaError_t launch_resample_select(int n_groups, const ntp_hit* hits, const double* tval,
+                                   const unsigned long long* start, const unsigned long long* nall,
+                                   const unsigned long long* nsel, const unsigned long long* out_start,
+                                   const unsigned long long* order, const unsigned long long* okey, int32_t* out_group,
+                                   double* out_time, unsigned long long* out_hit, cudaStream_t st);
 cudaError_t launch_time_residual(const HitTargetTable& t, const ntp_hit* hits, unsigned long long n,
                                  const double* tgeo, double* tres, cudaStream_t stream);
 

@@ -266,3 +266,70 @@ def calc_time_residual(hits: HitTable, setup: PhotonPropSetup) -> HitTable:
 
 
 calc_time_residual_ = calc_time_residual
+
+
+def pmt_summary(hits: HitTable, setup: PhotonPropSetup, target_orientation, *, n_bins: int = 0,
+                t_range=(-20.0, 1500.0), time_residual: bool = True) -> dict:
+    """Per (target, PMT) weight sums, hit counts and weighted time histograms
+    in double precision (ntp_pmt_summary): the fusion of
+    make_hits_from_photons, calc_total_weight and calc_time_residual with the
+    per-(module, PMT) grouping of resample_simulation.  Arrays are indexed
+    [target index, pmt - 1 (, bin)]."""
+    lib, ctx = setup.context()
+    max_pmts = max([t.pmt_coordinates.shape[1] if isinstance(t, MultiPMTDetector) else 1 for t in setup.targets]
+                   or [1])
+    n_t = len(setup.targets)
+    recs = np.ascontiguousarray(hits.records)
+    R = np.ascontiguousarray(np.asarray(target_orientation, dtype=np.float64).reshape(3, 3))
+    n800 = float(np.float32(np.asarray(setup.medium.refractive_index(np.array([800.0])))[0]))
+    spec = _abi.NtpSummarySpec(max_pmts=max_pmts, n_bins=n_bins, t_min=t_range[0], t_max=t_range[1],
+                               use_time_residual=int(time_residual),
+                               source_position=tuple(float(v) for v in setup.sources[0].position) if setup.sources
+                               else (0.0, 0.0, 0.0), n800=n800)
+    wsum = np.zeros((n_t, max_pmts))
+    count = np.zeros((n_t, max_pmts))
+    hist = np.zeros((n_t, max_pmts, max(n_bins, 1)))
+    _check(lib, ctx, lib.ntp_pmt_summary(ctx, recs.ctypes.data, len(recs), R.ctypes.data_as(C.POINTER(C.c_double)),
+                                         C.byref(spec), wsum.ctypes.data, count.ctypes.data,
+                                         hist.ctypes.data if n_bins > 0 else None, 0, None))
+    out = {"weight_sum": wsum, "hit_count": count}
+    if n_bins > 0:
+        out["time_hist"] = hist
+        out["bin_edges"] = np.linspace(t_range[0], t_range[1], n_bins + 1)
+    return out
+
+
+def resample_simulation(hits: HitTable, setup: PhotonPropSetup, *, downsample: float = 1.0, seed: int = 0,
+                        time_col: str = "time") -> dict:
+    """Poisson-resampled hits per (module, PMT) (resample_simulation with
+    per_pmt = true, pmt_frontend/pipeline.jl:86-116) on the device.
+
+    ``hits`` needs the ``pmt_id`` column (make_hits_from_photons) and
+    ``total_weight`` (calc_total_weight); ``time_col`` names the time that is
+    kept ("time", or "tres" after calc_time_residual).  Returns columns
+    pmt_id, module_id, the time column and hit_index (row in ``hits``),
+    grouped by (module, PMT).
+    """
+    lib, ctx = setup.context()
+    max_pmts = max([t.pmt_coordinates.shape[1] if isinstance(t, MultiPMTDetector) else 1 for t in setup.targets]
+                   or [1])
+    recs = np.ascontiguousarray(hits.records)
+    n = len(recs)
+    pmt = np.ascontiguousarray(hits["pmt_id"], dtype=np.int32)
+    w = np.ascontiguousarray(hits["total_weight"], dtype=np.float64)
+    tv = np.ascontiguousarray(hits[time_col], dtype=np.float64)
+    cap = max(n, 1)
+    g = np.zeros(cap, dtype=np.int32)
+    t = np.zeros(cap)
+    hi = np.zeros(cap, dtype=np.uint64)
+    n_out = C.c_uint64()
+    _check(lib, ctx, lib.ntp_resample(ctx, recs.ctypes.data, n, pmt.ctypes.data, w.ctypes.data, tv.ctypes.data,
+                                      max_pmts, float(downsample), C.c_uint64(seed & (2 ** 64 - 1)), g.ctypes.data,
+                                      t.ctypes.data, hi.ctypes.data, cap, C.byref(n_out), 0, None))
+    k = n_out.value
+    g, t, hi = g[:k], t[:k], hi[:k]
+    order = np.lexsort((hi, g))
+    g, t, hi = g[order], t[order], hi[order]
+    module_ids = np.array([tg.module_id for tg in setup.targets], dtype=np.uint32)
+    return {"pmt_id": (g % max_pmts + 1).astype(np.int32), "module_id": module_ids[g // max_pmts],
+            time_col: t, "hit_index": hi}

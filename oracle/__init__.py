@@ -76,6 +76,10 @@ def lib() -> C.CDLL:
         L.ntpo_frank_tamm_norm.restype = d
         L.ntpo_sample_wavelengths.argtypes = [C.POINTER(_abi.NtpSpectrumDesc), u64, u32, u64, dp]
         L.ntpo_sample_gamma.argtypes = [C.c_float, C.c_float, u64, u32, u64, dp]
+        L.ntpo_poisson.argtypes = [d, u64, u32]
+        L.ntpo_poisson.restype = d
+        L.ntpo_resample.argtypes = [vp, u64, vp, vp, vp, C.POINTER(_abi.NtpTarget), i32, i32, d, u64, vp, vp, vp, u64]
+        L.ntpo_resample.restype = u64
         L.ntpo_hg_costheta.argtypes = [d, d]
         L.ntpo_hg_costheta.restype = d
         L.ntpo_rayleigh_costheta.argtypes = [d]
@@ -235,3 +239,21 @@ def sample_gamma(shape, scale, n, seed=0, src_index=0) -> np.ndarray:
     out = np.zeros(n)
     lib().ntpo_sample_gamma(shape, scale, seed, src_index, n, out.ctypes.data_as(C.POINTER(C.c_double)))
     return out
+
+
+def resample(hits: np.ndarray, pmt: np.ndarray, weight: np.ndarray, setup, max_pmts: int, downsample: float = 1.0,
+             seed: int = 0, time=None) -> dict:
+    from neutrinotelescopes_gb300.detection import pack_targets
+    tg, _ = pack_targets(setup.targets)
+    hits = np.ascontiguousarray(hits)
+    pmt = np.ascontiguousarray(pmt, dtype=np.int32)
+    weight = np.ascontiguousarray(weight, dtype=np.float64)
+    tv = None if time is None else np.ascontiguousarray(time, dtype=np.float64)
+    cap = max(1, len(hits))
+    g = np.zeros(cap, dtype=np.int32)
+    t = np.zeros(cap)
+    h = np.zeros(cap, dtype=np.uint64)
+    n = lib().ntpo_resample(hits.ctypes.data, len(hits), pmt.ctypes.data, weight.ctypes.data,
+                            None if tv is None else tv.ctypes.data, tg, len(setup.targets), max_pmts, downsample, seed,
+                            g.ctypes.data, t.ctypes.data, h.ctypes.data, cap)
+    return {"group": g[:n], "time": t[:n], "hit": h[:n]}

@@ -417,3 +417,114 @@ void ntpo_sample_gamma(float shape, float scale, uint64_t seed, uint32_t src_ind
 /* Scattering cosines for tests of the phase functions. */
 double ntpo_hg_costheta(double g, double eta) { return hg_costheta_f64(g, eta); }
 double ntpo_rayleigh_costheta(double u) { return rayleigh_costheta_f64(u); }
+
+/* ------------------------------------------------------------------------
+ * resample_simulation, pmt_frontend/pipeline.jl:86-116 (per_pmt = true),
+ * with the random draws of the device version: Poisson counts from the
+ * Philox stream of each (module, PMT) group (inversion below a mean of 30,
+ * Hormann's PTRS above), and the weighted draw without replacement as the N
+ * largest exponential keys log(u)/w (Efraimidis-Spirakis), u from the Philox
+ * stream of each hit's (source, photon). */
+#define NTPO_DRAW_RESAMPLE_KEY 0x52534B59u
+#define NTPO_DRAW_POISSON 0x504F4953u
+
+static double ntpo_u01_53(uint32_t a, uint32_t b) {
+    uint64_t m = ((uint64_t)a << 21) ^ (b >> 11);
+    return ((double)(m & ((1ull << 53) - 1)) + 0.5) * (1.0 / 9007199254740992.0);
+}
+
+static uint64_t ntpo_ordered(double x) {
+    uint64_t b;
+    memcpy(&b, &x, 8);
+    return (b >> 63) ? ~b : (b | 0x8000000000000000ull);
+}
+
+double ntpo_poisson(double lam, uint64_t seed, uint32_t group) {
+    uint32_t key[2] = {(uint32_t)seed, (uint32_t)(seed >> 32)}, r[4];
+    if (!(lam > 0.0)) return 0.0;
+    if (lam < 30.0) {
+        uint32_t c[4] = {NTPO_DRAW_POISSON, group, 0u, 0u};
+        ntpo_philox4x32_10(c, key, r);
+        double u = ntpo_u01_53(r[0], r[1]), p = exp(-lam), F = p, k = 0.0;
+        while (u > F && k < 1000.0) {
+            k += 1.0;
+            p *= lam / k;
+            F += p;
+        }
+        return k;
+    }
+    double slam = sqrt(lam), loglam = log(lam);
+    double b = 0.931 + 2.53 * slam, a = -0.059 + 0.02483 * b;
+    double invalpha = 1.1239 + 1.1328 / (b - 3.4), vr = 0.9277 - 3.6224 / (b - 2.0);
+    for (int t = 0; t < 64; ++t) {
+        uint32_t c[4] = {NTPO_DRAW_POISSON, group, (uint32_t)t + 1u, 0u};
+        ntpo_philox4x32_10(c, key, r);
+        double U = ntpo_u01_53(r[0], r[1]) - 0.5, V = ntpo_u01_53(r[2], r[3]);
+        double us = 0.5 - fabs(U);
+        double k = floor((2.0 * a / us + b) * U + lam + 0.43);
+        if (us >= 0.07 && V <= vr) return k;
+        if (k < 0.0 || (us < 0.013 && V > us)) continue;
+        if (log(V) + log(invalpha) - log(a / (us * us) + b) <= -lam + k * loglam - lgamma(k + 1.0)) return k;
+    }
+    return floor(lam + 0.5);
+}
+
+typedef struct { uint64_t key, hit; } ntpo_keyed;
+static int ntpo_desc(const void* a, const void* b) {
+    uint64_t x = ((const ntpo_keyed*)a)->key, y = ((const ntpo_keyed*)b)->key;
+    return x < y ? 1 : (x > y ? -1 : 0);
+}
+
+/* Returns the number of drawn hits; writes (group, time, hit index) grouped by
+   increasing group, each group by decreasing key, up to cap. */
+uint64_t ntpo_resample(const ntp_hit* hits, uint64_t n, const int32_t* pmt, const double* w, const double* tval,
+                       const ntp_target* tg, int n_tg, int max_pmts, double downsample, uint64_t seed,
+                       int32_t* out_group, double* out_time, uint64_t* out_hit, uint64_t cap) {
+    uint32_t key[2] = {(uint32_t)seed, (uint32_t)(seed >> 32)};
+    size_t G = (size_t)n_tg * (size_t)max_pmts;
+    int32_t* grp = (int32_t*)malloc(sizeof(int32_t) * (n ? n : 1));
+    double* wsum = (double*)calloc(G ? G : 1, sizeof(double));
+    uint64_t* npos = (uint64_t*)calloc(G ? G : 1, sizeof(uint64_t));
+    for (uint64_t i = 0; i < n; ++i) {
+        int k = -1;
+        for (int t = 0; t < n_tg; ++t)
+            if (tg[t].module_id == hits[i].module_id) { k = t; break; }
+        grp[i] = -1;
+        if (k >= 0 && pmt[i] > 0 && pmt[i] <= max_pmts) {
+            grp[i] = k * max_pmts + pmt[i] - 1;
+            wsum[grp[i]] += w[i];
+            if (w[i] > 0.0) npos[grp[i]]++;
+        }
+    }
+    uint64_t total = 0;
+    ntpo_keyed* buf = (ntpo_keyed*)malloc(sizeof(ntpo_keyed) * (n ? n : 1));
+    for (size_t g = 0; g < G; ++g) {
+        double kk = ntpo_poisson(wsum[g] * downsample, seed, (uint32_t)g);
+        uint64_t want = kk < (double)npos[g] ? (uint64_t)kk : npos[g];
+        if (!want) continue;
+        uint64_t m = 0;
+        for (uint64_t i = 0; i < n; ++i) {
+            if (grp[i] != (int32_t)g || !(w[i] > 0.0)) continue;
+            uint32_t c[4] = {NTPO_DRAW_RESAMPLE_KEY, (uint32_t)hits[i].photon_index,
+                             (uint32_t)(hits[i].photon_index >> 32), hits[i].source_index}, r[4];
+            ntpo_philox4x32_10(c, key, r);
+            buf[m].key = ntpo_ordered(log(ntpo_u01_53(r[0], r[1])) / w[i]);
+            buf[m].hit = i;
+            ++m;
+        }
+        qsort(buf, m, sizeof(ntpo_keyed), ntpo_desc);
+        for (uint64_t q = 0; q < want; ++q, ++total) {
+            if (total < cap) {
+                uint64_t i = buf[q].hit;
+                if (out_group) out_group[total] = (int32_t)g;
+                if (out_time) out_time[total] = tval ? tval[i] : (double)hits[i].time;
+                if (out_hit) out_hit[total] = i;
+            }
+        }
+    }
+    free(buf);
+    free(grp);
+    free(wsum);
+    free(npos);
+    return total;
+}

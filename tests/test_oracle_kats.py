@@ -118,3 +118,12 @@ def test_split_source_conserves_photons(kats):
     assert sum(p.photons for p in parts) == src.photons
     with pytest.raises(ValueError):
         split_source(PointlikeTimeRangeEmitter((0, 0, 0), (0, 1), 3), 4)
+
+
+@pytest.mark.parametrize("lam", [0.3, 5.0, 29.0, 31.0, 300.0, 1e4])
+def test_poisson_sampler_moments(oracle_lib, lam):
+    L = oracle_lib.lib()
+    x = np.array([L.ntpo_poisson(lam, 12345, g) for g in range(20000)])
+    assert abs(x.mean() - lam) < 5 * np.sqrt(lam / len(x))
+    assert abs(x.var() / lam - 1) < 0.1
+    assert np.all(x == np.floor(x)) and np.all(x >= 0)

@@ -296,3 +296,61 @@ def test_single_target_column_swap():
     h = nt.propagate_photons(s, seed=2)
     assert np.array_equal(h["direction"], h.records["initial_direction"])
     assert np.array_equal(h["initial_direction"], h.records["direction"])
+
+
+def test_pmt_summary_matches_oracle_composition(orc):
+    # per (module, PMT) FP64 sums of the oracle's per-hit PMT ids, weights and time residuals
+    s = cascade_small_setup(1_000_000)
+    h = nt.propagate_photons(s, seed=31, reference_columns=False)
+    R = nt.utils.random_rotation(np.random.default_rng(4))
+    out = nt.pmt_summary(h, s, R, n_bins=64, t_range=(-20.0, 300.0))
+    recs = h.records
+    pmt = orc.make_hits(recs, s, R)
+    w = orc.total_weight(recs, s, nt.p_one_pmt_acc)["total_weight"]
+    n800 = float(np.float32(s.medium.refractive_index(np.array([800.0]))[0]))
+    tres = orc.time_residual(recs, s, n800)
+    index = {t.module_id: i for i, t in enumerate(s.targets)}
+    k = np.array([index[m] for m in recs["module_id"]])
+    sel = pmt > 0
+    want_w = np.zeros((20, 16))
+    want_c = np.zeros((20, 16))
+    np.add.at(want_w, (k[sel], pmt[sel] - 1), w[sel])
+    np.add.at(want_c, (k[sel], pmt[sel] - 1), 1.0)
+    np.testing.assert_array_equal(out["hit_count"], want_c)
+    np.testing.assert_allclose(out["weight_sum"], want_w, rtol=1e-6, atol=1e-12)
+    assert want_c.sum() > 10
+    edges = out["bin_edges"]
+    want_h = np.zeros((20, 16, 64))
+    b = np.floor((tres - edges[0]) * 64 / (edges[-1] - edges[0]))
+    inb = sel & (b >= 0) & (b < 64)
+    np.add.at(want_h, (k[inb], pmt[inb] - 1, b[inb].astype(int)), w[inb])
+    np.testing.assert_allclose(out["time_hist"], want_h, rtol=1e-6, atol=1e-12)
+
+
+def test_resample_matches_oracle_and_reference_usage(orc):
+    # the reference's chain (simulate_event_full_test.jl:61-65): make_hits -> weights -> resample
+    s = cascade_small_setup(2_000_000)
+    h = nt.propagate_photons(s, seed=41, reference_columns=False)
+    R = np.eye(3)
+    hits = nt.make_hits_from_photons(h, s, R)
+    nt.calc_total_weight(hits, s)
+    nt.calc_time_residual(hits, s)
+    assert len(hits) > 30
+    for seed, down in ((5, 1.0), (6, 25.0)):
+        got = nt.resample_simulation(hits, s, downsample=down, seed=seed, time_col="tres")
+        want = orc.resample(hits.records, hits["pmt_id"], hits["total_weight"], s, 16, down, seed, hits["tres"])
+        a = sorted(zip(got["hit_index"].tolist(), (got["module_id"] * 100 + got["pmt_id"]).tolist()))
+        index = {t.module_id: i for i, t in enumerate(s.targets)}
+        b = sorted(zip(want["hit"].tolist(),
+                       [s.targets[g // 16].module_id * 100 + g % 16 + 1 for g in want["group"].tolist()]))
+        assert a == b
+        np.testing.assert_array_equal(np.sort(got["tres"]), np.sort(want["time"]))
+        # drawn hits are distinct and belong to their group
+        assert len(set(got["hit_index"].tolist())) == len(got["hit_index"])
+        assert np.all(hits["pmt_id"][got["hit_index"].astype(int)] == got["pmt_id"])
+    # a large downsample factor draws (nearly) every hit with w > 0, never more
+    big = nt.resample_simulation(hits, s, downsample=1e6, seed=1, time_col="tres")
+    want = orc.resample(hits.records, hits["pmt_id"], hits["total_weight"], s, 16, 1e6, 1, hits["tres"])
+    assert sorted(big["hit_index"].tolist()) == sorted(want["hit"].tolist())
+    assert len(big["tres"]) <= int(np.sum(hits["total_weight"] > 0))
+    assert len(big["tres"]) >= 0.9 * int(np.sum(hits["total_weight"] > 0))
