@@ -315,6 +315,19 @@ ntp_status ntp_resample(ntp_ctx* ctx, const ntp_hit* hits, uint64_t n_hits, cons
                         uint64_t seed, int32_t* out_group, double* out_time, uint64_t* out_hit,
                         uint64_t capacity, uint64_t* n_out, int32_t buffers_on_device, void* stream);
 
+/* ------------------------------------------------------------ tensor cores
+ * C = A * B^T with BF16 A [M x K] and B [N x K] (row-major, K contiguous,
+ * device pointers, 16-byte aligned rows: lda, ldb multiples of 8, K a
+ * multiple of 64), FP32 accumulation on the tensor cores (tcgen05 + TMA),
+ * plus bias[N] (FP32, may be NULL) and optional ReLU.  out_kind 0 stores
+ * FP32, 1 stores BF16, 2 adds FP32 atomically (with splits > 1 the K range is
+ * split across CTAs; C must be zeroed first).  The GEMM of the flow's
+ * conditioner network (no reference counterpart: the reference uses
+ * Flux Dense layers, extended_cascade_model.jl:53-101). */
+ntp_status ntp_gemm_bf16(const void* A, int32_t lda, const void* B, int32_t ldb, void* C, int32_t ldc, int32_t M,
+                         int32_t N, int32_t K, const float* bias, int32_t relu, int32_t out_kind, int32_t splits,
+                         void* stream);
+
 /* ------------------------------------------------------------------ serving
  * Continuous-batching event server (no reference counterpart; the reference
  * runs one propagate_photons per event, photon_prop_cuda.jl:804-817).  Each

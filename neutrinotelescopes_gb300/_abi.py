@@ -221,6 +221,7 @@ EXPORTED = (
     "ntp_calc_time_residual",
     "ntp_pmt_summary",
     "ntp_resample",
+    "ntp_gemm_bf16",
     "ntp_server_create",
     "ntp_server_destroy",
     "ntp_server_submit",
@@ -262,6 +263,8 @@ def _declare(lib: C.CDLL) -> None:
     lib.ntp_resample.argtypes = [vp, vp, u64, vp, vp, vp, i32, C.c_double, u64, vp, vp, vp, u64, C.POINTER(u64),
                                  i32, vp]
     lib.ntp_resample.restype = C.c_int
+    lib.ntp_gemm_bf16.argtypes = [vp, i32, vp, i32, vp, i32, i32, i32, i32, vp, i32, i32, i32, vp]
+    lib.ntp_gemm_bf16.restype = C.c_int
     lib.ntp_server_create.argtypes = [vp, C.POINTER(NtpServerConfig), C.POINTER(vp)]
     lib.ntp_server_destroy.argtypes = [vp]
     lib.ntp_server_destroy.restype = None

@@ -1,0 +1,338 @@
+// flow_gemm.cu -- BF16 GEMM on the 5th-generation tensor cores (tcgen05) for
+// the conditioner MLP of the arrival-time flow.
+//
+// C[M x N] = A[M x K] * B[N x K]^T (+ bias[N], optional ReLU), A and B
+// row-major with K contiguous (K-major), FP32 accumulation in tensor memory.
+//   * one CTA per 128 x BN output tile, 128 threads (4 warps);
+//   * operands staged in shared memory by TMA (cp.async.bulk.tensor) in the
+//     128-byte-swizzled layout, two pipeline stages of 64-wide K slices;
+//   * one elected thread issues tcgen05.mma (cta_group::1, kind::f16, BF16
+//     inputs, FP32 accumulator of 128 lanes x BN columns in TMEM) and
+//     tcgen05.commit signals the stage free / the accumulator complete;
+//   * the epilogue: each warp reads its 32 TMEM lanes with tcgen05.ld, adds
+//     the bias, applies ReLU and stores FP32 or BF16, or atomically adds FP32
+//     (split-K, for weight gradients whose K is the batch).
+// Every wait on an mbarrier gives up after a bounded number of polls, sets
+// the error word and skips to the TMEM release, so a fault in the pipeline
+// returns a status instead of hanging the GPU.
+#include <cuda.h>
+#include <cuda_bf16.h>
+#include <cuda_runtime.h>
+
+#include <cstdint>
+#include <mutex>
+
+#include "ntp_internal.h"
+
+namespace ntp {
+
+namespace {
+
+constexpr int kBM = 128;   // rows of a tile (UMMA M)
+constexpr int kBK = 64;    // K slice per stage: 64 bf16 = 128 bytes = one swizzle row
+constexpr int kUK = 16;    // K of one tcgen05.mma for 16-bit inputs
+constexpr int kStages = 2;
+constexpr int kThreads = 128;
+constexpr unsigned long long kWaitLimitNs = 2000000000ull;  // a wait gives up after 2 s
+
+__device__ __forceinline__ uint32_t smem_u32(const void* p) {
+    return static_cast<uint32_t>(__cvta_generic_to_shared(p));
+}
+
+__device__ __forceinline__ void mbar_init(uint64_t* bar, uint32_t count) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count));
+}
+
+__device__ __forceinline__ void mbar_expect_tx(uint64_t* bar, uint32_t bytes) {
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)), "r"(bytes)
+                 : "memory");
+}
+
+__device__ __forceinline__ unsigned long long global_ns() {
+    unsigned long long t;
+    asm volatile("mov.u64 %0, %globaltimer;" : "=l"(t));
+    return t;
+}
+
+// Bounded wait for the phase with the given parity; false after kWaitLimitNs.
+__device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity) {
+    const uint32_t a = smem_u32(bar);
+    const unsigned long long t0 = global_ns();
+    for (unsigned i = 0;; ++i) {
+        uint32_t done;
+        asm volatile(
+            "{\n.reg .pred p;\nmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\nselp.b32 %0, 1, 0, p;\n}\n"
+            : "=r"(done)
+            : "r"(a), "r"(parity)
+            : "memory");
+        if (done) return true;
+        if ((i & 255u) == 255u && global_ns() - t0 > kWaitLimitNs) return false;
+    }
+}
+
+__device__ __forceinline__ void tma_load_2d(void* dst, const CUtensorMap* map, uint64_t* bar, int x, int y) {
+    asm volatile(
+        "cp.async.bulk.tensor.2d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%3, %4}], [%2];"
+        ::"r"(smem_u32(dst)), "l"(reinterpret_cast<uint64_t>(map)), "r"(smem_u32(bar)), "r"(x), "r"(y)
+        : "memory");
+}
+
+// Shared-memory matrix descriptor of a K-major tile with 128-byte swizzle:
+// 8-row groups of 128-byte rows, 1024 bytes apart (stride byte offset),
+// descriptor version 1, layout type 2 (SWIZZLE_128B).
+__device__ __forceinline__ uint64_t smem_desc_sw128(const void* p) {
+    const uint64_t addr = smem_u32(p);
+    uint64_t d = (addr & 0x3FFFFull) >> 4;
+    d |= static_cast<uint64_t>(1) << 16;             // leading byte offset (unused for swizzled K-major)
+    d |= static_cast<uint64_t>(1024 >> 4) << 32;     // stride byte offset
+    d |= static_cast<uint64_t>(1) << 46;             // version
+    d |= static_cast<uint64_t>(2) << 61;             // SWIZZLE_128B
+    return d;
+}
+
+// Instruction descriptor, kind::f16: FP32 accumulator, BF16 A and B, both
+// K-major, N and M encoded as N/8 and M/16.
+__host__ __device__ constexpr uint32_t instr_desc_bf16(int m, int n) {
+    return (1u << 4) | (1u << 7) | (1u << 10) | (static_cast<uint32_t>(n >> 3) << 17) |
+           (static_cast<uint32_t>(m >> 4) << 24);
+}
+
+__device__ __forceinline__ void umma_bf16(uint32_t tmem_d, uint64_t adesc, uint64_t bdesc, uint32_t idesc,
+                                          uint32_t accumulate) {
+    asm volatile(
+        "{\n.reg .pred p;\nsetp.ne.b32 p, %4, 0;\ntcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}\n"
+        ::"r"(tmem_d), "l"(adesc), "l"(bdesc), "r"(idesc), "r"(accumulate)
+        : "memory");
+}
+
+__device__ __forceinline__ void umma_commit(uint64_t* bar) {
+    asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(smem_u32(bar))
+                 : "memory");
+}
+
+__device__ __forceinline__ void tmem_ld32(uint32_t taddr, float* v) {
+    uint32_t r[32];
+    asm volatile(
+        "tcgen05.ld.sync.aligned.32x32b.x32.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15,"
+        "%16,%17,%18,%19,%20,%21,%22,%23,%24,%25,%26,%27,%28,%29,%30,%31}, [%32];"
+        : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),
+          "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15]),
+          "=r"(r[16]), "=r"(r[17]), "=r"(r[18]), "=r"(r[19]), "=r"(r[20]), "=r"(r[21]), "=r"(r[22]), "=r"(r[23]),
+          "=r"(r[24]), "=r"(r[25]), "=r"(r[26]), "=r"(r[27]), "=r"(r[28]), "=r"(r[29]), "=r"(r[30]), "=r"(r[31])
+        : "r"(taddr));
+    asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+#pragma unroll
+    for (int i = 0; i < 32; ++i) v[i] = __uint_as_float(r[i]);
+}
+
+template <int BN>
+struct Smem {
+    alignas(1024) __nv_bfloat16 a[kStages][kBM * kBK];
+    alignas(1024) __nv_bfloat16 b[kStages][BN * kBK];
+    uint64_t full[kStages];
+    uint64_t empty[kStages];
+    uint64_t done;
+    uint32_t tmem;
+};
+
+// out_kind: 0 = FP32 store, 1 = BF16 store, 2 = FP32 atomic add (split-K)
+template <int BN>
+__global__ void __launch_bounds__(kThreads, 1)
+    gemm_bf16_kernel(const __grid_constant__ CUtensorMap map_a, const __grid_constant__ CUtensorMap map_b, void* c,
+                     int M, int N, int ldc, int k_tiles_per_split, int k_tiles_total, const float* __restrict__ bias,
+                     int relu, int out_kind, int* __restrict__ error) {
+    extern __shared__ unsigned char smem_raw[];
+    Smem<BN>* s = reinterpret_cast<Smem<BN>*>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int m0 = blockIdx.x * kBM, n0 = blockIdx.y * BN;
+    const int kt0 = blockIdx.z * k_tiles_per_split;
+    const int kt1 = min(kt0 + k_tiles_per_split, k_tiles_total);
+    constexpr uint32_t kCols = BN <= 32 ? 32 : (BN <= 64 ? 64 : (BN <= 128 ? 128 : 256));
+
+    if (warp == 0) {
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(&s->tmem)),
+                     "r"(kCols));
+        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
+    }
+    if (threadIdx.x == 0) {
+        for (int i = 0; i < kStages; ++i) {
+            mbar_init(&s->full[i], 1);
+            mbar_init(&s->empty[i], 1);
+        }
+        mbar_init(&s->done, 1);
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+        asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+    }
+    asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+    __syncthreads();
+    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+    const uint32_t tmem = s->tmem;
+    bool ok = true;
+
+    if (threadIdx.x == 0 && kt1 > kt0) {
+        constexpr uint32_t kStageBytes = (kBM + BN) * kBK * sizeof(__nv_bfloat16);
+        const uint32_t idesc = instr_desc_bf16(kBM, BN);
+        const int nk = kt1 - kt0;
+        int issued[kStages] = {}, landed[kStages] = {};  // TMA pairs per stage
+        for (int i = 0; i < kStages && i < nk; ++i) {
+            mbar_expect_tx(&s->full[i], kStageBytes);
+            tma_load_2d(s->a[i], &map_a, &s->full[i], (kt0 + i) * kBK, m0);
+            tma_load_2d(s->b[i], &map_b, &s->full[i], (kt0 + i) * kBK, n0);
+            ++issued[i];
+        }
+        for (int i = 0; i < nk && ok; ++i) {
+            const int st = i % kStages;
+            ok = mbar_wait(&s->full[st], (i / kStages) & 1);
+            if (!ok) break;
+            ++landed[st];
+            asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+#pragma unroll
+            for (int kk = 0; kk < kBK / kUK; ++kk) {
+                const uint64_t ad = smem_desc_sw128(s->a[st]) + static_cast<uint64_t>((kk * kUK * 2) >> 4);
+                const uint64_t bd = smem_desc_sw128(s->b[st]) + static_cast<uint64_t>((kk * kUK * 2) >> 4);
+                umma_bf16(tmem, ad, bd, idesc, (i > 0 || kk > 0) ? 1u : 0u);
+            }
+            umma_commit(&s->empty[st]);
+            // refill the stage of the previous slice once its MMAs have read it
+            const int prev = i - 1;
+            if (prev >= 0 && prev + kStages < nk) {
+                const int ps = prev % kStages;
+                ok = mbar_wait(&s->empty[ps], (prev / kStages) & 1);
+                if (!ok) break;
+                mbar_expect_tx(&s->full[ps], kStageBytes);
+                tma_load_2d(s->a[ps], &map_a, &s->full[ps], (kt0 + prev + kStages) * kBK, m0);
+                tma_load_2d(s->b[ps], &map_b, &s->full[ps], (kt0 + prev + kStages) * kBK, n0);
+                ++issued[ps];
+            }
+        }
+        umma_commit(&s->done);
+        if (!ok) {
+            atomicExch(error, 1);
+            // let copies still in flight land before the CTA's shared memory goes away
+            for (int st = 0; st < kStages; ++st)
+                while (landed[st] < issued[st] && mbar_wait(&s->full[st], landed[st] & 1)) ++landed[st];
+        }
+    }
+    __syncwarp();
+    // the accumulator is complete when `done` flips (a thread that timed out
+    // above still committed, so this wait ends once its MMAs drain)
+    const bool have = (kt1 > kt0) && mbar_wait(&s->done, 0);
+    if (kt1 > kt0 && !have && lane == 0) atomicExch(error, 2);
+    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+
+    if (have) {
+        const int row = m0 + warp * 32 + lane;
+#pragma unroll 1
+        for (int c0 = 0; c0 < BN; c0 += 32) {
+            float v[32];
+            tmem_ld32(tmem + (static_cast<uint32_t>(warp * 32) << 16) + static_cast<uint32_t>(c0), v);
+            if (row < M) {
+#pragma unroll
+                for (int j = 0; j < 32; ++j) {
+                    const int col = n0 + c0 + j;
+                    if (col >= N) continue;
+                    float x = v[j];
+                    if (bias && blockIdx.z == 0) x += bias[col];
+                    if (relu) x = fmaxf(x, 0.0f);
+                    const size_t o = static_cast<size_t>(row) * ldc + col;
+                    if (out_kind == 0) static_cast<float*>(c)[o] = x;
+                    else if (out_kind == 1) static_cast<__nv_bfloat16*>(c)[o] = __float2bfloat16(x);
+                    else atomicAdd(static_cast<float*>(c) + o, x);
+                }
+            }
+        }
+    }
+    asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+    __syncthreads();
+    if (warp == 0) asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(kCols));
+}
+
+using EncodeTiled = CUresult (*)(CUtensorMap*, CUtensorMapDataType, cuuint32_t, void*, const cuuint64_t*,
+                                 const cuuint64_t*, const cuuint32_t*, const cuuint32_t*, CUtensorMapInterleave,
+                                 CUtensorMapSwizzle, CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
+
+EncodeTiled encode_fn() {
+    static EncodeTiled fn = nullptr;
+    static std::once_flag once;
+    std::call_once(once, [] {
+        void* p = nullptr;
+        cudaDriverEntryPointQueryResult q;
+        if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) ==
+                cudaSuccess &&
+            q == cudaDriverEntryPointSuccess)
+            fn = reinterpret_cast<EncodeTiled>(p);
+    });
+    return fn;
+}
+
+// Tensor map of a row-major bf16 matrix [rows x cols] (leading dimension ld
+// elements) read in boxes of box_rows x 64 with 128-byte swizzle; rows and
+// columns beyond the matrix read as zero.
+bool make_map(CUtensorMap* map, const void* base, int rows, int cols, int ld, int box_rows) {
+    EncodeTiled enc = encode_fn();
+    if (!enc) return false;
+    const cuuint64_t dims[2] = {static_cast<cuuint64_t>(cols), static_cast<cuuint64_t>(rows)};
+    const cuuint64_t strides[1] = {static_cast<cuuint64_t>(ld) * 2};
+    const cuuint32_t box[2] = {static_cast<cuuint32_t>(kBK), static_cast<cuuint32_t>(box_rows)};
+    const cuuint32_t estr[2] = {1, 1};
+    return enc(map, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2, const_cast<void*>(base), dims, strides, box, estr,
+               CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+               CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
+}
+
+template <int BN>
+cudaError_t launch_bn(const CUtensorMap& ma, const CUtensorMap& mb, void* c, int M, int N, int ldc, int splits,
+                      int k_tiles, const float* bias, int relu, int out_kind, int* error, cudaStream_t st) {
+    const size_t smem = sizeof(Smem<BN>) + 1024;
+    cudaError_t e = cudaFuncSetAttribute(gemm_bf16_kernel<BN>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         static_cast<int>(smem));
+    if (e != cudaSuccess) return e;
+    const int per = (k_tiles + splits - 1) / splits;
+    dim3 grid((M + kBM - 1) / kBM, (N + BN - 1) / BN, splits);
+    gemm_bf16_kernel<BN><<<grid, kThreads, smem, st>>>(ma, mb, c, M, N, ldc, per, k_tiles, bias, relu, out_kind,
+                                                      error);
+    return cudaGetLastError();
+}
+
+}  // namespace
+
+// C = A * B^T on the tensor cores; see the file comment.  lda / ldb / ldc in
+// elements; A's and B's rows must start on 16-byte boundaries (lda, ldb
+// multiples of 8) and K a multiple of 64.  splits > 1 splits K across CTAs
+// and requires out_kind 2 (atomic add into a zeroed C).
+cudaError_t gemm_bf16(const void* A, int lda, const void* B, int ldb, void* C, int ldc, int M, int N, int K,
+                      const float* bias, int relu, int out_kind, int splits, int* error, cudaStream_t st) {
+    if (M <= 0 || N <= 0 || K <= 0 || K % kBK || lda % 8 || ldb % 8 || (splits > 1 && out_kind != 2) ||
+        (reinterpret_cast<uintptr_t>(A) & 15) || (reinterpret_cast<uintptr_t>(B) & 15))
+        return cudaErrorInvalidValue;
+    const int bn = N <= 64 ? 64 : (N <= 128 ? 128 : 256);
+    CUtensorMap ma, mb;
+    if (!make_map(&ma, A, M, K, lda, kBM) || !make_map(&mb, B, N, K, ldb, bn)) return cudaErrorInvalidValue;
+    const int k_tiles = K / kBK;
+    splits = splits < 1 ? 1 : (splits > k_tiles ? k_tiles : splits);
+    if (bn == 64) return launch_bn<64>(ma, mb, C, M, N, ldc, splits, k_tiles, bias, relu, out_kind, error, st);
+    if (bn == 128) return launch_bn<128>(ma, mb, C, M, N, ldc, splits, k_tiles, bias, relu, out_kind, error, st);
+    return launch_bn<256>(ma, mb, C, M, N, ldc, splits, k_tiles, bias, relu, out_kind, error, st);
+}
+
+}  // namespace ntp
+
+extern "C" ntp_status ntp_gemm_bf16(const void* A, int32_t lda, const void* B, int32_t ldb, void* C, int32_t ldc,
+                                    int32_t M, int32_t N, int32_t K, const float* bias, int32_t relu,
+                                    int32_t out_kind, int32_t splits, void* stream) {
+    if (!A || !B || !C || out_kind < 0 || out_kind > 2) return NTP_ERR_INVALID;
+    static int* d_err = nullptr;  // error word of the GEMM pipeline (one per process)
+    static std::mutex mu;
+    std::lock_guard<std::mutex> lock(mu);
+    if (!d_err && cudaMalloc(&d_err, sizeof(int)) != cudaSuccess) return NTP_ERR_CUDA;
+    cudaStream_t st = static_cast<cudaStream_t>(stream);
+    if (cudaMemsetAsync(d_err, 0, sizeof(int), st) != cudaSuccess) return NTP_ERR_CUDA;
+    const cudaError_t e = ntp::gemm_bf16(A, lda, B, ldb, C, ldc, M, N, K, bias, relu, out_kind, splits, d_err, st);
+    if (e == cudaErrorInvalidValue) return NTP_ERR_INVALID;
+    if (e != cudaSuccess) return NTP_ERR_CUDA;
+    int h = 0;
+    if (cudaMemcpyAsync(&h, d_err, sizeof(int), cudaMemcpyDeviceToHost, st) != cudaSuccess ||
+        cudaStreamSynchronize(st) != cudaSuccess)
+        return NTP_ERR_CUDA;
+    return h ? NTP_ERR_TIMEOUT : NTP_OK;
+}

@@ -129,6 +129,11 @@ cudaError_t launch_pmt_summary(const HitTargetTable& t, const ntp_hit* hits, uns
                                const double* acc, int n_acc, const double* tgeo, int use_tres, int max_pmts,
                                int n_bins, double t_min, double t_max, double* wsum, double* count, double* hist,
                                cudaStream_t stream);
+// C = A * B^T, BF16 operands (K-major), FP32 accumulation on the tensor cores
+// (flow_gemm.cu).  out_kind: 0 = FP32, 1 = BF16, 2 = FP32 atomic add.
+cudaError_t gemm_bf16(const void* A, int lda, const void* B, int ldb, void* C, int ldc, int M, int N, int K,
+                      const float* bias, int relu, int out_kind, int splits, int* error, cudaStream_t st);
+
 // resample_simulation passes (resample.cu)
 cudaError_t launch_resample_group(const ntp_hit* hits, unsigned long long n, const int32_t* pmt, const double* w,
                                   const uint2* sorted_ids, int n_targets, int max_pmts, int32_t* group, double* wsum,
