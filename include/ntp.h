@@ -328,6 +328,59 @@ ntp_status ntp_gemm_bf16(const void* A, int32_t lda, const void* B, int32_t ldb,
                          int32_t N, int32_t K, const float* bias, int32_t relu, int32_t out_kind, int32_t splits,
                          void* stream);
 
+/* --------------------------------------------------------- arrival-time flow
+ * The per-module arrival-time surrogate: RQNormFlow with a log-expectation
+ * head (src/surrogate_models/extended_cascade_model.jl:53-139, with the
+ * spline of rq_spline_flow.jl:170-418), trained and evaluated on the GPU.
+ * Conditioner: 5 condition features -> 3 ReLU layers of 256 -> per spline
+ * layer 3K+1 raw values (K bins on [t_min, t_max]), then shift, raw scale and
+ * log expectation; n_layers stacked inverse splines (1 = the reference's
+ * model).  Weights BF16 on the tensor cores with FP32 accumulation, FP32
+ * master weights and Adam (Flux's defaults).  Parameters form one flat FP32
+ * vector: W1 [256 x 64] (only the first 5 input columns used), b1 [256],
+ * W2 [256 x 256], b2, W3 [256 x 256], b3, W4 [n_outputs_padded x 256], b4;
+ * rows of W4 beyond n_outputs stay zero. */
+typedef struct ntp_flow ntp_flow;
+
+typedef struct ntp_flow_config {
+    int32_t batch_capacity; /* most samples per training step / conditions per pass; multiple of 128 */
+    int32_t n_layers;       /* spline layers, 1..5                                           */
+    int32_t n_bins;         /* K, bins per spline: 10 (the reference's default) or 12        */
+    float t_min, t_max;     /* spline range (ns); linear tails outside                        */
+    float lr, beta1, beta2, eps; /* Adam                                                      */
+    uint64_t seed;          /* weight initialisation                                           */
+} ntp_flow_config;
+
+ntp_status ntp_flow_create(int32_t device, const ntp_flow_config* config, ntp_flow** out);
+void ntp_flow_destroy(ntp_flow* flow);
+const char* ntp_flow_last_error(const ntp_flow* flow);
+ntp_status ntp_flow_get_layout(const ntp_flow* flow, uint64_t* n_params, int32_t* n_outputs,
+                               int32_t* n_outputs_padded);
+/* Replaces the weights (host FP32, n = n_params) and resets Adam. */
+ntp_status ntp_flow_set_params(ntp_flow* flow, const float* host, uint64_t n);
+/* which: 0 weights, 1 gradient of the last training step, 2 / 3 Adam moments. */
+ntp_status ntp_flow_get_params(ntp_flow* flow, float* host, uint64_t n, int32_t which);
+/* One step of train_model! (extended_cascade_model.jl:237-295) on a batch of
+   B samples (a multiple of 128): cond [B x 5], time residual tres [B],
+   label hit count nhits [B], has_time [B] (0: the sample adds only the count
+   term).  update = 0 computes loss and gradient without an Adam step.  All
+   inputs on the host, or on the device when on_device != 0. */
+ntp_status ntp_flow_train_step(ntp_flow* flow, const float* cond, const float* tres, const float* nhits,
+                               const int32_t* has_time, int32_t B, int32_t on_device, int32_t update,
+                               double* loss);
+/* The conditioner's raw outputs for n conditions (host): params_out [n x n_outputs]. */
+ntp_status ntp_flow_forward(ntp_flow* flow, const float* cond, int32_t n, float* params_out);
+/* The loss and its gradient by the raw outputs, for given raw outputs
+   params [B x n_outputs] (host buffers; B <= batch_capacity). */
+ntp_status ntp_flow_head(ntp_flow* flow, const float* params, const float* tres, const float* nhits,
+                         const int32_t* has_time, int32_t B, double* loss, float* grad_out);
+/* The model call (extended_cascade_model.jl:110-125): log p(t | cond) for
+   n_tuples (condition index, time) pairs, and per condition the log
+   expectation (log_expec may be NULL).  An index outside [0, n_cond) gives NaN. */
+ntp_status ntp_flow_evaluate(ntp_flow* flow, const float* cond, int32_t n_cond, const int32_t* cond_index,
+                             const float* times, uint64_t n_tuples, float* logpdf, float* log_expec,
+                             int32_t on_device);
+
 /* ------------------------------------------------------------------ serving
  * Continuous-batching event server (no reference counterpart; the reference
  * runs one propagate_photons per event, photon_prop_cuda.jl:804-817).  Each

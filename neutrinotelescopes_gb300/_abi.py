@@ -183,6 +183,21 @@ class NtpSummarySpec(C.Structure):
     ]
 
 
+class NtpFlowConfig(C.Structure):
+    _fields_ = [
+        ("batch_capacity", C.c_int32),
+        ("n_layers", C.c_int32),
+        ("n_bins", C.c_int32),
+        ("t_min", C.c_float),
+        ("t_max", C.c_float),
+        ("lr", C.c_float),
+        ("beta1", C.c_float),
+        ("beta2", C.c_float),
+        ("eps", C.c_float),
+        ("seed", C.c_uint64),
+    ]
+
+
 assert C.sizeof(NtpSource) == 64
 assert C.sizeof(NtpTarget) == 48
 
@@ -222,6 +237,16 @@ EXPORTED = (
     "ntp_pmt_summary",
     "ntp_resample",
     "ntp_gemm_bf16",
+    "ntp_flow_create",
+    "ntp_flow_destroy",
+    "ntp_flow_last_error",
+    "ntp_flow_get_layout",
+    "ntp_flow_set_params",
+    "ntp_flow_get_params",
+    "ntp_flow_train_step",
+    "ntp_flow_forward",
+    "ntp_flow_head",
+    "ntp_flow_evaluate",
     "ntp_server_create",
     "ntp_server_destroy",
     "ntp_server_submit",
@@ -265,6 +290,21 @@ def _declare(lib: C.CDLL) -> None:
     lib.ntp_resample.restype = C.c_int
     lib.ntp_gemm_bf16.argtypes = [vp, i32, vp, i32, vp, i32, i32, i32, i32, vp, i32, i32, i32, vp]
     lib.ntp_gemm_bf16.restype = C.c_int
+    lib.ntp_flow_create.argtypes = [i32, C.POINTER(NtpFlowConfig), C.POINTER(vp)]
+    lib.ntp_flow_destroy.argtypes = [vp]
+    lib.ntp_flow_destroy.restype = None
+    lib.ntp_flow_last_error.argtypes = [vp]
+    lib.ntp_flow_last_error.restype = C.c_char_p
+    lib.ntp_flow_get_layout.argtypes = [vp, C.POINTER(u64), C.POINTER(i32), C.POINTER(i32)]
+    lib.ntp_flow_set_params.argtypes = [vp, vp, u64]
+    lib.ntp_flow_get_params.argtypes = [vp, vp, u64, i32]
+    lib.ntp_flow_train_step.argtypes = [vp, vp, vp, vp, vp, i32, i32, i32, C.POINTER(C.c_double)]
+    lib.ntp_flow_forward.argtypes = [vp, vp, i32, vp]
+    lib.ntp_flow_head.argtypes = [vp, vp, vp, vp, vp, i32, C.POINTER(C.c_double), vp]
+    lib.ntp_flow_evaluate.argtypes = [vp, vp, i32, vp, vp, u64, vp, vp, i32]
+    for name in ("ntp_flow_create", "ntp_flow_get_layout", "ntp_flow_set_params", "ntp_flow_get_params",
+                 "ntp_flow_train_step", "ntp_flow_forward", "ntp_flow_head", "ntp_flow_evaluate"):
+        getattr(lib, name).restype = C.c_int
     lib.ntp_server_create.argtypes = [vp, C.POINTER(NtpServerConfig), C.POINTER(vp)]
     lib.ntp_server_destroy.argtypes = [vp]
     lib.ntp_server_destroy.restype = None

@@ -45,12 +45,15 @@ def _stale(target: Path) -> bool:
 
 def _compile(src: Path, extra: list[str]) -> Path:
     obj = BUILD / (src.stem + ".o")
+    log = BUILD / (src.stem + ".log")
+    if log.exists():
+        log.unlink()
     cmd = [nvcc(), *ARCH, *NVCC_FLAGS, *extra, "-I", str(INCLUDE), "-c", str(src), "-o", str(obj)]
     r = subprocess.run(cmd, capture_output=True, text=True)
     if r.returncode != 0:
         raise RuntimeError(f"nvcc failed on {src.name}:\n{r.stdout}\n{r.stderr}")
     if r.stderr.strip():
-        (BUILD / (src.stem + ".log")).write_text(r.stderr)
+        log.write_text(r.stderr)
     return obj
 
 

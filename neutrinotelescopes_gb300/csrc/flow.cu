@@ -1,0 +1,981 @@
+// flow.cu -- the arrival-time surrogate: a conditional rational-quadratic-
+// spline flow with a Poisson count head, trained and evaluated on the GPU.
+//
+// Model (RQNormFlow, src/surrogate_models/extended_cascade_model.jl:53-125 and
+// rq_spline_flow.jl:127-418 of chrhck/NeutrinoTelescopes): a conditioner
+// network maps the condition c (5 features, zero-padded to 64) through three
+// ReLU layers of 256 to the flow parameters: for each of L spline layers
+// 3K+1 raw values (K = 10 or 12 bins) (K bin widths, K bin heights, K+1 knot slopes, constrained
+// as constrain_spline_params, :170-206), then shift, raw scale (scale =
+// 100 sigmoid(raw), :396-418) and the log expected hit count
+// (extended_cascade_model.jl:119-121).  The output width L(3K+1)+3 is padded
+// to a multiple of 64 with rows that stay zero.  The density of a time
+// residual y: x = g_0(g_1(... g_{L-1}(y))) with g_l the inverse spline of
+// layer l (inv_rqs_univariate, :334-389, linear outside [t_min, t_max]), and
+// log p(y) = log N(x; shift, scale) + the sum of the inverse log-determinants.
+// L = 1 is the reference's model.  Loss (log_likelihood_with_poisson,
+// extended_cascade_model.jl:132-139): per sample -(n log lambda - lambda -
+// lgamma(n + 1)) for its label's hit count n, plus -log p(y) when the sample
+// carries a time; the mean over the batch.  The reference's dropout is not
+// applied.
+//
+// The GEMMs of the network run on the tensor cores (flow_gemm.cu) with BF16
+// weights / activations and FP32 accumulation; master weights, Adam moments
+// and the spline head are FP32.  The head's gradient: the in-bin inverse
+// spline in forward-mode dual numbers over its 7 inputs (y, bin x0, width,
+// y0, height, two knot slopes), chained analytically through the softmax /
+// cumulative-sum / softplus parametrisation, and in reverse mode across the
+// spline layers and the base normal.
+#include <cuda_bf16.h>
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <random>
+#include <string>
+#include <type_traits>
+#include <vector>
+
+#include "ntp_internal.h"
+
+namespace ntp {
+
+namespace {
+
+constexpr int kCond = 5;
+constexpr int kIn = 64;        // padded input width (one K slice of the GEMM)
+constexpr int kMaxLayers = 5;
+constexpr float kMinBin = 1e-4f, kMinSlope = 1e-4f;
+constexpr float kLog2Pi = 1.8378770664093453f;
+constexpr float kSlopeOffset = 0.5411666523385311f;  // log(exp(1 - 1e-4) - 1), rq_spline_flow.jl:152
+
+// K bins per spline layer: 3K+1 raw parameters; per layer 3(K+1) knot values
+__host__ __device__ constexpr int n_outputs(int L, int K) { return L * (3 * K + 1) + 3; }
+__host__ __device__ constexpr int n_outputs_padded(int L, int K) { return (n_outputs(L, K) + 63) / 64 * 64; }
+__host__ __device__ constexpr int knot_row(int L, int K) { return L * 3 * (K + 1) + 3; }
+
+// ---------------------------------------------------------------- dual numbers
+template <int N>
+struct Dual {
+    float v;
+    float g[N];
+};
+template <int N>
+__device__ __forceinline__ Dual<N> dvar(float v, int i) {
+    Dual<N> r;
+    r.v = v;
+#pragma unroll
+    for (int j = 0; j < N; ++j) r.g[j] = (j == i) ? 1.0f : 0.0f;
+    return r;
+}
+template <int N>
+__device__ __forceinline__ Dual<N> dconst(float v) {
+    Dual<N> r;
+    r.v = v;
+#pragma unroll
+    for (int j = 0; j < N; ++j) r.g[j] = 0.0f;
+    return r;
+}
+template <int N>
+__device__ __forceinline__ Dual<N> operator+(const Dual<N>& a, const Dual<N>& b) {
+    Dual<N> r;
+    r.v = a.v + b.v;
+#pragma unroll
+    for (int j = 0; j < N; ++j) r.g[j] = a.g[j] + b.g[j];
+    return r;
+}
+template <int N>
+__device__ __forceinline__ Dual<N> operator-(const Dual<N>& a, const Dual<N>& b) {
+    Dual<N> r;
+    r.v = a.v - b.v;
+#pragma unroll
+    for (int j = 0; j < N; ++j) r.g[j] = a.g[j] - b.g[j];
+    return r;
+}
+template <int N>
+__device__ __forceinline__ Dual<N> operator*(const Dual<N>& a, const Dual<N>& b) {
+    Dual<N> r;
+    r.v = a.v * b.v;
+#pragma unroll
+    for (int j = 0; j < N; ++j) r.g[j] = a.g[j] * b.v + a.v * b.g[j];
+    return r;
+}
+template <int N>
+__device__ __forceinline__ Dual<N> operator/(const Dual<N>& a, const Dual<N>& b) {
+    Dual<N> r;
+    const float inv = 1.0f / b.v;
+    r.v = a.v * inv;
+#pragma unroll
+    for (int j = 0; j < N; ++j) r.g[j] = (a.g[j] - r.v * b.g[j]) * inv;
+    return r;
+}
+template <int N>
+__device__ __forceinline__ Dual<N> operator*(float s, const Dual<N>& a) {
+    Dual<N> r;
+    r.v = s * a.v;
+#pragma unroll
+    for (int j = 0; j < N; ++j) r.g[j] = s * a.g[j];
+    return r;
+}
+template <int N>
+__device__ __forceinline__ Dual<N> dlog(const Dual<N>& a) {
+    Dual<N> r;
+    r.v = logf(a.v);
+    const float inv = 1.0f / a.v;
+#pragma unroll
+    for (int j = 0; j < N; ++j) r.g[j] = a.g[j] * inv;
+    return r;
+}
+template <int N>
+__device__ __forceinline__ Dual<N> dsqrt(const Dual<N>& a) {
+    Dual<N> r;
+    r.v = sqrtf(a.v);
+    const float h = r.v > 0.0f ? 0.5f / r.v : 0.0f;
+#pragma unroll
+    for (int j = 0; j < N; ++j) r.g[j] = a.g[j] * h;
+    return r;
+}
+// clamp to [0, 1]: outside the interval the value is constant
+template <int N>
+__device__ __forceinline__ Dual<N> dclamp01(const Dual<N>& a) {
+    if (a.v < 0.0f) return dconst<N>(0.0f);
+    if (a.v > 1.0f) return dconst<N>(1.0f);
+    return a;
+}
+
+// ------------------------------------------------------------------- splines
+template <int K>
+struct Knots {
+    float xp[K + 1], yp[K + 1], d[K + 1];
+    float sw[K], sh[K];  // softmax of the raw widths / heights
+    float sig[K + 1];        // derivative of each slope by its raw value
+};
+
+__device__ __forceinline__ float softplus(float t) { return t > 20.0f ? t : log1pf(expf(t)); }
+
+// constrain_spline_params, rq_spline_flow.jl:170-206 (with _normalize_bin_sizes
+// :127-136 and _normalize_knot_slopes :146-154)
+template <int K>
+__device__ __forceinline__ void constrain(const float* __restrict__ p, float r0, float r1, Knots<K>& kn) {
+    const float span = (r1 - r0) - K * kMinBin;
+    float mw = p[0], mh = p[K];
+#pragma unroll
+    for (int i = 1; i < K; ++i) {
+        mw = fmaxf(mw, p[i]);
+        mh = fmaxf(mh, p[K + i]);
+    }
+    float zw = 0.0f, zh = 0.0f;
+#pragma unroll
+    for (int i = 0; i < K; ++i) {
+        kn.sw[i] = expf(p[i] - mw);
+        kn.sh[i] = expf(p[K + i] - mh);
+        zw += kn.sw[i];
+        zh += kn.sh[i];
+    }
+    const float izw = 1.0f / zw, izh = 1.0f / zh;
+    float cx = r0, cy = r0;
+    kn.xp[0] = r0;
+    kn.yp[0] = r0;
+#pragma unroll
+    for (int i = 0; i < K; ++i) {
+        kn.sw[i] *= izw;
+        kn.sh[i] *= izh;
+        cx += kMinBin + span * kn.sw[i];
+        cy += kMinBin + span * kn.sh[i];
+        kn.xp[i + 1] = cx;
+        kn.yp[i + 1] = cy;
+    }
+    kn.xp[K] = r1;
+    kn.yp[K] = r1;
+#pragma unroll
+    for (int i = 0; i <= K; ++i) {
+        const float t = p[2 * K + i] + kSlopeOffset;
+        kn.d[i] = softplus(t) + kMinSlope;
+        kn.sig[i] = 1.0f / (1.0f + expf(-t));
+    }
+}
+
+// the bin k with yp[k] <= y < yp[k+1] (y strictly inside the range)
+template <int K>
+__device__ __forceinline__ int find_bin(const float* yp, float y) {
+    int k = 0;
+#pragma unroll
+    for (int i = 1; i < K; ++i) k += (y >= yp[i]) ? 1 : 0;
+    return k;
+}
+
+// safe_quadratic_root, rq_spline_flow.jl:215-244
+__device__ __forceinline__ Dual<7> quad_root(const Dual<7>& a, const Dual<7>& b, const Dual<7>& c) {
+    const Dual<7> disc = b * b - 4.0f * (a * c);
+    const Dual<7> sq = disc.v > 0.0f ? dsqrt(disc) : dconst<7>(0.0f);
+    if (b.v >= 0.0f) return (2.0f * c) / (dconst<7>(0.0f) - b - sq);
+    return (dconst<7>(0.0f) - b + sq) / (2.0f * a);
+}
+
+// Inverse spline on one bin (inv_rqs_univariate, rq_spline_flow.jl:358-381)
+// with derivatives by u = (y, x0, w, y0, h, d0, d1).
+__device__ __forceinline__ void inv_bin_dual(float yv, float x0v, float wv, float y0v, float hv, float d0v, float d1v,
+                                             Dual<7>& x, Dual<7>& logdet) {
+    using D = Dual<7>;
+    const D y = dvar<7>(yv, 0), x0 = dvar<7>(x0v, 1), w = dvar<7>(wv, 2), y0 = dvar<7>(y0v, 3);
+    const D h = dvar<7>(hv, 4), d0 = dvar<7>(d0v, 5), d1 = dvar<7>(d1v, 6);
+    const D s = h / w;
+    const D ww = dclamp01((y - y0) / h);
+    const D st = d1 + d0 - 2.0f * s;
+    const D c = dconst<7>(0.0f) - s * ww;
+    const D b = d0 - st * ww;
+    const D a = s - b;
+    const D z = dclamp01(quad_root(a, b, c));
+    x = w * z + x0;
+    const D sq_z = z * z, z1mz = z - sq_z;
+    const D omz = dconst<7>(1.0f) - z;
+    const D den = s + st * z1mz;
+    logdet = dconst<7>(0.0f) - 2.0f * dlog(s) - dlog(d1 * sq_z + 2.0f * (s * z1mz) + d0 * (omz * omz)) +
+             2.0f * dlog(den);
+}
+
+__device__ __forceinline__ void inv_bin(float y, float x0, float w, float y0, float h, float d0, float d1, float& x,
+                                        float& logdet) {
+    const float s = h / w;
+    const float ww = fminf(fmaxf((y - y0) / h, 0.0f), 1.0f);
+    const float st = d1 + d0 - 2.0f * s;
+    const float c = -s * ww, b = d0 - st * ww, a = s - b;
+    const float disc = b * b - 4.0f * a * c;
+    const float sq = disc > 0.0f ? sqrtf(disc) : 0.0f;
+    float z = b >= 0.0f ? (2.0f * c) / (-b - sq) : (-b + sq) / (2.0f * a);
+    z = fminf(fmaxf(z, 0.0f), 1.0f);
+    x = w * z + x0;
+    const float z1mz = z - z * z, omz = 1.0f - z;
+    const float den = s + st * z1mz;
+    logdet = -2.0f * logf(s) - logf(d1 * z * z + 2.0f * s * z1mz + d0 * omz * omz) + 2.0f * logf(den);
+}
+
+// inv_rqs_univariate on constrained knots: x and the log-determinant
+template <int K>
+__device__ __forceinline__ void inv_spline(const float* xp, const float* yp, const float* d, float y, float& x,
+                                           float& logdet) {
+    if (y <= yp[0]) {
+        x = (y - yp[0]) / d[0] + xp[0];
+        logdet = -logf(d[0]);
+    } else if (y >= yp[K]) {
+        x = (y - yp[K]) / d[K] + xp[K];
+        logdet = -logf(d[K]);
+    } else {
+        const int k = find_bin<K>(yp, y);
+        inv_bin(y, xp[k], xp[k + 1] - xp[k], yp[k], yp[k + 1] - yp[k], d[k], d[k + 1], x, logdet);
+    }
+}
+
+// Adjoint of one inverse spline layer: given a_x = dL/dx and a_l = dL/dlogdet
+// at input y, adds the gradient by the layer's raw parameters into g[0..(3 * K + 1))
+// and returns dL/dy.
+template <int K>
+__device__ __forceinline__ float inv_layer_grad(const float* __restrict__ p, float r0, float r1, float y, float a_x,
+                                                float a_l, float* __restrict__ g) {
+    Knots<K> kn;
+    constrain<K>(p, r0, r1, kn);
+    if (y <= kn.yp[0] || y >= kn.yp[K]) {
+        // linear tails: x = (y - y_e)/d_e + x_e, logdet = -log d_e (x_e = y_e = a range end, fixed)
+        const int e = y <= kn.yp[0] ? 0 : K;
+        const float d = kn.d[e];
+        const float gd = a_x * (-(y - kn.yp[e]) / (d * d)) - a_l / d;
+        g[2 * K + e] += gd * kn.sig[e];
+        return a_x / d;
+    }
+    const int k = find_bin<K>(kn.yp, y);
+    Dual<7> x, ld;
+    inv_bin_dual(y, kn.xp[k], kn.xp[k + 1] - kn.xp[k], kn.yp[k], kn.yp[k + 1] - kn.yp[k], kn.d[k], kn.d[k + 1], x, ld);
+    float gu[7];
+#pragma unroll
+    for (int j = 0; j < 7; ++j) gu[j] = a_x * x.g[j] + a_l * ld.g[j];
+    // x0 = r0 + sum_{i<k} wd_i, w = wd_k with wd = kMinBin + span * softmax(raw);
+    // (the last knot is pinned to r1, which equals the cumulative sum exactly)
+    const float span = (r1 - r0) - K * kMinBin;
+    float dot_w = 0.0f, dot_h = 0.0f;
+#pragma unroll
+    for (int i = 0; i < K; ++i) {
+        const float gwd = i < k ? gu[1] : (i == k ? gu[2] : 0.0f);
+        const float ghd = i < k ? gu[3] : (i == k ? gu[4] : 0.0f);
+        dot_w += kn.sw[i] * gwd;
+        dot_h += kn.sh[i] * ghd;
+    }
+#pragma unroll
+    for (int j = 0; j < K; ++j) {
+        const float gwd = j < k ? gu[1] : (j == k ? gu[2] : 0.0f);
+        const float ghd = j < k ? gu[3] : (j == k ? gu[4] : 0.0f);
+        g[j] += span * kn.sw[j] * (gwd - dot_w);
+        g[K + j] += span * kn.sh[j] * (ghd - dot_h);
+    }
+#pragma unroll
+    for (int j = 0; j <= K; ++j) {
+        const float gd = (j == k ? gu[5] : 0.0f) + (j == k + 1 ? gu[6] : 0.0f);
+        g[2 * K + j] += gd * kn.sig[j];
+    }
+    return gu[0];
+}
+
+__device__ __forceinline__ float warp_sum(float x) {
+#pragma unroll
+    for (int off = 16; off > 0; off >>= 1) x += __shfl_xor_sync(0xffffffffu, x, off);
+    return x;
+}
+
+// ------------------------------------------------------------------- kernels
+// cond [n x 5] FP32 -> X [n x 64] BF16 (zero padded) and X^T [64 x n];
+// rows >= n_valid are zero
+__global__ void pack_kernel(const float* __restrict__ cond, int n_valid, int n, __nv_bfloat16* __restrict__ x,
+                            __nv_bfloat16* __restrict__ xt) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n * kIn) return;
+    const int b = i / kIn, j = i % kIn;
+    const __nv_bfloat16 v = __float2bfloat16(j < kCond && b < n_valid ? cond[b * kCond + j] : 0.0f);
+    x[i] = v;
+    xt[static_cast<size_t>(j) * n + b] = v;
+}
+
+// Loss and gradient of the head, one thread per sample.  P [B x ldp] FP32.
+// Writes dL/dP as BF16 row-major dp [B x ldp] and transposed dpt [ldp x B]
+// (zero in the padding columns), optionally FP32 row-major gf, adds the bias
+// gradient of the output layer into gbias and the batch-mean loss into *loss.
+template <int K>
+__global__ void __launch_bounds__(128) head_grad_kernel(const float* __restrict__ P, int ldp, int L,
+                                                        const float* __restrict__ y, const float* __restrict__ nhits,
+                                                        const int* __restrict__ has_y, int B, float r0, float r1,
+                                                        __nv_bfloat16* __restrict__ dp,
+                                                        __nv_bfloat16* __restrict__ dpt, float* __restrict__ gf,
+                                                        float* __restrict__ gbias, double* __restrict__ loss) {
+    const int b = blockIdx.x * blockDim.x + threadIdx.x;
+    const bool act = b < B;
+    const int bb = act ? b : 0;
+    const float* p = P + static_cast<size_t>(bb) * ldp;
+    const int o_shift = L * (3 * K + 1), o_scale = o_shift + 1, o_le = o_shift + 2;
+    const float inv_b = 1.0f / static_cast<float>(B);
+    auto emit = [&](int col, float v) {
+        if (act) {
+            dp[static_cast<size_t>(b) * ldp + col] = __float2bfloat16(v);
+            dpt[static_cast<size_t>(col) * B + b] = __float2bfloat16(v);
+            if (gf) gf[static_cast<size_t>(b) * ldp + col] = v;
+        }
+        if (gbias) {
+            const float s = warp_sum(act ? v : 0.0f);
+            if ((threadIdx.x & 31) == 0 && s != 0.0f) atomicAdd(gbias + col, s);
+        }
+    };
+
+    float l = 0.0f;
+    // count head: -(n log lambda - lambda - lgamma(n + 1))
+    const float le = p[o_le], n = act ? nhits[bb] : 0.0f;
+    const float lam = expf(fminf(le, 80.0f));
+    const bool timed = act && has_y[bb];
+    if (act) l -= n * le - lam - lgammaf(n + 1.0f);
+    float g_le = act ? (lam - n) * inv_b : 0.0f;
+
+    float ys[kMaxLayers];
+    float a = 0.0f, g_shift = 0.0f, g_scale = 0.0f;
+    if (timed) {
+        float cur = y[bb], ldsum = 0.0f;
+        for (int li = L - 1; li >= 0; --li) {  // outermost layer first
+            ys[li] = cur;
+            Knots<K> kn;
+            constrain<K>(p + li * (3 * K + 1), r0, r1, kn);
+            float x, ld;
+            inv_spline<K>(kn.xp, kn.yp, kn.d, cur, x, ld);
+            cur = x;
+            ldsum += ld;
+        }
+        const float sg = 1.0f / (1.0f + expf(-p[o_scale]));
+        const float scale = 100.0f * sg;
+        const float u = (cur - p[o_shift]) / scale;
+        l -= -logf(scale) - 0.5f * (kLog2Pi + u * u) + ldsum;
+        a = u / scale * inv_b;  // dL/dx of the innermost output
+        g_shift = -u / scale * inv_b;
+        g_scale = (1.0f - u * u) / scale * 100.0f * sg * (1.0f - sg) * inv_b;
+    }
+    for (int li = 0; li < L; ++li) {
+        float g[(3 * K + 1)];
+#pragma unroll
+        for (int i = 0; i < (3 * K + 1); ++i) g[i] = 0.0f;
+        if (timed) a = inv_layer_grad<K>(p + li * (3 * K + 1), r0, r1, ys[li], a, -inv_b, g);
+#pragma unroll 1
+        for (int i = 0; i < (3 * K + 1); ++i) emit(li * (3 * K + 1) + i, g[i]);
+    }
+    emit(o_shift, g_shift);
+    emit(o_scale, g_scale);
+    emit(o_le, g_le);
+    if (act)
+        for (int col = o_le + 1; col < ldp; ++col) {
+            dp[static_cast<size_t>(b) * ldp + col] = __float2bfloat16(0.0f);
+            dpt[static_cast<size_t>(col) * B + b] = __float2bfloat16(0.0f);
+            if (gf) gf[static_cast<size_t>(b) * ldp + col] = 0.0f;
+        }
+    l = warp_sum(l);
+    if ((threadIdx.x & 31) == 0 && l != 0.0f) atomicAdd(loss, static_cast<double>(l) / B);
+}
+
+// Adam on an FP32 parameter block (Flux's Adam: bias-corrected moments);
+// refreshes the BF16 copy and, when wt != nullptr, the BF16 transpose
+// [cols x rows].
+__global__ void adam_kernel(float* __restrict__ w, float* __restrict__ m, float* __restrict__ v,
+                            const float* __restrict__ g, int n, int cols, int rows, float lr, float b1, float b2,
+                            float eps, float c1, float c2, __nv_bfloat16* __restrict__ wb,
+                            __nv_bfloat16* __restrict__ wt) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const float gi = g[i];
+    const float mi = b1 * m[i] + (1.0f - b1) * gi;
+    const float vi = b2 * v[i] + (1.0f - b2) * gi * gi;
+    m[i] = mi;
+    v[i] = vi;
+    const float wi = w[i] - lr * (mi / c1) / (sqrtf(vi / c2) + eps);
+    w[i] = wi;
+    if (wb) wb[i] = __float2bfloat16(wi);
+    if (wt) wt[static_cast<size_t>(i % cols) * rows + i / cols] = __float2bfloat16(wi);
+}
+
+__global__ void to_bf16_kernel(const float* __restrict__ w, int n, int cols, int rows,
+                               __nv_bfloat16* __restrict__ wb, __nv_bfloat16* __restrict__ wt) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    wb[i] = __float2bfloat16(w[i]);
+    wt[static_cast<size_t>(i % cols) * rows + i / cols] = __float2bfloat16(w[i]);
+}
+
+// Per condition: the constrained knots of every layer, then shift, scale and
+// log expectation.  Row of knot_row(L, K) floats.
+template <int K>
+__global__ void knots_kernel(const float* __restrict__ P, int ldp, int L, int n, float r0, float r1,
+                             float* __restrict__ out) {
+    const int c = blockIdx.x * blockDim.x + threadIdx.x;
+    if (c >= n) return;
+    const float* p = P + static_cast<size_t>(c) * ldp;
+    float* o = out + static_cast<size_t>(c) * knot_row(L, K);
+    for (int li = 0; li < L; ++li) {
+        Knots<K> kn;
+        constrain<K>(p + li * (3 * K + 1), r0, r1, kn);
+        float* q = o + li * (3 * (K + 1));
+        for (int i = 0; i <= K; ++i) {
+            q[i] = kn.xp[i];
+            q[K + 1 + i] = kn.yp[i];
+            q[2 * (K + 1) + i] = kn.d[i];
+        }
+    }
+    o[L * (3 * (K + 1))] = p[L * (3 * K + 1)];
+    o[L * (3 * (K + 1)) + 1] = 100.0f / (1.0f + expf(-p[L * (3 * K + 1) + 1]));
+    o[L * (3 * (K + 1)) + 2] = p[L * (3 * K + 1) + 2];
+}
+
+// log p(t | condition) for (condition index, time) tuples
+template <int K>
+__global__ void logpdf_kernel(const float* __restrict__ knots, int L, int n_cond, const int* __restrict__ cidx,
+                              const float* __restrict__ t, unsigned long long n, float* __restrict__ out) {
+    const int row = knot_row(L, K);
+    for (unsigned long long i = blockIdx.x * static_cast<unsigned long long>(blockDim.x) + threadIdx.x; i < n;
+         i += static_cast<unsigned long long>(gridDim.x) * blockDim.x) {
+        const int c = __ldg(cidx + i);
+        if (c < 0 || c >= n_cond) {
+            out[i] = __int_as_float(0x7fc00000);  // NaN for an index outside the conditions
+            continue;
+        }
+        const float* o = knots + static_cast<size_t>(c) * row;
+        float cur = __ldg(t + i), ldsum = 0.0f;
+        for (int li = L - 1; li >= 0; --li) {
+            const float* xp = o + li * (3 * (K + 1));
+            float x, ld;
+            inv_spline<K>(xp, xp + K + 1, xp + 2 * (K + 1), cur, x, ld);
+            cur = x;
+            ldsum += ld;
+        }
+        const float scale = o[L * (3 * (K + 1)) + 1];
+        const float u = (cur - o[L * (3 * (K + 1))]) / scale;
+        out[i] = -logf(scale) - 0.5f * (kLog2Pi + u * u) + ldsum;
+    }
+}
+
+int blocks_for(long long n, int t = 256) { return static_cast<int>((n + t - 1) / t); }
+
+}  // namespace
+}  // namespace ntp
+
+// ======================================================================= host
+namespace {
+
+using bf16 = __nv_bfloat16;
+
+struct Block {  // one parameter block of the flat FP32 vector
+    int rows, cols;
+    size_t off;
+};
+
+}  // namespace
+
+struct ntp_flow {
+    int device = 0;
+    cudaStream_t stream = nullptr;
+    int cap = 0;  // batch capacity (multiple of 128)
+    int L = 1, K = 12, n_out = 0, n_pad = 0;
+    float r0 = -20.0f, r1 = 1500.0f;
+    float lr = 1e-3f, b1 = 0.9f, b2 = 0.999f, eps = 1e-8f;
+    long long step = 0;
+    std::string err;
+    Block blk[8];  // W1 b1 W2 b2 W3 b3 W4 b4
+    size_t n_params = 0;
+    float *theta = nullptr, *m = nullptr, *v = nullptr, *grad = nullptr;
+    bf16 *wb[4] = {}, *wt[4] = {};
+    // activations of one batch
+    bf16 *x = nullptr, *xt = nullptr, *h[3] = {}, *ht[3] = {}, *dz[3] = {}, *dzt[3] = {};
+    bf16 *dp = nullptr, *dpt = nullptr;
+    float* P = nullptr;
+    float *cond = nullptr, *y = nullptr, *nh = nullptr;
+    int* hy = nullptr;
+    double* loss = nullptr;
+    int* gemm_err = nullptr;
+    // inference
+    float* knots = nullptr;
+    size_t knots_cap = 0;
+};
+
+namespace {
+
+constexpr int kHid = 256, kIn = 64, kCond = 5;
+
+ntp_status ferr(ntp_flow* f, cudaError_t e, const char* what) {
+    f->err = std::string(what) + ": " + cudaGetErrorString(e);
+    return e == cudaErrorInvalidValue ? NTP_ERR_INVALID : (e == cudaErrorMemoryAllocation ? NTP_ERR_NOMEM : NTP_ERR_CUDA);
+}
+
+#define F_CUDA(f, call)                                     \
+    do {                                                    \
+        cudaError_t e_ = (call);                            \
+        if (e_ != cudaSuccess) return ferr((f), e_, #call); \
+    } while (0)
+
+#define F_OK(expr)                          \
+    do {                                    \
+        const ntp_status s_ = (expr);       \
+        if (s_ != NTP_OK) return s_;        \
+    } while (0)
+
+// calls fn with the bin count as a compile-time constant (10 or 12)
+template <typename Fn>
+void with_bins(int K, Fn&& fn) {
+    if (K == 10) fn(std::integral_constant<int, 10>{});
+    else fn(std::integral_constant<int, 12>{});
+}
+
+template <typename T>
+cudaError_t dalloc(T** p, size_t n) {
+    return cudaMalloc(reinterpret_cast<void**>(p), sizeof(T) * (n ? n : 1));
+}
+
+ntp_status gemm(ntp_flow* f, const bf16* A, int lda, const bf16* B, int ldb, int M, int N, int K,
+                const ntp::GemmEpilogue& ep, int splits = 1) {
+    F_CUDA(f, ntp::gemm_bf16_ep(A, lda, B, ldb, M, N, K, ep, splits, f->gemm_err, f->stream));
+    return NTP_OK;
+}
+
+// P = conditioner(X) for n rows (X packed, n a multiple of 128); for
+// training also the transposed activations the weight gradients read
+ntp_status forward(ntp_flow* f, int n, bool keep_transposed) {
+    ntp::GemmEpilogue e{};
+    e.out_kind = 1;
+    e.relu = 1;
+    e.ldc = kHid;
+    e.ldct = n;
+    const bf16* in = f->x;
+    int k_in = kIn;
+    for (int l = 0; l < 3; ++l) {
+        e.c = f->h[l];
+        e.ct = keep_transposed ? f->ht[l] : nullptr;
+        e.bias = f->theta + f->blk[2 * l + 1].off;
+        F_OK(gemm(f, in, k_in, f->wb[l], k_in, n, kHid, k_in, e));
+        in = f->h[l];
+        k_in = kHid;
+    }
+    ntp::GemmEpilogue o{};
+    o.c = f->P;
+    o.ldc = f->n_pad;
+    o.out_kind = 0;
+    o.bias = f->theta + f->blk[7].off;
+    return gemm(f, f->h[2], kHid, f->wb[3], kHid, n, f->n_pad, kHid, o);
+}
+
+// conditions (host or device, n_valid rows) -> packed X with n rows
+ntp_status pack(ntp_flow* f, const float* cond, int n_valid, int n, int on_device) {
+    const float* dc = cond;
+    if (!on_device) {
+        F_CUDA(f, cudaMemcpyAsync(f->cond, cond, sizeof(float) * kCond * n_valid, cudaMemcpyHostToDevice, f->stream));
+        dc = f->cond;
+    }
+    ntp::pack_kernel<<<ntp::blocks_for(static_cast<long long>(n) * kIn), 256, 0, f->stream>>>(dc, n_valid, n, f->x,
+                                                                                               f->xt);
+    F_CUDA(f, cudaGetLastError());
+    return NTP_OK;
+}
+
+ntp_status check_gemm(ntp_flow* f) {
+    int herr = 0;
+    F_CUDA(f, cudaMemcpyAsync(&herr, f->gemm_err, sizeof(int), cudaMemcpyDeviceToHost, f->stream));
+    F_CUDA(f, cudaStreamSynchronize(f->stream));
+    if (herr) {
+        f->err = "tensor-core pipeline wait timed out";
+        return NTP_ERR_TIMEOUT;
+    }
+    return NTP_OK;
+}
+
+void free_all(ntp_flow* f) {
+    void* ps[] = {f->theta, f->m, f->v, f->grad, f->x, f->xt, f->dp, f->dpt, f->P, f->cond, f->y, f->nh, f->hy,
+                  f->loss, f->gemm_err, f->knots};
+    for (void* p : ps)
+        if (p) cudaFree(p);
+    for (int l = 0; l < 4; ++l) {
+        if (f->wb[l]) cudaFree(f->wb[l]);
+        if (f->wt[l]) cudaFree(f->wt[l]);
+    }
+    for (int l = 0; l < 3; ++l) {
+        if (f->h[l]) cudaFree(f->h[l]);
+        if (f->ht[l]) cudaFree(f->ht[l]);
+        if (f->dz[l]) cudaFree(f->dz[l]);
+        if (f->dzt[l]) cudaFree(f->dzt[l]);
+    }
+}
+
+}  // namespace
+
+extern "C" {
+
+ntp_status ntp_flow_create(int32_t device, const ntp_flow_config* cfg, ntp_flow** out) {
+    if (!cfg || !out) return NTP_ERR_INVALID;
+    *out = nullptr;
+    if (cfg->batch_capacity < 128 || cfg->batch_capacity % 128 || cfg->n_layers < 1 ||
+        (cfg->n_bins != 10 && cfg->n_bins != 12) ||
+        cfg->n_layers > ntp::kMaxLayers || !(cfg->t_max > cfg->t_min) || !(cfg->lr > 0.0f) ||
+        !(cfg->beta1 >= 0.0f && cfg->beta1 < 1.0f) || !(cfg->beta2 >= 0.0f && cfg->beta2 < 1.0f) ||
+        !(cfg->eps > 0.0f))
+        return NTP_ERR_INVALID;
+    ntp_flow* f = new ntp_flow();
+    f->device = device;
+    f->cap = cfg->batch_capacity;
+    f->L = cfg->n_layers;
+    f->K = cfg->n_bins;
+    f->n_out = ntp::n_outputs(f->L, f->K);
+    f->n_pad = ntp::n_outputs_padded(f->L, f->K);
+    f->r0 = cfg->t_min;
+    f->r1 = cfg->t_max;
+    f->lr = cfg->lr;
+    f->b1 = cfg->beta1;
+    f->b2 = cfg->beta2;
+    f->eps = cfg->eps;
+    const int dims[4][2] = {{kHid, kIn}, {kHid, kHid}, {kHid, kHid}, {f->n_pad, kHid}};
+    size_t off = 0;
+    for (int l = 0; l < 4; ++l) {
+        f->blk[2 * l] = Block{dims[l][0], dims[l][1], off};
+        off += static_cast<size_t>(dims[l][0]) * dims[l][1];
+        f->blk[2 * l + 1] = Block{1, dims[l][0], off};
+        off += dims[l][0];
+    }
+    f->n_params = off;
+    auto fail = [&](cudaError_t e) {
+        if (f->stream) cudaStreamDestroy(f->stream);
+        free_all(f);
+        delete f;
+        return e == cudaErrorMemoryAllocation ? NTP_ERR_NOMEM : NTP_ERR_CUDA;
+    };
+    cudaError_t e;
+    if ((e = cudaSetDevice(device)) != cudaSuccess) return fail(e);
+    if ((e = cudaStreamCreateWithFlags(&f->stream, cudaStreamNonBlocking)) != cudaSuccess) return fail(e);
+    const size_t B = f->cap;
+    if ((e = dalloc(&f->theta, off)) || (e = dalloc(&f->m, off)) || (e = dalloc(&f->v, off)) ||
+        (e = dalloc(&f->grad, off)))
+        return fail(e);
+    for (int l = 0; l < 4; ++l) {
+        const size_t n = static_cast<size_t>(dims[l][0]) * dims[l][1];
+        if ((e = dalloc(&f->wb[l], n)) || (e = dalloc(&f->wt[l], n))) return fail(e);
+    }
+    if ((e = dalloc(&f->x, B * kIn)) || (e = dalloc(&f->xt, B * kIn))) return fail(e);
+    for (int l = 0; l < 3; ++l)
+        if ((e = dalloc(&f->h[l], B * kHid)) || (e = dalloc(&f->ht[l], B * kHid)) ||
+            (e = dalloc(&f->dz[l], B * kHid)) || (e = dalloc(&f->dzt[l], B * kHid)))
+            return fail(e);
+    const size_t np = static_cast<size_t>(f->n_pad);
+    if ((e = dalloc(&f->dp, B * np)) || (e = dalloc(&f->dpt, B * np)) || (e = dalloc(&f->P, B * np)) ||
+        (e = dalloc(&f->cond, B * kCond)) || (e = dalloc(&f->y, B)) || (e = dalloc(&f->nh, B)) ||
+        (e = dalloc(&f->hy, B)) || (e = dalloc(&f->loss, 1)) || (e = dalloc(&f->gemm_err, 1)))
+        return fail(e);
+    // He-uniform weights (seeded); zero biases, zero padding input columns of
+    // W1 and zero padding rows of W4; the output layer scaled by 0.1
+    std::vector<float> th(off, 0.0f);
+    std::mt19937_64 rng(cfg->seed);
+    for (int l = 0; l < 4; ++l) {
+        const Block& b = f->blk[2 * l];
+        const int fan_in = l == 0 ? kCond : b.cols;
+        const float lim = std::sqrt(6.0f / fan_in) * (l == 3 ? 0.1f : 1.0f);
+        std::uniform_real_distribution<float> u(-lim, lim);
+        for (int r = 0; r < b.rows; ++r)
+            for (int c = 0; c < b.cols; ++c) {
+                const bool pad = (l == 0 && c >= kCond) || (l == 3 && r >= f->n_out);
+                const float val = u(rng);
+                th[b.off + static_cast<size_t>(r) * b.cols + c] = pad ? 0.0f : val;
+            }
+    }
+    const ntp_status s = ntp_flow_set_params(f, th.data(), off);
+    if (s != NTP_OK) {
+        ntp_flow_destroy(f);
+        return s;
+    }
+    *out = f;
+    return NTP_OK;
+}
+
+void ntp_flow_destroy(ntp_flow* f) {
+    if (!f) return;
+    cudaSetDevice(f->device);
+    if (f->stream) cudaStreamSynchronize(f->stream);
+    free_all(f);
+    if (f->stream) cudaStreamDestroy(f->stream);
+    delete f;
+}
+
+const char* ntp_flow_last_error(const ntp_flow* f) { return f ? f->err.c_str() : "null flow"; }
+
+ntp_status ntp_flow_get_layout(const ntp_flow* f, uint64_t* n_params, int32_t* n_outputs, int32_t* n_outputs_padded) {
+    if (!f) return NTP_ERR_INVALID;
+    if (n_params) *n_params = f->n_params;
+    if (n_outputs) *n_outputs = f->n_out;
+    if (n_outputs_padded) *n_outputs_padded = f->n_pad;
+    return NTP_OK;
+}
+
+ntp_status ntp_flow_set_params(ntp_flow* f, const float* host, uint64_t n) {
+    if (!f || !host || n != f->n_params) return NTP_ERR_INVALID;
+    F_CUDA(f, cudaSetDevice(f->device));
+    F_CUDA(f, cudaMemcpyAsync(f->theta, host, sizeof(float) * n, cudaMemcpyHostToDevice, f->stream));
+    for (int l = 0; l < 4; ++l) {
+        const Block& b = f->blk[2 * l];
+        const int cnt = b.rows * b.cols;
+        ntp::to_bf16_kernel<<<ntp::blocks_for(cnt), 256, 0, f->stream>>>(f->theta + b.off, cnt, b.cols, b.rows,
+                                                                         f->wb[l], f->wt[l]);
+        F_CUDA(f, cudaGetLastError());
+    }
+    F_CUDA(f, cudaMemsetAsync(f->m, 0, sizeof(float) * n, f->stream));
+    F_CUDA(f, cudaMemsetAsync(f->v, 0, sizeof(float) * n, f->stream));
+    F_CUDA(f, cudaMemsetAsync(f->grad, 0, sizeof(float) * n, f->stream));
+    F_CUDA(f, cudaStreamSynchronize(f->stream));
+    f->step = 0;
+    return NTP_OK;
+}
+
+ntp_status ntp_flow_get_params(ntp_flow* f, float* host, uint64_t n, int32_t which) {
+    if (!f || !host || n != f->n_params || which < 0 || which > 3) return NTP_ERR_INVALID;
+    const float* src = which == 0 ? f->theta : which == 1 ? f->grad : which == 2 ? f->m : f->v;
+    F_CUDA(f, cudaSetDevice(f->device));
+    F_CUDA(f, cudaMemcpyAsync(host, src, sizeof(float) * n, cudaMemcpyDeviceToHost, f->stream));
+    F_CUDA(f, cudaStreamSynchronize(f->stream));
+    return NTP_OK;
+}
+
+ntp_status ntp_flow_train_step(ntp_flow* f, const float* cond, const float* tres, const float* nhits,
+                               const int32_t* has_time, int32_t B, int32_t on_device, int32_t update,
+                               double* loss_out) {
+    if (!f || !cond || !tres || !nhits || !has_time) return NTP_ERR_INVALID;
+    if (B < 128 || B > f->cap || B % 128) {
+        f->err = "ntp_flow_train_step: the batch must be a multiple of 128 up to the capacity";
+        return NTP_ERR_INVALID;
+    }
+    F_CUDA(f, cudaSetDevice(f->device));
+    cudaStream_t st = f->stream;
+    const float* dy = tres;
+    const float* dn = nhits;
+    const int* dh = has_time;
+    if (!on_device) {
+        F_CUDA(f, cudaMemcpyAsync(f->y, tres, sizeof(float) * B, cudaMemcpyHostToDevice, st));
+        F_CUDA(f, cudaMemcpyAsync(f->nh, nhits, sizeof(float) * B, cudaMemcpyHostToDevice, st));
+        F_CUDA(f, cudaMemcpyAsync(f->hy, has_time, sizeof(int) * B, cudaMemcpyHostToDevice, st));
+        dy = f->y;
+        dn = f->nh;
+        dh = f->hy;
+    }
+    F_CUDA(f, cudaMemsetAsync(f->gemm_err, 0, sizeof(int), st));
+    F_OK(pack(f, cond, B, B, on_device));
+    F_OK(forward(f, B, true));
+    F_CUDA(f, cudaMemsetAsync(f->loss, 0, sizeof(double), st));
+    F_CUDA(f, cudaMemsetAsync(f->grad, 0, sizeof(float) * f->n_params, st));
+    float* g = f->grad;
+    auto gw = [&](int l) { return g + f->blk[2 * l].off; };
+    auto gb = [&](int l) { return g + f->blk[2 * l + 1].off; };
+    with_bins(f->K, [&](auto kc) {
+        ntp::head_grad_kernel<decltype(kc)::value><<<ntp::blocks_for(B, 128), 128, 0, st>>>(
+            f->P, f->n_pad, f->L, dy, dn, dh, B, f->r0, f->r1, f->dp, f->dpt, nullptr, gb(3), f->loss);
+    });
+    F_CUDA(f, cudaGetLastError());
+    const int splits = std::max(1, B / 512);
+    // output layer: dW4 = dP^T H3
+    ntp::GemmEpilogue ew{};
+    ew.out_kind = 2;
+    ew.ldc = kHid;
+    ew.c = gw(3);
+    F_OK(gemm(f, f->dpt, B, f->ht[2], B, f->n_pad, kHid, B, ew, splits));
+    const bf16* dnext = f->dp;
+    int k_next = f->n_pad;
+    for (int l = 2; l >= 0; --l) {
+        // dZ_l = (dZ_{l+1} W_{l+1}) masked by H_l > 0, its transpose, and its
+        // column sums (the bias gradient of layer l)
+        ntp::GemmEpilogue ed{};
+        ed.c = f->dz[l];
+        ed.ldc = kHid;
+        ed.out_kind = 1;
+        ed.ct = f->dzt[l];
+        ed.ldct = B;
+        ed.mask = f->h[l];
+        ed.ldm = kHid;
+        ed.colsum = gb(l);
+        F_OK(gemm(f, dnext, k_next, f->wt[l + 1], k_next, B, kHid, k_next, ed));
+        // dW_l = dZ_l^T X_l with X_l = H_{l-1} or the packed input
+        ntp::GemmEpilogue eg{};
+        eg.out_kind = 2;
+        eg.c = gw(l);
+        eg.ldc = l == 0 ? kIn : kHid;
+        const bf16* xt = l == 0 ? f->xt : f->ht[l - 1];
+        F_OK(gemm(f, f->dzt[l], B, xt, B, kHid, l == 0 ? kIn : kHid, B, eg, splits));
+        dnext = f->dz[l];
+        k_next = kHid;
+    }
+    if (update) {
+        ++f->step;
+        const float c1 = 1.0f - std::pow(f->b1, static_cast<float>(f->step));
+        const float c2 = 1.0f - std::pow(f->b2, static_cast<float>(f->step));
+        for (int i = 0; i < 8; ++i) {
+            const Block& b = f->blk[i];
+            const int cnt = b.rows * b.cols;
+            const bool w = (i % 2) == 0;
+            ntp::adam_kernel<<<ntp::blocks_for(cnt), 256, 0, st>>>(
+                f->theta + b.off, f->m + b.off, f->v + b.off, g + b.off, cnt, b.cols, b.rows, f->lr, f->b1, f->b2,
+                f->eps, c1, c2, w ? f->wb[i / 2] : nullptr, w ? f->wt[i / 2] : nullptr);
+            F_CUDA(f, cudaGetLastError());
+        }
+    }
+    double hl = 0.0;
+    F_CUDA(f, cudaMemcpyAsync(&hl, f->loss, sizeof(double), cudaMemcpyDeviceToHost, st));
+    F_OK(check_gemm(f));
+    if (loss_out) *loss_out = hl;
+    return NTP_OK;
+}
+
+ntp_status ntp_flow_forward(ntp_flow* f, const float* cond, int32_t n, float* params_out) {
+    if (!f || !cond || !params_out || n <= 0) return NTP_ERR_INVALID;
+    F_CUDA(f, cudaSetDevice(f->device));
+    cudaStream_t st = f->stream;
+    F_CUDA(f, cudaMemsetAsync(f->gemm_err, 0, sizeof(int), st));
+    for (int c0 = 0; c0 < n; c0 += f->cap) {
+        const int m = std::min(f->cap, n - c0);
+        const int mp = (m + 127) / 128 * 128;
+        F_OK(pack(f, cond + static_cast<size_t>(c0) * kCond, m, mp, 0));
+        F_OK(forward(f, mp, false));
+        F_CUDA(f, cudaMemcpy2DAsync(params_out + static_cast<size_t>(c0) * f->n_out, sizeof(float) * f->n_out, f->P,
+                                    sizeof(float) * f->n_pad, sizeof(float) * f->n_out, m, cudaMemcpyDeviceToHost,
+                                    st));
+    }
+    return check_gemm(f);
+}
+
+ntp_status ntp_flow_head(ntp_flow* f, const float* params, const float* tres, const float* nhits,
+                         const int32_t* has_time, int32_t B, double* loss_out, float* grad_out) {
+    if (!f || !params || !tres || !nhits || !has_time || B <= 0 || B > f->cap) return NTP_ERR_INVALID;
+    F_CUDA(f, cudaSetDevice(f->device));
+    cudaStream_t st = f->stream;
+    float* gf = nullptr;
+    F_CUDA(f, dalloc(&gf, static_cast<size_t>(B) * f->n_pad));
+    auto run = [&]() -> ntp_status {
+        F_CUDA(f, cudaMemcpy2DAsync(f->P, sizeof(float) * f->n_pad, params, sizeof(float) * f->n_out,
+                                    sizeof(float) * f->n_out, B, cudaMemcpyHostToDevice, st));
+        F_CUDA(f, cudaMemcpyAsync(f->y, tres, sizeof(float) * B, cudaMemcpyHostToDevice, st));
+        F_CUDA(f, cudaMemcpyAsync(f->nh, nhits, sizeof(float) * B, cudaMemcpyHostToDevice, st));
+        F_CUDA(f, cudaMemcpyAsync(f->hy, has_time, sizeof(int) * B, cudaMemcpyHostToDevice, st));
+        F_CUDA(f, cudaMemsetAsync(f->loss, 0, sizeof(double), st));
+        with_bins(f->K, [&](auto kc) {
+            ntp::head_grad_kernel<decltype(kc)::value><<<ntp::blocks_for(B, 128), 128, 0, st>>>(
+                f->P, f->n_pad, f->L, f->y, f->nh, f->hy, B, f->r0, f->r1, f->dp, f->dpt, gf, nullptr, f->loss);
+        });
+        F_CUDA(f, cudaGetLastError());
+        double hl = 0.0;
+        F_CUDA(f, cudaMemcpyAsync(&hl, f->loss, sizeof(double), cudaMemcpyDeviceToHost, st));
+        if (grad_out)
+            F_CUDA(f, cudaMemcpy2DAsync(grad_out, sizeof(float) * f->n_out, gf, sizeof(float) * f->n_pad,
+                                        sizeof(float) * f->n_out, B, cudaMemcpyDeviceToHost, st));
+        F_CUDA(f, cudaStreamSynchronize(st));
+        if (loss_out) *loss_out = hl;
+        return NTP_OK;
+    };
+    const ntp_status s = run();
+    cudaFree(gf);
+    return s;
+}
+
+ntp_status ntp_flow_evaluate(ntp_flow* f, const float* cond, int32_t n_cond, const int32_t* cond_index,
+                             const float* times, uint64_t n_tuples, float* logpdf, float* log_expec,
+                             int32_t on_device) {
+    if (!f || !cond || n_cond <= 0) return NTP_ERR_INVALID;
+    if (n_tuples > 0 && (!cond_index || !times || !logpdf)) return NTP_ERR_INVALID;
+    F_CUDA(f, cudaSetDevice(f->device));
+    cudaStream_t st = f->stream;
+    const int row = ntp::knot_row(f->L, f->K);
+    const size_t need = static_cast<size_t>(n_cond) * row;
+    if (need > f->knots_cap) {
+        if (f->knots) cudaFree(f->knots);
+        f->knots = nullptr;
+        f->knots_cap = 0;
+        F_CUDA(f, dalloc(&f->knots, need));
+        f->knots_cap = need;
+    }
+    F_CUDA(f, cudaMemsetAsync(f->gemm_err, 0, sizeof(int), st));
+    // the conditioner in chunks of the batch capacity, then the knots
+    for (int c0 = 0; c0 < n_cond; c0 += f->cap) {
+        const int m = std::min(f->cap, n_cond - c0);
+        const int mp = (m + 127) / 128 * 128;
+        F_OK(pack(f, cond + static_cast<size_t>(c0) * kCond, m, mp, on_device));
+        F_OK(forward(f, mp, false));
+        with_bins(f->K, [&](auto kc) {
+            ntp::knots_kernel<decltype(kc)::value><<<ntp::blocks_for(m, 128), 128, 0, st>>>(
+                f->P, f->n_pad, f->L, m, f->r0, f->r1, f->knots + static_cast<size_t>(c0) * row);
+        });
+        F_CUDA(f, cudaGetLastError());
+    }
+    if (log_expec) {
+        F_CUDA(f, cudaMemcpy2DAsync(log_expec, sizeof(float), f->knots + row - 1, sizeof(float) * row, sizeof(float),
+                                    n_cond, on_device ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost, st));
+    }
+    if (n_tuples > 0) {
+        const int grid = static_cast<int>(std::min<unsigned long long>((n_tuples + 255) / 256, 152ull * 16));
+        if (on_device) {
+            with_bins(f->K, [&](auto kc) {
+                ntp::logpdf_kernel<decltype(kc)::value>
+                    <<<grid, 256, 0, st>>>(f->knots, f->L, n_cond, cond_index, times, n_tuples, logpdf);
+            });
+            F_CUDA(f, cudaGetLastError());
+        } else {
+            void* tmp = nullptr;
+            F_CUDA(f, cudaMalloc(&tmp, n_tuples * (sizeof(int) + 2 * sizeof(float))));
+            int* di = static_cast<int*>(tmp);
+            float* dt = reinterpret_cast<float*>(di + n_tuples);
+            float* dout = dt + n_tuples;
+            cudaError_t e = cudaMemcpyAsync(di, cond_index, sizeof(int) * n_tuples, cudaMemcpyHostToDevice, st);
+            if (e == cudaSuccess) e = cudaMemcpyAsync(dt, times, sizeof(float) * n_tuples, cudaMemcpyHostToDevice, st);
+            if (e == cudaSuccess) {
+                with_bins(f->K, [&](auto kc) {
+                    ntp::logpdf_kernel<decltype(kc)::value>
+                        <<<grid, 256, 0, st>>>(f->knots, f->L, n_cond, di, dt, n_tuples, dout);
+                });
+                e = cudaGetLastError();
+            }
+            if (e == cudaSuccess)
+                e = cudaMemcpyAsync(logpdf, dout, sizeof(float) * n_tuples, cudaMemcpyDeviceToHost, st);
+            if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+            cudaFree(tmp);
+            if (e != cudaSuccess) return ferr(f, e, "ntp_flow_evaluate");
+        }
+    }
+    return check_gemm(f);
+}
+
+}  // extern "C"

@@ -138,9 +138,8 @@ struct Smem {
 // out_kind: 0 = FP32 store, 1 = BF16 store, 2 = FP32 atomic add (split-K)
 template <int BN>
 __global__ void __launch_bounds__(kThreads, 1)
-    gemm_bf16_kernel(const __grid_constant__ CUtensorMap map_a, const __grid_constant__ CUtensorMap map_b, void* c,
-                     int M, int N, int ldc, int k_tiles_per_split, int k_tiles_total, const float* __restrict__ bias,
-                     int relu, int out_kind, int* __restrict__ error) {
+    gemm_bf16_kernel(const __grid_constant__ CUtensorMap map_a, const __grid_constant__ CUtensorMap map_b, int M,
+                     int N, int k_tiles_per_split, int k_tiles_total, const GemmEpilogue ep, int* __restrict__ error) {
     extern __shared__ unsigned char smem_raw[];
     Smem<BN>* s = reinterpret_cast<Smem<BN>*>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
@@ -226,18 +225,30 @@ __global__ void __launch_bounds__(kThreads, 1)
         for (int c0 = 0; c0 < BN; c0 += 32) {
             float v[32];
             tmem_ld32(tmem + (static_cast<uint32_t>(warp * 32) << 16) + static_cast<uint32_t>(c0), v);
-            if (row < M) {
 #pragma unroll
-                for (int j = 0; j < 32; ++j) {
-                    const int col = n0 + c0 + j;
-                    if (col >= N) continue;
-                    float x = v[j];
-                    if (bias && blockIdx.z == 0) x += bias[col];
-                    if (relu) x = fmaxf(x, 0.0f);
-                    const size_t o = static_cast<size_t>(row) * ldc + col;
-                    if (out_kind == 0) static_cast<float*>(c)[o] = x;
-                    else if (out_kind == 1) static_cast<__nv_bfloat16*>(c)[o] = __float2bfloat16(x);
-                    else atomicAdd(static_cast<float*>(c) + o, x);
+            for (int j = 0; j < 32; ++j) {
+                const int col = n0 + c0 + j;
+                float x = v[j];
+                const bool in = row < M && col < N;
+                if (in) {
+                    if (ep.bias && blockIdx.z == 0) x += ep.bias[col];
+                    if (ep.relu) x = fmaxf(x, 0.0f);
+                    if (ep.mask && !(__bfloat162float(ep.mask[static_cast<size_t>(row) * ep.ldm + col]) > 0.0f))
+                        x = 0.0f;
+                    const size_t o = static_cast<size_t>(row) * ep.ldc + col;
+                    if (ep.c) {
+                        if (ep.out_kind == 0) static_cast<float*>(ep.c)[o] = x;
+                        else if (ep.out_kind == 1) static_cast<__nv_bfloat16*>(ep.c)[o] = __float2bfloat16(x);
+                        else atomicAdd(static_cast<float*>(ep.c) + o, x);
+                    }
+                    if (ep.ct) ep.ct[static_cast<size_t>(col) * ep.ldct + row] = __float2bfloat16(x);
+                } else {
+                    x = 0.0f;
+                }
+                if (ep.colsum) {  // column sums: the warp's 32 rows, then one atomic
+#pragma unroll
+                    for (int off = 16; off > 0; off >>= 1) x += __shfl_xor_sync(0xffffffffu, x, off);
+                    if (lane == 0 && col < N) atomicAdd(ep.colsum + col, x);
                 }
             }
         }
@@ -281,28 +292,28 @@ bool make_map(CUtensorMap* map, const void* base, int rows, int cols, int ld, in
 }
 
 template <int BN>
-cudaError_t launch_bn(const CUtensorMap& ma, const CUtensorMap& mb, void* c, int M, int N, int ldc, int splits,
-                      int k_tiles, const float* bias, int relu, int out_kind, int* error, cudaStream_t st) {
+cudaError_t launch_bn(const CUtensorMap& ma, const CUtensorMap& mb, int M, int N, int splits, int k_tiles,
+                      const GemmEpilogue& ep, int* error, cudaStream_t st) {
     const size_t smem = sizeof(Smem<BN>) + 1024;
     cudaError_t e = cudaFuncSetAttribute(gemm_bf16_kernel<BN>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                          static_cast<int>(smem));
     if (e != cudaSuccess) return e;
     const int per = (k_tiles + splits - 1) / splits;
     dim3 grid((M + kBM - 1) / kBM, (N + BN - 1) / BN, splits);
-    gemm_bf16_kernel<BN><<<grid, kThreads, smem, st>>>(ma, mb, c, M, N, ldc, per, k_tiles, bias, relu, out_kind,
-                                                      error);
+    gemm_bf16_kernel<BN><<<grid, kThreads, smem, st>>>(ma, mb, M, N, per, k_tiles, ep, error);
     return cudaGetLastError();
 }
 
 }  // namespace
 
-// C = A * B^T on the tensor cores; see the file comment.  lda / ldb / ldc in
-// elements; A's and B's rows must start on 16-byte boundaries (lda, ldb
-// multiples of 8) and K a multiple of 64.  splits > 1 splits K across CTAs
-// and requires out_kind 2 (atomic add into a zeroed C).
-cudaError_t gemm_bf16(const void* A, int lda, const void* B, int ldb, void* C, int ldc, int M, int N, int K,
-                      const float* bias, int relu, int out_kind, int splits, int* error, cudaStream_t st) {
-    if (M <= 0 || N <= 0 || K <= 0 || K % kBK || lda % 8 || ldb % 8 || (splits > 1 && out_kind != 2) ||
+// C = A * B^T on the tensor cores with the epilogue ep; see the file comment.
+// lda / ldb in elements; A's and B's rows must start on 16-byte boundaries
+// (lda, ldb multiples of 8) and K a multiple of 64.  splits > 1 splits K
+// across CTAs and allows only the atomic FP32 output (out_kind 2).
+cudaError_t gemm_bf16_ep(const void* A, int lda, const void* B, int ldb, int M, int N, int K, const GemmEpilogue& ep,
+                         int splits, int* error, cudaStream_t st) {
+    if (M <= 0 || N <= 0 || K <= 0 || K % kBK || lda % 8 || ldb % 8 ||
+        (splits > 1 && (ep.out_kind != 2 || ep.ct || ep.mask || ep.colsum || ep.relu)) ||
         (reinterpret_cast<uintptr_t>(A) & 15) || (reinterpret_cast<uintptr_t>(B) & 15))
         return cudaErrorInvalidValue;
     const int bn = N <= 64 ? 64 : (N <= 128 ? 128 : 256);
@@ -310,9 +321,20 @@ cudaError_t gemm_bf16(const void* A, int lda, const void* B, int ldb, void* C, i
     if (!make_map(&ma, A, M, K, lda, kBM) || !make_map(&mb, B, N, K, ldb, bn)) return cudaErrorInvalidValue;
     const int k_tiles = K / kBK;
     splits = splits < 1 ? 1 : (splits > k_tiles ? k_tiles : splits);
-    if (bn == 64) return launch_bn<64>(ma, mb, C, M, N, ldc, splits, k_tiles, bias, relu, out_kind, error, st);
-    if (bn == 128) return launch_bn<128>(ma, mb, C, M, N, ldc, splits, k_tiles, bias, relu, out_kind, error, st);
-    return launch_bn<256>(ma, mb, C, M, N, ldc, splits, k_tiles, bias, relu, out_kind, error, st);
+    if (bn == 64) return launch_bn<64>(ma, mb, M, N, splits, k_tiles, ep, error, st);
+    if (bn == 128) return launch_bn<128>(ma, mb, M, N, splits, k_tiles, ep, error, st);
+    return launch_bn<256>(ma, mb, M, N, splits, k_tiles, ep, error, st);
+}
+
+cudaError_t gemm_bf16(const void* A, int lda, const void* B, int ldb, void* C, int ldc, int M, int N, int K,
+                      const float* bias, int relu, int out_kind, int splits, int* error, cudaStream_t st) {
+    GemmEpilogue ep{};
+    ep.c = C;
+    ep.ldc = ldc;
+    ep.out_kind = out_kind;
+    ep.bias = bias;
+    ep.relu = relu;
+    return gemm_bf16_ep(A, lda, B, ldb, M, N, K, ep, splits, error, st);
 }
 
 }  // namespace ntp

@@ -6,6 +6,7 @@
 #include <string>
 #include <vector>
 
+#include <cuda_bf16.h>
 #include <cuda_runtime.h>
 
 #include "../../include/ntp.h"
@@ -129,6 +130,25 @@ cudaError_t launch_pmt_summary(const HitTargetTable& t, const ntp_hit* hits, uns
                                const double* acc, int n_acc, const double* tgeo, int use_tres, int max_pmts,
                                int n_bins, double t_min, double t_max, double* wsum, double* count, double* hist,
                                cudaStream_t stream);
+// Epilogue of the tensor-core GEMM: value = acc (+ bias[col]) (ReLU) (zeroed
+// where mask[row][col] <= 0); stored to c (FP32 / BF16 / FP32 atomic add),
+// to ct transposed (BF16, ct[col * ldct + row]) and summed per column into
+// colsum (FP32 atomics); every output pointer may be NULL.
+struct GemmEpilogue {
+    void* c;
+    int ldc;
+    int out_kind;                // 0 FP32, 1 BF16, 2 FP32 atomic add
+    const float* bias;
+    int relu;
+    __nv_bfloat16* ct;
+    int ldct;
+    const __nv_bfloat16* mask;
+    int ldm;
+    float* colsum;
+};
+cudaError_t gemm_bf16_ep(const void* A, int lda, const void* B, int ldb, int M, int N, int K, const GemmEpilogue& ep,
+                         int splits, int* error, cudaStream_t st);
+
 // C = A * B^T, BF16 operands (K-major), FP32 accumulation on the tensor cores
 // (flow_gemm.cu).  out_kind: 0 = FP32, 1 = BF16, 2 = FP32 atomic add.
 cudaError_t gemm_bf16(const void* A, int lda, const void* B, int ldb, void* C, int ldc, int M, int N, int K,

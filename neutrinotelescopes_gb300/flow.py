@@ -1,0 +1,254 @@
+"""The arrival-time surrogate: RQNormFlow on the GPU (include/ntp.h, ntp_flow_*).
+
+Mirrors src/surrogate_models/extended_cascade_model.jl of
+chrhck/NeutrinoTelescopes: ``RQNormFlow`` (:53-101) with its call
+``model(x, cond, pred_log_expec)`` (:110-125), ``log_likelihood_with_poisson``
+(:132-139), ``RQNormFlowHParams`` (:153-164) and a ``train_model!``-style loop
+(:237-295).  The conditioner's GEMMs run on the tensor cores (BF16 weights,
+FP32 accumulation), the spline head and Adam in FP32, all in libntp.so.
+
+Conditions are 5 features; ``flow_features`` maps (distance, cos theta of the
+source direction, cos theta of the PMT axis, azimuth, energy) to them.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import math
+from dataclasses import dataclass
+
+import numpy as np
+
+from . import _abi
+
+N_FEATURES = 5
+
+
+def flow_features(distance, cos_theta_src, cos_theta_pmt, phi, log10_energy) -> np.ndarray:
+    """Normalised condition features [n x 5] (float32): log-distance over
+    1-200 m and log10 E over 2-6 mapped to [-1, 1], the cosines as they are,
+    the azimuth over [0, 2 pi) mapped to [-1, 1]."""
+    d = np.asarray(distance, np.float64)
+    f = np.stack([
+        2.0 * (np.log(d) - math.log(1.0)) / (math.log(200.0) - math.log(1.0)) - 1.0,
+        np.asarray(cos_theta_src, np.float64),
+        np.asarray(cos_theta_pmt, np.float64),
+        np.asarray(phi, np.float64) / math.pi - 1.0,
+        (np.asarray(log10_energy, np.float64) - 4.0) / 2.0,
+    ], axis=-1)
+    return np.ascontiguousarray(f, dtype=np.float32)
+
+
+@dataclass
+class RQNormFlowHParams:
+    """RQNormFlowHParams (extended_cascade_model.jl:153-164) for this model:
+    the MLP is fixed at 3 x 256 and dropout is not applied."""
+    K: int = 12
+    n_layers: int = 5
+    range_min: float = -20.0
+    range_max: float = 1500.0
+    batch_size: int = 8192
+    lr: float = 1e-3
+    beta1: float = 0.9
+    beta2: float = 0.999
+    eps: float = 1e-8
+    seed: int = 31338
+
+
+def _f32(a, n=None) -> np.ndarray:
+    a = np.ascontiguousarray(a, dtype=np.float32)
+    if n is not None and a.shape[0] != n:
+        raise ValueError(f"expected {n} rows, got {a.shape[0]}")
+    return a
+
+
+class RQNormFlow:
+    """Conditional RQ-spline flow with a log-expectation head on one GPU."""
+
+    def __init__(self, hparams: RQNormFlowHParams | None = None, *, device: int = 0, batch_capacity: int | None = None):
+        self.hparams = hp = hparams or RQNormFlowHParams()
+        self.lib = _abi.load_library()
+        cap = int(batch_capacity or max(hp.batch_size, 128))
+        cap = (cap + 127) // 128 * 128
+        cfg = _abi.NtpFlowConfig(batch_capacity=cap, n_layers=int(hp.n_layers), n_bins=int(hp.K),
+                                 t_min=float(hp.range_min), t_max=float(hp.range_max), lr=float(hp.lr),
+                                 beta1=float(hp.beta1), beta2=float(hp.beta2), eps=float(hp.eps),
+                                 seed=int(hp.seed) & (2 ** 64 - 1))
+        h = C.c_void_p()
+        st = self.lib.ntp_flow_create(int(device), C.byref(cfg), C.byref(h))
+        if st != 0:
+            raise _abi.NtpError(st, "ntp_flow_create failed (invalid configuration or CUDA error)")
+        self._h = h
+        self.batch_capacity = cap
+        n_params, n_out, n_pad = C.c_uint64(), C.c_int32(), C.c_int32()
+        self._check(self.lib.ntp_flow_get_layout(h, C.byref(n_params), C.byref(n_out), C.byref(n_pad)))
+        self.n_params, self.n_outputs, self.n_outputs_padded = n_params.value, n_out.value, n_pad.value
+        self.K, self.n_layers = hp.K, hp.n_layers
+        self.range_min, self.range_max = hp.range_min, hp.range_max
+
+    # ----------------------------------------------------------------- plumbing
+    def _check(self, status: int) -> None:
+        if status != 0:
+            msg = self.lib.ntp_flow_last_error(self._h) if getattr(self, "_h", None) else b""
+            raise _abi.NtpError(status, (msg or b"").decode())
+
+    def close(self) -> None:
+        if getattr(self, "_h", None):
+            self.lib.ntp_flow_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    def layout(self) -> list[tuple[str, tuple[int, int], int]]:
+        """(name, shape, offset) of each block of the flat parameter vector."""
+        dims = [("W1", (256, 64)), ("b1", (256,)), ("W2", (256, 256)), ("b2", (256,)), ("W3", (256, 256)),
+                ("b3", (256,)), ("W4", (self.n_outputs_padded, 256)), ("b4", (self.n_outputs_padded,))]
+        out, off = [], 0
+        for name, shape in dims:
+            out.append((name, shape, off))
+            off += int(np.prod(shape))
+        assert off == self.n_params
+        return out
+
+    # -------------------------------------------------------------- parameters
+    def get_params(self, which: int = 0) -> np.ndarray:
+        """which: 0 weights, 1 gradient of the last step, 2 / 3 Adam moments."""
+        out = np.empty(self.n_params, np.float32)
+        self._check(self.lib.ntp_flow_get_params(self._h, out.ctypes.data, self.n_params, int(which)))
+        return out
+
+    def set_params(self, theta) -> None:
+        theta = _f32(theta)
+        if theta.size != self.n_params:
+            raise ValueError(f"expected {self.n_params} parameters, got {theta.size}")
+        self._check(self.lib.ntp_flow_set_params(self._h, theta.ctypes.data, self.n_params))
+
+    def gradient(self) -> np.ndarray:
+        return self.get_params(1)
+
+    # ---------------------------------------------------------------- training
+    def train_step(self, cond, tres, nhits, has_time=None, *, update: bool = True) -> float:
+        """One Adam step on a batch (rows a multiple of 128); returns the loss
+        of log_likelihood_with_poisson before the step.  Inputs may be numpy
+        arrays (host) or CUDA torch tensors (device)."""
+        dev = _is_device(cond)
+        if dev:
+            B = int(cond.shape[0])
+            ptrs = [cond.data_ptr(), tres.data_ptr(), nhits.data_ptr(), has_time.data_ptr()]
+            keep = None
+        else:
+            cond = _f32(cond)
+            B = cond.shape[0]
+            tres, nhits = _f32(tres, B), _f32(nhits, B)
+            has_time = np.ones(B, np.int32) if has_time is None else np.ascontiguousarray(has_time, np.int32)
+            keep = (cond, tres, nhits, has_time)
+            ptrs = [a.ctypes.data for a in keep]
+        loss = C.c_double()
+        self._check(self.lib.ntp_flow_train_step(self._h, *ptrs, B, int(dev), int(bool(update)), C.byref(loss)))
+        del keep
+        return loss.value
+
+    def fit(self, cond, tres, nhits, has_time=None, *, epochs: int = 1, batch_size: int | None = None,
+            seed: int = 0, max_steps: int | None = None) -> list[float]:
+        """train_model! (extended_cascade_model.jl:237-295) without the test
+        split and early stopping: shuffled mini-batches over the table, one
+        Adam step each; returns the per-step losses.  A ragged last batch is
+        dropped (batches are multiples of 128)."""
+        cond = _f32(cond)
+        n = cond.shape[0]
+        tres, nhits = _f32(tres, n), _f32(nhits, n)
+        has_time = np.ones(n, np.int32) if has_time is None else np.ascontiguousarray(has_time, np.int32)
+        bs = int(batch_size or self.hparams.batch_size)
+        bs = max(128, min(bs, self.batch_capacity) // 128 * 128)
+        rng = np.random.default_rng(seed)
+        losses: list[float] = []
+        for _ in range(epochs):
+            perm = rng.permutation(n)
+            for s in range(0, n - bs + 1, bs):
+                idx = perm[s:s + bs]
+                losses.append(self.train_step(cond[idx], tres[idx], nhits[idx], has_time[idx]))
+                if max_steps is not None and len(losses) >= max_steps:
+                    return losses
+        return losses
+
+    # --------------------------------------------------------------- inference
+    def forward_params(self, cond) -> np.ndarray:
+        """The conditioner's raw outputs [n x n_outputs] (spline parameters,
+        shift, raw scale, log expectation)."""
+        cond = _f32(cond)
+        out = np.empty((cond.shape[0], self.n_outputs), np.float32)
+        self._check(self.lib.ntp_flow_forward(self._h, cond.ctypes.data, cond.shape[0], out.ctypes.data))
+        return out
+
+    def head(self, params, tres, nhits, has_time=None) -> tuple[float, np.ndarray]:
+        """Loss and its gradient by the raw outputs for given raw outputs."""
+        params = _f32(params)
+        B = params.shape[0]
+        tres, nhits = _f32(tres, B), _f32(nhits, B)
+        has_time = np.ones(B, np.int32) if has_time is None else np.ascontiguousarray(has_time, np.int32)
+        grad = np.empty_like(params)
+        loss = C.c_double()
+        self._check(self.lib.ntp_flow_head(self._h, params.ctypes.data, tres.ctypes.data, nhits.ctypes.data,
+                                           has_time.ctypes.data, B, C.byref(loss), grad.ctypes.data))
+        return loss.value, grad
+
+    def logpdf(self, cond, cond_index, times, *, log_expec: bool = False):
+        """log p(t | cond[cond_index]) for each (cond_index, time) pair, and
+        optionally the log expectation of every condition."""
+        dev = _is_device(cond)
+        n_cond = int(cond.shape[0])
+        if dev:
+            import torch
+            n = int(times.numel())
+            out = torch.empty(n, dtype=torch.float32, device=times.device)
+            le = torch.empty(n_cond, dtype=torch.float32, device=times.device) if log_expec else None
+            self._check(self.lib.ntp_flow_evaluate(self._h, cond.data_ptr(), n_cond, cond_index.data_ptr(),
+                                                   times.data_ptr(), n, out.data_ptr(),
+                                                   le.data_ptr() if le is not None else None, 1))
+        else:
+            cond = _f32(cond)
+            cond_index = np.ascontiguousarray(cond_index, np.int32)
+            times = _f32(times)
+            n = times.size
+            if cond_index.size != n:
+                raise ValueError("cond_index and times differ in length")
+            out = np.empty(n, np.float32)
+            le = np.empty(n_cond, np.float32) if log_expec else None
+            self._check(self.lib.ntp_flow_evaluate(self._h, cond.ctypes.data, n_cond, cond_index.ctypes.data,
+                                                   times.ctypes.data, n, out.ctypes.data,
+                                                   le.ctypes.data if le is not None else None, 0))
+        return (out, le) if log_expec else out
+
+    def __call__(self, x, cond, pred_log_expec: bool = False):
+        """The reference's model call (extended_cascade_model.jl:110-125):
+        per sample i the log-pdf of x[i] under cond[i], and with
+        pred_log_expec the per-sample log expectation."""
+        cond = _f32(cond)
+        n = cond.shape[0]
+        idx = np.arange(n, dtype=np.int32)
+        if pred_log_expec:
+            return self.logpdf(cond, idx, _f32(x, n), log_expec=True)
+        return self.logpdf(cond, idx, _f32(x, n))
+
+
+def log_likelihood_with_poisson(x: dict, model: RQNormFlow) -> float:
+    """log_likelihood_with_poisson (extended_cascade_model.jl:132-139):
+    -(sum(logpdf(tres)) + sum(Poisson log-likelihood of nhits)) / n."""
+    lp, le = model(x["tres"], x["label"], True)
+    n = np.asarray(x["nhits"], np.float64)
+    le = le.astype(np.float64)
+    poiss = n * le - np.exp(le) - np.array([math.lgamma(v + 1.0) for v in n])
+    return float(-(lp.astype(np.float64).sum() + poiss.sum()) / len(lp))
+
+
+def _is_device(a) -> bool:
+    return hasattr(a, "is_cuda") and bool(a.is_cuda)

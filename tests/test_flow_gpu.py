@@ -1,0 +1,233 @@
+"""The flow's CUDA kernels (ntp_flow_*) against the torch-float64 CPU oracle
+(oracle/flow_ref.py).
+
+Tolerances, and why:
+* head (spline loss and its gradient by the raw outputs, FP32 on the GPU
+  versus float64 on the same FP32 inputs): loss to 1e-5 relative; gradient
+  rows to 2e-3 relative L2 (the inverse spline in FP32 loses a few bits in
+  steep bins, where dx/dy reaches ~100, and the loss of 5 stacked layers
+  chains them).
+* conditioner forward (BF16 tensor cores, FP32 accumulation) versus the
+  oracle with the same BF16 rounding of input, weights and activations in
+  float64: |dP| <= 2e-3 (1 + |P|) (accumulation order, and an activation
+  that rounds to a neighbouring BF16 value).
+* full-network gradient: the GPU backward also rounds dP, dZ and the
+  transposed weights to BF16; per parameter block relative L2 error <= 3e-2
+  and cosine similarity >= 0.999 against the float64 autograd gradient.
+* Adam: the update itself is FP32 elementwise: 1e-6 relative.
+"""
+import math
+
+import numpy as np
+import pytest
+
+torch = pytest.importorskip("torch")
+
+from neutrinotelescopes_gb300 import _abi  # noqa: E402
+from neutrinotelescopes_gb300.flow import RQNormFlow, RQNormFlowHParams, log_likelihood_with_poisson  # noqa: E402
+from oracle import flow_ref as R  # noqa: E402
+
+pytestmark = pytest.mark.gpu
+
+CASES = [  # (n_layers, K, range): the reference's default model and the 5-layer benchmark model
+    (1, 10, -20.0, 100.0),
+    (5, 12, -20.0, 1500.0),
+]
+
+
+def make(L, K, r0, r1, cap=2048, seed=1):
+    return RQNormFlow(RQNormFlowHParams(K=K, n_layers=L, range_min=r0, range_max=r1, batch_size=cap, seed=seed))
+
+
+def batch(rng, B, r0, r1, frac_count_only=0.1):
+    R_ = r1 - r0
+    tres = rng.uniform(r0 - 0.1 * R_, r0 + 0.6 * R_, B).astype(np.float32)
+    nhits = rng.poisson(3.0, B).astype(np.float32)
+    has = (rng.uniform(size=B) > frac_count_only).astype(np.int32)
+    cond = rng.uniform(-1, 1, (B, 5)).astype(np.float32)
+    return cond, tres, nhits, has
+
+
+@pytest.mark.parametrize("L,K,r0,r1", CASES)
+def test_head_loss_and_gradient(L, K, r0, r1):
+    rng = np.random.default_rng(10 + L)
+    B = 1024
+    with make(L, K, r0, r1) as fl:
+        n_out = fl.n_outputs
+        raw = (rng.standard_normal((B, n_out)) * 0.8).astype(np.float32)
+        NP = 3 * K + 1
+        raw[:, L * NP] = rng.uniform(r0, r0 + 0.5 * (r1 - r0), B)     # shift
+        raw[:, L * NP + 2] = rng.standard_normal(B) * 2.0               # log expectation
+        _, tres, nhits, has = batch(rng, B, r0, r1)
+        loss, grad = fl.head(raw, tres, nhits, has)
+    t = torch.as_tensor(raw.astype(np.float64)).requires_grad_(True)
+    ref = R.head_loss(t, torch.as_tensor(tres.astype(np.float64)), torch.as_tensor(nhits.astype(np.float64)),
+                      torch.as_tensor(has.astype(bool)), L, K, r0, r1)
+    ref.backward()
+    g_ref = t.grad.numpy()
+    assert loss == pytest.approx(ref.item(), rel=1e-5)
+    err = np.linalg.norm(grad - g_ref, axis=1) / (np.linalg.norm(g_ref, axis=1) + 1e-12)
+    assert np.quantile(err, 0.99) < 2e-3, np.sort(err)[-5:]
+    assert np.linalg.norm(grad - g_ref) / np.linalg.norm(g_ref) < 2e-3
+
+
+@pytest.mark.parametrize("L,K,r0,r1", CASES)
+def test_conditioner_forward(L, K, r0, r1):
+    rng = np.random.default_rng(3)
+    with make(L, K, r0, r1) as fl:
+        cond = rng.uniform(-1, 1, (1000, 5)).astype(np.float32)   # not a multiple of 128: padded pass
+        P = fl.forward_params(cond)
+        theta = fl.get_params()
+        n_pad = fl.n_outputs_padded
+    ref = R.conditioner(R.unpack(theta, n_pad), torch.as_tensor(cond.astype(np.float64)), bf16=True).numpy()
+    ref = ref[:, :P.shape[1]]
+    assert np.all(np.abs(P - ref) <= 2e-3 * (1 + np.abs(ref))), np.abs(P - ref).max()
+
+
+@pytest.mark.parametrize("L,K,r0,r1", CASES)
+def test_full_gradient(L, K, r0, r1):
+    rng = np.random.default_rng(20 + L)
+    B = 1024
+    with make(L, K, r0, r1) as fl:
+        cond, tres, nhits, has = batch(rng, B, r0, r1)
+        loss = fl.train_step(cond, tres, nhits, has, update=False)
+        g = fl.gradient()
+        theta = fl.get_params()
+        layout = fl.layout()
+        n_pad, n_out = fl.n_outputs_padded, fl.n_outputs
+    ref_loss, g_ref = R.full_loss(theta, cond, tres, nhits, has.astype(bool), L, K, r0, r1, n_pad, bf16=True)
+    assert loss == pytest.approx(ref_loss, rel=1e-3)
+    for name, shape, off in layout:
+        size = int(np.prod(shape))
+        a, b = g[off:off + size].astype(np.float64), g_ref[off:off + size]
+        if name == "W1":  # padding input columns carry no gradient
+            assert np.all(a.reshape(shape)[:, 5:] == 0.0)
+        if name in ("W4", "b4"):
+            rows = a.reshape(shape[0], -1)
+            assert np.all(rows[n_out:] == 0.0)
+        nb = np.linalg.norm(b)
+        assert np.linalg.norm(a - b) <= 3e-2 * nb + 1e-7, (name, np.linalg.norm(a - b) / nb)
+        assert np.dot(a, b) >= 0.999 * np.linalg.norm(a) * nb, name
+
+
+def test_adam_steps_and_weight_copies():
+    L, K, r0, r1 = 5, 12, -20.0, 1500.0
+    rng = np.random.default_rng(30)
+    hp = RQNormFlowHParams(K=K, n_layers=L, range_min=r0, range_max=r1, batch_size=512, seed=9, lr=1e-3)
+    with RQNormFlow(hp) as fl:
+        th = fl.get_params().astype(np.float64)
+        m = np.zeros_like(th)
+        v = np.zeros_like(th)
+        for step in (1, 2):
+            cond, tres, nhits, has = batch(rng, 512, r0, r1)
+            fl.train_step(cond, tres, nhits, has)
+            g = fl.gradient().astype(np.float64)
+            # the hyperparameters as the FP32 values the kernel uses (1 - 0.999f differs from 1e-3 by 1.3e-5)
+            f32 = lambda x: float(np.float32(x))  # noqa: E731
+            th, m, v = R.adam_update(th, m, v, g, step, f32(hp.lr), f32(hp.beta1), f32(hp.beta2), f32(hp.eps))
+            # FP32 elementwise: relative to each array's scale where b1 m + (1 - b1) g cancels
+            np.testing.assert_allclose(fl.get_params(2), m, rtol=1e-5, atol=1e-6 * np.abs(m).max())
+            np.testing.assert_allclose(fl.get_params(3), v, rtol=1e-5, atol=1e-6 * np.abs(v).max())
+            np.testing.assert_allclose(fl.get_params(0), th, rtol=1e-6, atol=1e-7)
+        # the BF16 copies follow the updated master weights
+        cond = rng.uniform(-1, 1, (256, 5)).astype(np.float32)
+        P = fl.forward_params(cond)
+        ref = R.conditioner(R.unpack(fl.get_params(), fl.n_outputs_padded),
+                            torch.as_tensor(cond.astype(np.float64)), bf16=True).numpy()[:, :P.shape[1]]
+        assert np.all(np.abs(P - ref) <= 2e-3 * (1 + np.abs(ref)))
+
+
+@pytest.mark.parametrize("L,K,r0,r1", CASES)
+def test_evaluate_matches_oracle_on_the_same_parameters(L, K, r0, r1):
+    rng = np.random.default_rng(40)
+    with make(L, K, r0, r1) as fl:
+        n_cond = 300
+        cond = rng.uniform(-1, 1, (n_cond, 5)).astype(np.float32)
+        P = fl.forward_params(cond)
+        idx = rng.integers(0, n_cond, 20000).astype(np.int32)
+        t = rng.uniform(r0 - 0.2 * (r1 - r0), r1 + 0.2 * (r1 - r0), idx.size).astype(np.float32)
+        lp, le = fl.logpdf(cond, idx, t, log_expec=True)
+        bad = fl.logpdf(cond, np.array([-1, n_cond], np.int32), np.zeros(2, np.float32))
+        # the reference-style call and loss
+        x = {"tres": t[:1000], "label": cond[idx[:1000]], "nhits": rng.poisson(2.0, 1000).astype(np.float32)}
+        ll = log_likelihood_with_poisson(x, fl)
+    Pt = torch.as_tensor(P[idx].astype(np.float64))
+    ref = R.flow_logpdf(torch.as_tensor(t.astype(np.float64)), Pt, L, r0, r1, K).numpy()
+    np.testing.assert_allclose(lp, ref, rtol=1e-4, atol=2e-4)
+    np.testing.assert_allclose(le, P[:, -1], rtol=0, atol=0)
+    assert np.all(np.isnan(bad))
+    P1 = torch.as_tensor(P[idx[:1000]].astype(np.float64))
+    lp1 = R.flow_logpdf(torch.as_tensor(t[:1000].astype(np.float64)), P1, L, r0, r1, K).numpy()
+    le1 = P[idx[:1000], -1].astype(np.float64)
+    n = x["nhits"].astype(np.float64)
+    want = -(lp1.sum() + (n * le1 - np.exp(le1) - np.array([math.lgamma(a + 1) for a in n])).sum()) / 1000
+    assert ll == pytest.approx(want, rel=1e-4)
+
+
+def test_density_integrates_to_one_on_device():
+    # a size-independent property at a full-size evaluation (16.8 M tuples)
+    L, K, r0, r1 = 5, 12, -20.0, 1500.0
+    rng = np.random.default_rng(50)
+    with make(L, K, r0, r1, seed=4) as fl:
+        n_cond = 64
+        cond = torch.as_tensor(rng.uniform(-1, 1, (n_cond, 5)).astype(np.float32), device="cuda")
+        grid = np.unique(np.concatenate([np.linspace(-3000.0, r0, 20000), np.linspace(r0, r1, 222144),
+                                         np.linspace(r1, 6000.0, 20000)]))
+        n_t = grid.size
+        t = torch.as_tensor(np.tile(grid, n_cond).astype(np.float32), device="cuda")
+        idx = torch.arange(n_cond, device="cuda", dtype=torch.int32).repeat_interleave(n_t)
+        lp = fl.logpdf(cond, idx, t).view(n_cond, n_t).double().cpu().numpy()
+    p = np.exp(lp)
+    mass = np.sum((p[:, 1:] + p[:, :-1]) * 0.5 * np.diff(grid)[None, :], axis=1)
+    np.testing.assert_allclose(mass, 1.0, atol=2e-3)
+
+
+def test_training_learns_a_conditional_density():
+    """Loss falls and the fitted density matches held-out samples (KS) and
+    the expected counts on a synthetic conditional distribution."""
+    L, K, r0, r1 = 5, 12, -20.0, 1500.0
+    rng = np.random.default_rng(60)
+
+    def sample(cond):
+        mu = 50.0 + 40.0 * cond[:, 0]
+        return (mu + rng.gamma(2.0, 15.0 * (1.5 + cond[:, 1]))).astype(np.float32)
+
+    def lam(cond):
+        return np.exp(1.0 + 0.8 * cond[:, 2])
+
+    n = 1 << 19
+    cond = rng.uniform(-1, 1, (n, 5)).astype(np.float32)
+    tres = sample(cond)
+    nhits = rng.poisson(lam(cond)).astype(np.float32)
+    hp = RQNormFlowHParams(K=K, n_layers=L, range_min=r0, range_max=r1, batch_size=4096, lr=2e-3, seed=3)
+    with RQNormFlow(hp) as fl:
+        losses = fl.fit(cond, tres, nhits, epochs=24)
+        assert np.mean(losses[-20:]) < np.mean(losses[:5]) - 1.0, (losses[:5], losses[-20:])
+        test_c = np.array([[-0.5, 0.0, 0.5, 0.0, 0.0], [0.5, -0.5, -0.5, 0.3, 0.2]], np.float32)
+        grid = np.linspace(r0, 600.0, 20001).astype(np.float32)
+        for c in test_c:
+            lp, le = fl.logpdf(c[None], np.zeros(grid.size, np.int32), grid, log_expec=True)
+            pdf = np.exp(lp.astype(np.float64))
+            cdf = np.concatenate([[0.0], np.cumsum((pdf[1:] + pdf[:-1]) * 0.5 * np.diff(grid))])
+            s = np.sort(sample(np.repeat(c[None], 4000, axis=0)))
+            F = np.interp(s, grid, cdf)
+            ks = np.max(np.maximum(np.arange(1, s.size + 1) / s.size - F, F - np.arange(s.size) / s.size))
+            assert ks < 0.05, ks
+            assert abs(float(le[0]) - math.log(lam(c[None])[0])) < 0.1
+
+
+def test_invalid_arguments():
+    lib = _abi.load_library()
+    import ctypes as C
+    bad = _abi.NtpFlowConfig(batch_capacity=1024, n_layers=1, n_bins=11, t_min=-20, t_max=100, lr=1e-3, beta1=0.9,
+                             beta2=0.999, eps=1e-8, seed=0)
+    h = C.c_void_p()
+    assert lib.ntp_flow_create(0, C.byref(bad), C.byref(h)) == _abi.NTP_ERR_INVALID
+    assert not h.value
+    with make(1, 10, -20.0, 100.0, cap=256) as fl:
+        cond, tres, nhits, has = batch(np.random.default_rng(0), 200, -20.0, 100.0)
+        with pytest.raises(_abi.NtpError) as e:
+            fl.train_step(cond, tres, nhits, has)  # not a multiple of 128
+        assert e.value.status == _abi.NTP_ERR_INVALID
+        with pytest.raises(ValueError):
+            fl.set_params(np.zeros(3, np.float32))
