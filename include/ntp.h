@@ -315,6 +315,50 @@ ntp_status ntp_resample(ntp_ctx* ctx, const ntp_hit* hits, uint64_t n_hits, cons
                         uint64_t seed, int32_t* out_group, double* out_time, uint64_t* out_hit,
                         uint64_t capacity, uint64_t* n_out, int32_t buffers_on_device, void* stream);
 
+/* --------------------------------------------------- flow training tables
+ * run_sim of scripts/photon_tables.jl:52-170 for many simulations at once.
+ * The context holds exactly one MULTI_PMT target (the module); the hits of
+ * one propagation launch over n_sims sources (source_index = simulation) and
+ * their weights (ntp_calc_total_weight) are on the device; sim_weight_scale
+ * (host, per simulation, may be NULL = 1) multiplies the weights: photons of
+ * the source over photons simulated (the reference's oversampling
+ * correction, photon_tables.jl:110).  For each
+ * simulation s and each of n_orientations module orientations r
+ * (orientations[(s * R + r) * 9 ..], row-major, PMT axes rotated as
+ * ntp_make_hits does), every hit is assigned to the PMT whose cone contains
+ * it (FP32 dot product against cos of the opening angle) and each (s, r,
+ * PMT) group is resampled as ntp_resample does, except that the group count
+ * N = Poisson(sum(w) * downsample) is not capped by the number of simulated
+ * hits (with weights scaled up, fewer photons than the source's may have
+ * been simulated); min(N, #hits with w > 0, max_rows_per_group) hits are
+ * drawn without replacement, each a row: cond[5] (the group's condition
+ * features), tres (hit time minus (|source - module| - R) n800 / c,
+ * calc_time_residual!), nhits = N, has_time = 1.  With zero_rows a group
+ * with N = 0 gives one row with has_time = 0, nhits = 0.  Condition features of a group
+ * (u = unit vector module -> source, a = PMT axis, v = source direction):
+ * 2 ln(d)/ln(200) - 1, v.u, a.u, phi/pi - 1 with phi in [0, 2 pi) the angle
+ * from the projection of v to that of a on the plane normal to u (around u),
+ * (log10 E - 4)/2.  Outputs are device buffers; the group outputs (n_sims * R
+ * * n_pmts entries: features, expected count sum(w) * downsample, drawn
+ * count) may be NULL.  *n_rows receives the row count; above capacity
+ * nothing is written and NTP_ERR_OVERFLOW returned. */
+typedef struct ntp_table_spec {
+    int32_t n_sims;             /* simulations = sources of the propagation launch          */
+    int32_t n_orientations;     /* R module orientations per simulation (n_resample)          */
+    int32_t max_rows_per_group; /* rows kept per (simulation, orientation, PMT), e.g. 200      */
+    int32_t zero_rows;          /* 1: a count-only row for a group that draws no hit          */
+    double downsample;          /* resample_simulation's downsample                           */
+    float n800;                 /* refractive index of the time residual                      */
+    int32_t reserved;
+    uint64_t seed;              /* Philox key of the counts and the draws                     */
+} ntp_table_spec;
+
+ntp_status ntp_make_table(ntp_ctx* ctx, const ntp_hit* hits, uint64_t n_hits, const double* weight,
+                          const ntp_source* sims, const float* sim_log10_energy, const double* sim_weight_scale,
+                          const double* orientations, const ntp_table_spec* spec, float* cond, float* tres, float* nhits, int32_t* has_time,
+                          uint64_t capacity, uint64_t* n_rows, float* group_cond, double* group_expec,
+                          uint64_t* group_count, void* stream);
+
 /* ------------------------------------------------------------ tensor cores
  * C = A * B^T with BF16 A [M x K] and B [N x K] (row-major, K contiguous,
  * device pointers, 16-byte aligned rows: lda, ldb multiples of 8, K a

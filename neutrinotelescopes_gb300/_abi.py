@@ -198,6 +198,19 @@ class NtpFlowConfig(C.Structure):
     ]
 
 
+class NtpTableSpec(C.Structure):
+    _fields_ = [
+        ("n_sims", C.c_int32),
+        ("n_orientations", C.c_int32),
+        ("max_rows_per_group", C.c_int32),
+        ("zero_rows", C.c_int32),
+        ("downsample", C.c_double),
+        ("n800", C.c_float),
+        ("reserved", C.c_int32),
+        ("seed", C.c_uint64),
+    ]
+
+
 assert C.sizeof(NtpSource) == 64
 assert C.sizeof(NtpTarget) == 48
 
@@ -236,6 +249,7 @@ EXPORTED = (
     "ntp_calc_time_residual",
     "ntp_pmt_summary",
     "ntp_resample",
+    "ntp_make_table",
     "ntp_gemm_bf16",
     "ntp_flow_create",
     "ntp_flow_destroy",
@@ -290,6 +304,10 @@ def _declare(lib: C.CDLL) -> None:
     lib.ntp_resample.restype = C.c_int
     lib.ntp_gemm_bf16.argtypes = [vp, i32, vp, i32, vp, i32, i32, i32, i32, vp, i32, i32, i32, vp]
     lib.ntp_gemm_bf16.restype = C.c_int
+    lib.ntp_make_table.argtypes = [vp, vp, u64, vp, C.POINTER(NtpSource), C.POINTER(C.c_float),
+                                   C.POINTER(C.c_double), C.POINTER(C.c_double), C.POINTER(NtpTableSpec), vp, vp, vp,
+                                   vp, u64, C.POINTER(u64), vp, vp, vp, vp]
+    lib.ntp_make_table.restype = C.c_int
     lib.ntp_flow_create.argtypes = [i32, C.POINTER(NtpFlowConfig), C.POINTER(vp)]
     lib.ntp_flow_destroy.argtypes = [vp]
     lib.ntp_flow_destroy.restype = None

@@ -3,15 +3,21 @@
 //
 // C[M x N] = A[M x K] * B[N x K]^T (+ bias[N], optional ReLU), A and B
 // row-major with K contiguous (K-major), FP32 accumulation in tensor memory.
-//   * one CTA per 128 x BN output tile, 128 threads (4 warps);
+//   * one CTA per 128 x BN output tile (BN = 64, 128 or 256, the widest that
+//     still gives every SM a CTA), 128 threads (4 warps); split-K over
+//     blockIdx.z for the weight gradients, whose K is the batch;
 //   * operands staged in shared memory by TMA (cp.async.bulk.tensor) in the
-//     128-byte-swizzled layout, two pipeline stages of 64-wide K slices;
+//     128-byte-swizzled layout, 3-4 pipeline stages of 64-wide K slices;
 //   * one elected thread issues tcgen05.mma (cta_group::1, kind::f16, BF16
 //     inputs, FP32 accumulator of 128 lanes x BN columns in TMEM) and
 //     tcgen05.commit signals the stage free / the accumulator complete;
-//   * the epilogue: each warp reads its 32 TMEM lanes with tcgen05.ld, adds
-//     the bias, applies ReLU and stores FP32 or BF16, or atomically adds FP32
-//     (split-K, for weight gradients whose K is the batch).
+//   * the epilogue: each warp reads its 32 TMEM lanes (one row per lane) 32
+//     columns at a time with tcgen05.ld, adds the bias, applies ReLU or a
+//     ReLU mask read as 16-byte vectors, stores FP32 / BF16 or reduces FP32
+//     (split-K) with 16-byte vector operations along the row, writes the
+//     BF16 transpose (one contiguous run per column) and reduces column sums
+//     across the warp by a five-step transpose-reduce (31 shuffles for 32
+//     columns) with one atomic per column.
 // Every wait on an mbarrier gives up after a bounded number of polls, sets
 // the error word and skips to the TMEM release, so a fault in the pipeline
 // returns a status instead of hanging the GPU.
@@ -19,6 +25,8 @@
 #include <cuda_bf16.h>
 #include <cuda_runtime.h>
 
+#include <algorithm>
+#include <atomic>
 #include <cstdint>
 #include <mutex>
 
@@ -31,7 +39,6 @@ namespace {
 constexpr int kBM = 128;   // rows of a tile (UMMA M)
 constexpr int kBK = 64;    // K slice per stage: 64 bf16 = 128 bytes = one swizzle row
 constexpr int kUK = 16;    // K of one tcgen05.mma for 16-bit inputs
-constexpr int kStages = 2;
 constexpr int kThreads = 128;
 constexpr unsigned long long kWaitLimitNs = 2000000000ull;  // a wait gives up after 2 s
 
@@ -125,8 +132,13 @@ __device__ __forceinline__ void tmem_ld32(uint32_t taddr, float* v) {
     for (int i = 0; i < 32; ++i) v[i] = __uint_as_float(r[i]);
 }
 
+// pipeline depth: 4 stages (3 for the widest tile), within 227 KB of shared memory
+template <int BN>
+constexpr int stages_for() { return BN >= 256 ? 3 : 4; }
+
 template <int BN>
 struct Smem {
+    static constexpr int kStages = stages_for<BN>();
     alignas(1024) __nv_bfloat16 a[kStages][kBM * kBK];
     alignas(1024) __nv_bfloat16 b[kStages][BN * kBK];
     uint64_t full[kStages];
@@ -139,9 +151,11 @@ struct Smem {
 template <int BN>
 __global__ void __launch_bounds__(kThreads, 1)
     gemm_bf16_kernel(const __grid_constant__ CUtensorMap map_a, const __grid_constant__ CUtensorMap map_b, int M,
-                     int N, int k_tiles_per_split, int k_tiles_total, const GemmEpilogue ep, int* __restrict__ error) {
+                     int N, int k_tiles_per_split, int k_tiles_total, const GemmEpilogue ep, int vec_ok,
+                     int* __restrict__ error) {
     extern __shared__ unsigned char smem_raw[];
     Smem<BN>* s = reinterpret_cast<Smem<BN>*>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
+    constexpr int kStages = Smem<BN>::kStages;
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const int m0 = blockIdx.x * kBM, n0 = blockIdx.y * BN;
     const int kt0 = blockIdx.z * k_tiles_per_split;
@@ -221,35 +235,106 @@ __global__ void __launch_bounds__(kThreads, 1)
 
     if (have) {
         const int row = m0 + warp * 32 + lane;
+        const bool row_in = row < M;
 #pragma unroll 1
         for (int c0 = 0; c0 < BN; c0 += 32) {
+            const int colb = n0 + c0;
+            if (colb >= N) break;  // the same for every thread of the CTA
             float v[32];
             tmem_ld32(tmem + (static_cast<uint32_t>(warp * 32) << 16) + static_cast<uint32_t>(c0), v);
+            const bool full = colb + 32 <= N;
+            if (ep.bias && blockIdx.z == 0) {
 #pragma unroll
-            for (int j = 0; j < 32; ++j) {
-                const int col = n0 + c0 + j;
-                float x = v[j];
-                const bool in = row < M && col < N;
-                if (in) {
-                    if (ep.bias && blockIdx.z == 0) x += ep.bias[col];
-                    if (ep.relu) x = fmaxf(x, 0.0f);
-                    if (ep.mask && !(__bfloat162float(ep.mask[static_cast<size_t>(row) * ep.ldm + col]) > 0.0f))
-                        x = 0.0f;
-                    const size_t o = static_cast<size_t>(row) * ep.ldc + col;
-                    if (ep.c) {
-                        if (ep.out_kind == 0) static_cast<float*>(ep.c)[o] = x;
-                        else if (ep.out_kind == 1) static_cast<__nv_bfloat16*>(ep.c)[o] = __float2bfloat16(x);
-                        else atomicAdd(static_cast<float*>(ep.c) + o, x);
+                for (int j = 0; j < 32; ++j)
+                    if (full || colb + j < N) v[j] += __ldg(ep.bias + colb + j);
+            }
+            if (ep.relu) {
+#pragma unroll
+                for (int j = 0; j < 32; ++j) v[j] = fmaxf(v[j], 0.0f);
+            }
+            if (ep.mask && row_in) {
+                const __nv_bfloat16* mrow = ep.mask + static_cast<size_t>(row) * ep.ldm + colb;
+                if (full && vec_ok) {  // 64 contiguous bytes of the lane's row
+#pragma unroll
+                    for (int q = 0; q < 4; ++q) {
+                        const uint4 m4 = __ldg(reinterpret_cast<const uint4*>(mrow) + q);
+                        const uint32_t w[4] = {m4.x, m4.y, m4.z, m4.w};
+#pragma unroll
+                        for (int e = 0; e < 4; ++e) {
+                            // (bits - 1) < 0x7F80: positive, from the smallest subnormal up to +inf
+                            const uint32_t lo = w[e] & 0xFFFFu, hi = w[e] >> 16;
+                            if (!(lo - 1u < 0x7F80u)) v[q * 8 + 2 * e] = 0.0f;
+                            if (!(hi - 1u < 0x7F80u)) v[q * 8 + 2 * e + 1] = 0.0f;
+                        }
                     }
-                    if (ep.ct) ep.ct[static_cast<size_t>(col) * ep.ldct + row] = __float2bfloat16(x);
                 } else {
-                    x = 0.0f;
-                }
-                if (ep.colsum) {  // column sums: the warp's 32 rows, then one atomic
 #pragma unroll
-                    for (int off = 16; off > 0; off >>= 1) x += __shfl_xor_sync(0xffffffffu, x, off);
-                    if (lane == 0 && col < N) atomicAdd(ep.colsum + col, x);
+                    for (int j = 0; j < 32; ++j)
+                        if (colb + j < N && !(__bfloat162float(mrow[j]) > 0.0f)) v[j] = 0.0f;
                 }
+            }
+            // values outside the matrix take no part in stores and column sums
+            if (!row_in) {
+#pragma unroll
+                for (int j = 0; j < 32; ++j) v[j] = 0.0f;
+            } else if (!full) {
+#pragma unroll
+                for (int j = 0; j < 32; ++j)
+                    if (colb + j >= N) v[j] = 0.0f;
+            }
+            if (ep.c && row_in) {
+                const size_t o = static_cast<size_t>(row) * ep.ldc + colb;
+                if (full && vec_ok) {  // 16-byte vector stores / reductions along the lane's row
+                    if (ep.out_kind == 0) {
+                        float4* d = reinterpret_cast<float4*>(static_cast<float*>(ep.c) + o);
+#pragma unroll
+                        for (int q = 0; q < 8; ++q) d[q] = make_float4(v[4 * q], v[4 * q + 1], v[4 * q + 2], v[4 * q + 3]);
+                    } else if (ep.out_kind == 1) {
+                        uint4* d = reinterpret_cast<uint4*>(static_cast<__nv_bfloat16*>(ep.c) + o);
+#pragma unroll
+                        for (int q = 0; q < 4; ++q) {
+                            uint32_t w[4];
+#pragma unroll
+                            for (int e = 0; e < 4; ++e) {
+                                const __nv_bfloat162 h = __floats2bfloat162_rn(v[q * 8 + 2 * e], v[q * 8 + 2 * e + 1]);
+                                w[e] = *reinterpret_cast<const uint32_t*>(&h);
+                            }
+                            d[q] = make_uint4(w[0], w[1], w[2], w[3]);
+                        }
+                    } else {
+                        float4* d = reinterpret_cast<float4*>(static_cast<float*>(ep.c) + o);
+#pragma unroll
+                        for (int q = 0; q < 8; ++q)
+                            atomicAdd(d + q, make_float4(v[4 * q], v[4 * q + 1], v[4 * q + 2], v[4 * q + 3]));
+                    }
+                } else {
+#pragma unroll
+                    for (int j = 0; j < 32; ++j) {
+                        if (colb + j >= N) continue;
+                        if (ep.out_kind == 0) static_cast<float*>(ep.c)[o + j] = v[j];
+                        else if (ep.out_kind == 1) static_cast<__nv_bfloat16*>(ep.c)[o + j] = __float2bfloat16(v[j]);
+                        else atomicAdd(static_cast<float*>(ep.c) + o + j, v[j]);
+                    }
+                }
+            }
+            if (ep.ct && row_in) {  // lanes hold consecutive rows: each store is one contiguous 64-byte run
+#pragma unroll
+                for (int j = 0; j < 32; ++j)
+                    if (full || colb + j < N) ep.ct[static_cast<size_t>(colb + j) * ep.ldct + row] = __float2bfloat16(v[j]);
+            }
+            if (ep.colsum) {
+                // transpose-reduce: after the five halving steps lane l holds the warp's sum of column l
+#pragma unroll
+                for (int o = 16; o >= 1; o >>= 1) {
+                    const bool upper = (lane & o) != 0;
+#pragma unroll
+                    for (int k = 0; k < o; ++k) {
+                        const float send = upper ? v[k] : v[k + o];
+                        const float keep = upper ? v[k + o] : v[k];
+                        v[k] = keep + __shfl_xor_sync(0xffffffffu, send, o);
+                    }
+                }
+                if (colb + lane < N) atomicAdd(ep.colsum + colb + lane, v[0]);
             }
         }
     }
@@ -293,15 +378,36 @@ bool make_map(CUtensorMap* map, const void* base, int rows, int cols, int ld, in
 
 template <int BN>
 cudaError_t launch_bn(const CUtensorMap& ma, const CUtensorMap& mb, int M, int N, int splits, int k_tiles,
-                      const GemmEpilogue& ep, int* error, cudaStream_t st) {
+                      const GemmEpilogue& ep, int vec_ok, int* error, cudaStream_t st) {
     const size_t smem = sizeof(Smem<BN>) + 1024;
-    cudaError_t e = cudaFuncSetAttribute(gemm_bf16_kernel<BN>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                         static_cast<int>(smem));
+    int dev = 0;
+    cudaError_t e = cudaGetDevice(&dev);
     if (e != cudaSuccess) return e;
+    static std::atomic<unsigned long long> configured{0};  // one bit per device
+    const unsigned long long bit = 1ull << (dev & 63);
+    if (!(configured.load() & bit)) {
+        e = cudaFuncSetAttribute(gemm_bf16_kernel<BN>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 static_cast<int>(smem));
+        if (e != cudaSuccess) return e;
+        configured.fetch_or(bit);
+    }
     const int per = (k_tiles + splits - 1) / splits;
-    dim3 grid((M + kBM - 1) / kBM, (N + BN - 1) / BN, splits);
-    gemm_bf16_kernel<BN><<<grid, kThreads, smem, st>>>(ma, mb, M, N, per, k_tiles, ep, error);
+    dim3 grid((M + kBM - 1) / kBM, (N + BN - 1) / BN, (k_tiles + per - 1) / per);
+    gemm_bf16_kernel<BN><<<grid, kThreads, smem, st>>>(ma, mb, M, N, per, k_tiles, ep, vec_ok, error);
     return cudaGetLastError();
+}
+
+int sm_count() {
+    static std::atomic<int> cached{0};
+    int n = cached.load();
+    if (n == 0) {
+        int dev = 0;
+        if (cudaGetDevice(&dev) != cudaSuccess ||
+            cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess || n <= 0)
+            n = 148;
+        cached.store(n);
+    }
+    return n;
 }
 
 }  // namespace
@@ -309,21 +415,44 @@ cudaError_t launch_bn(const CUtensorMap& ma, const CUtensorMap& mb, int M, int N
 // C = A * B^T on the tensor cores with the epilogue ep; see the file comment.
 // lda / ldb in elements; A's and B's rows must start on 16-byte boundaries
 // (lda, ldb multiples of 8) and K a multiple of 64.  splits > 1 splits K
-// across CTAs and allows only the atomic FP32 output (out_kind 2).
+// across CTAs and allows only the atomic FP32 output (out_kind 2); splits = 0
+// chooses the split for about two CTAs per SM.
 cudaError_t gemm_bf16_ep(const void* A, int lda, const void* B, int ldb, int M, int N, int K, const GemmEpilogue& ep,
                          int splits, int* error, cudaStream_t st) {
-    if (M <= 0 || N <= 0 || K <= 0 || K % kBK || lda % 8 || ldb % 8 ||
-        (splits > 1 && (ep.out_kind != 2 || ep.ct || ep.mask || ep.colsum || ep.relu)) ||
+    if (M <= 0 || N <= 0 || K <= 0 || K % kBK || lda % 8 || ldb % 8 || splits < 0 ||
+        (splits != 1 && (ep.out_kind != 2 || ep.ct || ep.mask || ep.colsum || ep.relu)) ||
         (reinterpret_cast<uintptr_t>(A) & 15) || (reinterpret_cast<uintptr_t>(B) & 15))
         return cudaErrorInvalidValue;
-    const int bn = N <= 64 ? 64 : (N <= 128 ? 128 : 256);
+    const int k_tiles = K / kBK;
+    const int tiles_m = (M + kBM - 1) / kBM;
+    const int sms = sm_count();
+    // widest tile that still gives every SM a CTA (the GEMMs here are small), at most what N needs
+    auto ctas = [&](int bn, int sp) { return static_cast<long long>(tiles_m) * ((N + bn - 1) / bn) * sp; };
+    const int sp1 = splits == 0 ? 1 : splits;
+    int bn = 64;
+    for (int cand : {256, 128}) {
+        if (cand < 2 * N && ctas(cand, sp1) >= sms) {
+            bn = cand;
+            break;
+        }
+    }
+    if (splits == 0) {  // split K to about two CTAs per SM, at least 4 K slices each
+        const long long t = ctas(bn, 1);
+        long long sp = (2ll * sms + t - 1) / t;
+        sp = std::min<long long>(sp, std::max(1, k_tiles / 4));
+        splits = static_cast<int>(std::max<long long>(1, sp));
+    }
+    splits = splits > k_tiles ? k_tiles : splits;
     CUtensorMap ma, mb;
     if (!make_map(&ma, A, M, K, lda, kBM) || !make_map(&mb, B, N, K, ldb, bn)) return cudaErrorInvalidValue;
-    const int k_tiles = K / kBK;
-    splits = splits < 1 ? 1 : (splits > k_tiles ? k_tiles : splits);
-    if (bn == 64) return launch_bn<64>(ma, mb, M, N, splits, k_tiles, ep, error, st);
-    if (bn == 128) return launch_bn<128>(ma, mb, M, N, splits, k_tiles, ep, error, st);
-    return launch_bn<256>(ma, mb, M, N, splits, k_tiles, ep, error, st);
+    // 16-byte vector access along a row of C and of the mask
+    const size_t esz = ep.out_kind == 1 ? 2 : 4;
+    int vec_ok = 1;
+    if (ep.c && ((reinterpret_cast<uintptr_t>(ep.c) & 15) || (static_cast<size_t>(ep.ldc) * esz) % 16)) vec_ok = 0;
+    if (ep.mask && ((reinterpret_cast<uintptr_t>(ep.mask) & 15) || ep.ldm % 8)) vec_ok = 0;
+    if (bn == 64) return launch_bn<64>(ma, mb, M, N, splits, k_tiles, ep, vec_ok, error, st);
+    if (bn == 128) return launch_bn<128>(ma, mb, M, N, splits, k_tiles, ep, vec_ok, error, st);
+    return launch_bn<256>(ma, mb, M, N, splits, k_tiles, ep, vec_ok, error, st);
 }
 
 cudaError_t gemm_bf16(const void* A, int lda, const void* B, int ldb, void* C, int ldc, int M, int N, int K,

@@ -964,4 +964,180 @@ ntp_status ntp_calc_time_residual(ntp_ctx* ctx, const ntp_hit* hits, uint64_t n,
     return NTP_OK;
 }
 
+
+ntp_status ntp_make_table(ntp_ctx* ctx, const ntp_hit* hits, uint64_t n, const double* weight,
+                          const ntp_source* sims, const float* sim_log10_energy, const double* sim_weight_scale,
+                          const double* orientations, const ntp_table_spec* spec, float* cond, float* tres, float* nhits, int32_t* has_time,
+                          uint64_t capacity, uint64_t* n_rows, float* group_cond, double* group_expec,
+                          uint64_t* group_count, void* stream) {
+    if (!ctx) return NTP_ERR_INVALID;
+    if (n_rows) *n_rows = 0;
+    if (!ctx->have_targets) {
+        ctx->err = "ntp_make_table: targets must be set first";
+        return NTP_ERR_NOT_READY;
+    }
+    if (!spec || !sims || !sim_log10_energy || !orientations) return invalid(ctx, "ntp_make_table: NULL argument");
+    if (ctx->n_tgt != 1 || ctx->targets[0].kind != NTP_TARGET_MULTI_PMT || ctx->targets[0].n_pmts < 1)
+        return invalid(ctx, "ntp_make_table: the context must hold exactly one MULTI_PMT module");
+    if (spec->n_sims < 1 || spec->n_orientations < 1 || spec->max_rows_per_group < 1 || !(spec->downsample >= 0.0) ||
+        !(spec->n800 > 0.0f))
+        return invalid(ctx, "ntp_make_table: need n_sims, n_orientations, max_rows_per_group >= 1, downsample >= 0, "
+                            "n800 > 0");
+    if (n > 0 && (!hits || !weight)) return invalid(ctx, "ntp_make_table: NULL hits or weights");
+    const ntp_target& mod = ctx->targets[0];
+    const int S = spec->n_sims, R = spec->n_orientations, P = mod.n_pmts;
+    const long long G = static_cast<long long>(S) * R * P;
+    if (G > (1ll << 26)) return invalid(ctx, "ntp_make_table: too many (simulation, orientation, PMT) groups");
+    cudaSetDevice(ctx->device);
+    cudaStream_t st = pick_stream(ctx, stream);
+    const uint2 key = make_uint2(static_cast<uint32_t>(spec->seed), static_cast<uint32_t>(spec->seed >> 32));
+    const size_t g = static_cast<size_t>(G);
+
+    // host: PMT axes per (simulation, orientation), group features, tgeo per simulation
+    std::vector<float> axes(3 * g), gcond(5 * g);
+    std::vector<double> tgeo(S);
+    std::vector<double> pm(3 * static_cast<size_t>(P));
+    for (int j = 0; j < P; ++j) {  // module-frame axes as in ntp_make_hits
+        const float th = ctx->pmt_coords[2 * (mod.pmt_offset + j)], ph = ctx->pmt_coords[2 * (mod.pmt_offset + j) + 1];
+        const float s_t = sinf(th), c_t = cosf(th), s_p = sinf(ph), c_p = cosf(ph);
+        pm[3 * j] = static_cast<double>(c_p * s_t);
+        pm[3 * j + 1] = static_cast<double>(s_p * s_t);
+        pm[3 * j + 2] = static_cast<double>(c_t);
+    }
+    const double c_vac = 0.299792458, two_pi = 6.283185307179586;
+    for (int si = 0; si < S; ++si) {
+        const ntp_source& src = sims[si];
+        double u[3] = {static_cast<double>(src.position[0]) - mod.position[0],
+                       static_cast<double>(src.position[1]) - mod.position[1],
+                       static_cast<double>(src.position[2]) - mod.position[2]};
+        const double d = std::sqrt(u[0] * u[0] + u[1] * u[1] + u[2] * u[2]);
+        if (!(d > 0.0)) return invalid(ctx, "ntp_make_table: a simulation's source sits at the module centre");
+        for (double& x : u) x /= d;
+        {  // calc_time_residual!: (|src - module| - R) / (c / n800), with the Float32 distance
+            const float dx = src.position[0] - mod.position[0], dy = src.position[1] - mod.position[1],
+                        dz = src.position[2] - mod.position[2];
+            const float df = std::sqrt(dx * dx + dy * dy + dz * dz);
+            tgeo[si] = static_cast<double>(df - mod.radius) / (c_vac / static_cast<double>(spec->n800));
+        }
+        const double v[3] = {src.direction[0], src.direction[1], src.direction[2]};
+        const double vu = v[0] * u[0] + v[1] * u[1] + v[2] * u[2];
+        const double e1[3] = {v[0] - vu * u[0], v[1] - vu * u[1], v[2] - vu * u[2]};
+        for (int r = 0; r < R; ++r) {
+            const double* O = orientations + (static_cast<size_t>(si) * R + r) * 9;
+            for (int j = 0; j < P; ++j) {
+                const size_t gi = (static_cast<size_t>(si) * R + r) * P + j;
+                double a[3];
+                for (int k = 0; k < 3; ++k) a[k] = O[3 * k] * pm[3 * j] + O[3 * k + 1] * pm[3 * j + 1] + O[3 * k + 2] * pm[3 * j + 2];
+                for (int k = 0; k < 3; ++k) axes[3 * gi + k] = static_cast<float>(a[k]);
+                const double au = a[0] * u[0] + a[1] * u[1] + a[2] * u[2];
+                const double e2[3] = {a[0] - au * u[0], a[1] - au * u[1], a[2] - au * u[2]};
+                const double cr[3] = {e1[1] * e2[2] - e1[2] * e2[1], e1[2] * e2[0] - e1[0] * e2[2],
+                                      e1[0] * e2[1] - e1[1] * e2[0]};
+                double phi = std::atan2(cr[0] * u[0] + cr[1] * u[1] + cr[2] * u[2],
+                                        e1[0] * e2[0] + e1[1] * e2[1] + e1[2] * e2[2]);
+                if (phi < 0.0) phi += two_pi;
+                float* f = &gcond[5 * gi];
+                f[0] = static_cast<float>(2.0 * std::log(d) / std::log(200.0) - 1.0);
+                f[1] = static_cast<float>(vu);
+                f[2] = static_cast<float>(au);
+                f[3] = static_cast<float>(phi / M_PI - 1.0);
+                f[4] = static_cast<float>((static_cast<double>(sim_log10_energy[si]) - 4.0) / 2.0);
+            }
+        }
+    }
+    const float cos_open = static_cast<float>(std::cos(std::asin(std::sqrt(mod.pmt_area / static_cast<float>(M_PI)) /
+                                                                 mod.radius)));
+    const float3 center = make_float3(mod.position[0], mod.position[1], mod.position[2]);
+
+    // phase 1 scratch: axes f32[3G] | gcond f32[5G] | tgeo f64[S] | tres f64[n] | wsum f64[G] |
+    //                  npos, nall, nsel, fill u64[G] | start, ostart, want u64[G+1]
+    size_t off = 0;
+    auto take = [&](size_t bytes) { size_t o = off; off += (bytes + 255) / 256 * 256; return o; };
+    const size_t o_axes = take(4 * 3 * g), o_gcond = take(4 * 5 * g), o_tgeo = take(8 * S), o_tres = take(8 * n);
+    const size_t o_scale = take(8 * S);
+    const size_t o_wsum = take(8 * g), o_npos = take(8 * g), o_nall = take(8 * g), o_nsel = take(8 * g);
+    const size_t o_fill = take(8 * g), o_start = take(8 * (g + 1)), o_ostart = take(8 * (g + 1));
+    const size_t o_want = take(8 * (g + 1));
+    NTP_CUDA(ctx, ensure(ctx->d_scratch, ctx->scratch_bytes, off));
+    unsigned char* sc = static_cast<unsigned char*>(ctx->d_scratch);
+    auto u64p = [&](size_t o) { return reinterpret_cast<unsigned long long*>(sc + o); };
+    float* d_axes = reinterpret_cast<float*>(sc + o_axes);
+    float* d_gcond = reinterpret_cast<float*>(sc + o_gcond);
+    double* d_tgeo = reinterpret_cast<double*>(sc + o_tgeo);
+    double* d_tres = reinterpret_cast<double*>(sc + o_tres);
+    double* d_wsum = reinterpret_cast<double*>(sc + o_wsum);
+    NTP_CUDA(ctx, cudaMemcpyAsync(d_axes, axes.data(), 4 * 3 * g, cudaMemcpyHostToDevice, st));
+    NTP_CUDA(ctx, cudaMemcpyAsync(d_gcond, gcond.data(), 4 * 5 * g, cudaMemcpyHostToDevice, st));
+    NTP_CUDA(ctx, cudaMemcpyAsync(d_tgeo, tgeo.data(), 8 * S, cudaMemcpyHostToDevice, st));
+    std::vector<double> scale(S, 1.0);
+    if (sim_weight_scale) scale.assign(sim_weight_scale, sim_weight_scale + S);
+    double* d_scale = reinterpret_cast<double*>(sc + o_scale);
+    NTP_CUDA(ctx, cudaMemcpyAsync(d_scale, scale.data(), 8 * S, cudaMemcpyHostToDevice, st));
+    NTP_CUDA(ctx, cudaMemsetAsync(sc + o_wsum, 0, o_start - o_wsum, st));  // wsum, npos, nall, nsel, fill
+    NTP_CUDA(ctx, ntp::launch_table_count(hits, n, weight, d_scale, S, R, P, center, d_axes, cos_open, d_wsum, u64p(o_npos),
+                                          u64p(o_nall), st));
+    // the group count N = Poisson(sum(w) * downsample), not capped by the simulated hits (the
+    // oversampling factor may be below 1); the no-cap bound goes through the draw's cap argument
+    NTP_CUDA(ctx, cudaMemsetAsync(u64p(o_want), 0xFF, 8 * (g + 1), st));
+    NTP_CUDA(ctx, ntp::launch_resample_draw(static_cast<int>(G), d_wsum, u64p(o_want), spec->downsample, key,
+                                            u64p(o_nsel), st));
+    std::vector<unsigned long long> nall(g), npos(g), nsel(g), start(g + 1), ostart(g + 1), want(g + 1, 0);
+    NTP_CUDA(ctx, cudaMemcpyAsync(npos.data(), u64p(o_npos), 8 * g, cudaMemcpyDeviceToHost, st));
+    std::vector<double> wsum(g);
+    NTP_CUDA(ctx, cudaMemcpyAsync(nall.data(), u64p(o_nall), 8 * g, cudaMemcpyDeviceToHost, st));
+    NTP_CUDA(ctx, cudaMemcpyAsync(nsel.data(), u64p(o_nsel), 8 * g, cudaMemcpyDeviceToHost, st));
+    if (group_expec) NTP_CUDA(ctx, cudaMemcpyAsync(wsum.data(), d_wsum, 8 * g, cudaMemcpyDeviceToHost, st));
+    NTP_CUDA(ctx, cudaStreamSynchronize(st));
+    std::vector<int32_t> zero;
+    start[0] = ostart[0] = 0;
+    const unsigned long long cap_rows = static_cast<unsigned long long>(spec->max_rows_per_group);
+    for (size_t i = 0; i < g; ++i) {
+        start[i + 1] = start[i] + nall[i];
+        want[i] = std::min(std::min(nsel[i], cap_rows), npos[i]);
+        ostart[i + 1] = ostart[i] + want[i];
+        if (nsel[i] == 0 && spec->zero_rows) zero.push_back(static_cast<int32_t>(i));
+    }
+    const unsigned long long pairs = start[g], hit_rows = ostart[g], total = hit_rows + zero.size();
+    if (n_rows) *n_rows = total;
+    if (total > capacity) {
+        ctx->err = "ntp_make_table: capacity " + std::to_string(capacity) + " below " + std::to_string(total) + " rows";
+        return NTP_ERR_OVERFLOW;
+    }
+    if (total > 0 && (!cond || !tres || !nhits || !has_time)) return invalid(ctx, "ntp_make_table: NULL output");
+    // phase 2 scratch: order, okey u64[pairs] | og i32[rows] | ot f64[rows] | oh u64[rows] | zero i32[nz]
+    size_t off2 = 0;
+    auto take2 = [&](size_t bytes) { size_t o = off2; off2 += (bytes + 255) / 256 * 256; return o; };
+    const size_t o_order = take2(8 * pairs), o_okey = take2(8 * pairs), o_og = take2(4 * hit_rows);
+    const size_t o_ot = take2(8 * hit_rows), o_oh = take2(8 * hit_rows), o_zero = take2(4 * zero.size());
+    NTP_CUDA(ctx, ensure(ctx->d_stage2, ctx->stage2_bytes, off2));
+    unsigned char* s2 = static_cast<unsigned char*>(ctx->d_stage2);
+    auto u64q = [&](size_t o) { return reinterpret_cast<unsigned long long*>(s2 + o); };
+    NTP_CUDA(ctx, cudaMemcpyAsync(u64p(o_start), start.data(), 8 * (g + 1), cudaMemcpyHostToDevice, st));
+    NTP_CUDA(ctx, cudaMemcpyAsync(u64p(o_ostart), ostart.data(), 8 * (g + 1), cudaMemcpyHostToDevice, st));
+    NTP_CUDA(ctx, cudaMemcpyAsync(u64p(o_want), want.data(), 8 * (g + 1), cudaMemcpyHostToDevice, st));
+    if (!zero.empty())
+        NTP_CUDA(ctx, cudaMemcpyAsync(s2 + o_zero, zero.data(), 4 * zero.size(), cudaMemcpyHostToDevice, st));
+    if (pairs > 0) {
+        NTP_CUDA(ctx, ntp::launch_table_bucket(hits, n, weight, d_scale, S, R, P, center, d_axes, cos_open, key, u64p(o_start),
+                                               u64p(o_fill), u64q(o_order), u64q(o_okey), st));
+        NTP_CUDA(ctx, ntp::launch_table_tres(hits, n, d_tgeo, S, d_tres, st));
+        NTP_CUDA(ctx, ntp::launch_resample_select(static_cast<int>(G), hits, d_tres, u64p(o_start), u64p(o_nall),
+                                                  u64p(o_want), u64p(o_ostart), u64q(o_order), u64q(o_okey),
+                                                  reinterpret_cast<int32_t*>(s2 + o_og),
+                                                  reinterpret_cast<double*>(s2 + o_ot), u64q(o_oh), st));
+    }
+    NTP_CUDA(ctx, ntp::launch_table_rows(hit_rows, reinterpret_cast<const int32_t*>(s2 + o_og),
+                                         reinterpret_cast<const double*>(s2 + o_ot), zero.size(),
+                                         reinterpret_cast<const int32_t*>(s2 + o_zero), u64p(o_nsel), d_gcond, cond,
+                                         tres, nhits, has_time, st));
+    if (group_cond) NTP_CUDA(ctx, cudaMemcpyAsync(group_cond, d_gcond, 4 * 5 * g, cudaMemcpyDeviceToDevice, st));
+    if (group_count) NTP_CUDA(ctx, cudaMemcpyAsync(group_count, u64p(o_nsel), 8 * g, cudaMemcpyDeviceToDevice, st));
+    if (group_expec) {
+        for (double& w : wsum) w *= spec->downsample;
+        NTP_CUDA(ctx, cudaMemcpyAsync(group_expec, wsum.data(), 8 * g, cudaMemcpyHostToDevice, st));
+    }
+    NTP_CUDA(ctx, cudaStreamSynchronize(st));
+    return NTP_OK;
+}
+
 }  // extern "C"

@@ -154,6 +154,21 @@ cudaError_t gemm_bf16_ep(const void* A, int lda, const void* B, int ldb, int M, 
 cudaError_t gemm_bf16(const void* A, int lda, const void* B, int ldb, void* C, int ldc, int M, int N, int K,
                       const float* bias, int relu, int out_kind, int splits, int* error, cudaStream_t st);
 
+// training-table generator passes (tables.cu)
+cudaError_t launch_table_count(const ntp_hit* hits, unsigned long long n, const double* w, const double* scale,
+                               int n_sims, int R, int P, float3 center, const float* axes, float cos_open,
+                               double* wsum, unsigned long long* npos, unsigned long long* nall, cudaStream_t st);
+cudaError_t launch_table_bucket(const ntp_hit* hits, unsigned long long n, const double* w, const double* scale,
+                                int n_sims, int R, int P, float3 center, const float* axes, float cos_open, uint2 key,
+                                const unsigned long long* start, unsigned long long* fill, unsigned long long* order,
+                                unsigned long long* okey, cudaStream_t st);
+cudaError_t launch_table_tres(const ntp_hit* hits, unsigned long long n, const double* tgeo, int n_sims, double* tres,
+                              cudaStream_t st);
+cudaError_t launch_table_rows(unsigned long long n_hit_rows, const int32_t* og, const double* ot,
+                              unsigned long long n_zero, const int32_t* zero_groups, const unsigned long long* ndraw,
+                              const float* gcond, float* cond, float* tres, float* nhits, int32_t* has_time,
+                              cudaStream_t st);
+
 // resample_simulation passes (resample.cu)
 cudaError_t launch_resample_group(const ntp_hit* hits, unsigned long long n, const int32_t* pmt, const double* w,
                                   const uint2* sorted_ids, int n_targets, int max_pmts, int32_t* group, double* wsum,

@@ -180,6 +180,54 @@ class RQNormFlow:
                     return losses
         return losses
 
+    def init_output_bias(self, *, shift: float | None = None, log_expec: float | None = None) -> None:
+        """Sets the output-layer biases of the shift and of the log
+        expectation (a start near the data's scale; Adam at lr 1e-3 moves a
+        bias by about lr per step)."""
+        th = self.get_params()
+        off = dict((name, o) for name, _, o in self.layout())["b4"]
+        base = self.n_layers * (3 * self.K + 1)
+        if shift is not None:
+            th[off + base] = shift
+        if log_expec is not None:
+            th[off + base + 2] = log_expec
+        self.set_params(th)
+
+    def init_from_table(self, table) -> None:
+        """init_output_bias from a FlowTable: the median time residual of
+        its timed rows and the mean of log(N + 1) over its groups (a typical
+        count; the counts span many decades)."""
+        import torch
+        t = table.tres[table.has_time.bool()]
+        shift = float(torch.median(t).item()) if t.numel() else 0.0
+        log_n = float(torch.log1p(table.group_count.double()).mean().item())
+        self.init_output_bias(shift=shift, log_expec=log_n)
+
+    def fit_table(self, table, *, epochs: int = 1, batch_size: int | None = None, seed: int = 0,
+                  max_steps: int | None = None) -> list[float]:
+        """Trains on a FlowTable held in device memory: the rows are shuffled
+        on the device once per epoch and fed to the training step batch by
+        batch without leaving the GPU; returns the per-step losses."""
+        import torch
+        n = len(table)
+        bs = int(batch_size or self.hparams.batch_size)
+        bs = max(128, min(bs, self.batch_capacity) // 128 * 128)
+        gen = torch.Generator(device=table.tres.device)
+        gen.manual_seed(int(seed))
+        losses: list[float] = []
+        for _ in range(epochs):
+            perm = torch.randperm(n, device=table.tres.device, generator=gen)
+            cond = table.cond[perm].contiguous()
+            tres = table.tres[perm].contiguous()
+            nh = table.nhits[perm].contiguous()
+            has = table.has_time[perm].contiguous()
+            torch.cuda.synchronize()
+            for s in range(0, n - bs + 1, bs):
+                losses.append(self.train_step(cond[s:s + bs], tres[s:s + bs], nh[s:s + bs], has[s:s + bs]))
+                if max_steps is not None and len(losses) >= max_steps:
+                    return losses
+        return losses
+
     # --------------------------------------------------------------- inference
     def forward_params(self, cond) -> np.ndarray:
         """The conditioner's raw outputs [n x n_outputs] (spline parameters,

@@ -29,6 +29,10 @@ import torch
 
 F = torch.nn.functional
 DT = torch.float64
+# the kernels' FP32 range guards: log expectation within [-30, 30], raw scale
+# within [-20, 20] (held, zero gradient outside); inactive for ordinary values
+LE_CLAMP = 30.0
+SCALE_CLAMP = 20.0
 
 
 def normalize_bin_sizes(u: torch.Tensor, total: float, min_bin: float = 1e-4) -> torch.Tensor:
@@ -138,7 +142,7 @@ def flow_logpdf(y, raw, n_layers: int, r0: float, r1: float, K: int | None = Non
         cur, ld = inv_rqs_univariate(xp, yp, d, cur)
         ldsum = ldsum + ld
     shift = raw[:, L * NP]
-    scale = torch.sigmoid(raw[:, L * NP + 1]) * 100.0
+    scale = torch.sigmoid(torch.clamp(raw[:, L * NP + 1], -SCALE_CLAMP, SCALE_CLAMP)) * 100.0
     normal = -torch.log(scale) - 0.5 * (math.log(2 * math.pi) + ((cur - shift) / scale) ** 2)
     return normal + ldsum
 
@@ -146,7 +150,7 @@ def flow_logpdf(y, raw, n_layers: int, r0: float, r1: float, K: int | None = Non
 def head_loss(raw, tres, nhits, has_time, L: int, K: int, r0: float, r1: float):
     """Batch-mean loss of raw outputs [B x (L(3K+1)+3)] (log expectation last)."""
     NP = 3 * K + 1
-    le = raw[:, L * NP + 2]
+    le = torch.clamp(raw[:, L * NP + 2], -LE_CLAMP, LE_CLAMP)
     n = nhits
     poiss = n * le - torch.exp(le) - torch.lgamma(n + 1.0)
     lp = flow_logpdf(tres, raw, L, r0, r1, K)
