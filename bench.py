@@ -59,6 +59,7 @@ def parse():
     ap.add_argument("--e2e-steps", type=int, default=3)
     ap.add_argument("--serving-requests", type=int, default=4096,
                     help="requests of the serving measurement (0 = skip)")
+    ap.add_argument("--flow", type=int, default=1, help="1: include the flow surrogate measurement")
     ap.add_argument("--small", action="store_true",
                     help="profiling case: one cascade at 1% of its photons, 64 MB hit buffer, 256 MB L2 flush")
     return ap.parse_args()
@@ -173,6 +174,105 @@ def serving_bench(n_requests: int, budget_bytes: int = 120 * 10 ** 9) -> dict:
     srv.close()
     setup.close()
     return out
+
+
+def flow_bench(train_steps: int = 300, n_tuples: int = 100_000_000) -> dict:
+    """Flow surrogate workload (5 spline layers of 12 bins on [-20, 1500] ns,
+    3 x 256 conditioner, count head, batch 8192, Adam 1e-3):
+      table      -- the MC kernel generates a training table (8192 simulations,
+                    distance 1-200 m log-uniform, direction isotropic, log10 E
+                    2-6, 16 module orientations each) on the device;
+      training   -- train_step on rows of that table already in HBM;
+                    samples/s and the conditioner GEMMs' tensor throughput
+                    (algorithmic FLOPs: 3 x forward, forward = 2 x (5 x 256 +
+                    2 x 256 x 256 + 256 x 188) per sample);
+      inference  -- 1e8 (condition, time) log-pdf tuples over 128000 PMT
+                    conditions (8000 modules x 16 PMTs), inputs in HBM; and
+                    the same through host buffers (e2e)."""
+    import numpy as np
+    import torch
+
+    from neutrinotelescopes_gb300.flow import RQNormFlow, RQNormFlowHParams
+    from neutrinotelescopes_gb300.tables import TableConfig, make_flow_table
+
+    out = {"model": "5 x RQ spline (12 bins, [-20, 1500] ns) + affine normal + count head, 3 x 256 ReLU "
+                    "conditioner on 5 features, BF16 weights / FP32 accumulate and master weights"}
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    tab = make_flow_table(TableConfig(n_sims=8192, n_orientations=16, target_hits=300, max_photons=10_000_000,
+                                      seed=1))
+    torch.cuda.synchronize()
+    dt = time.perf_counter() - t0
+    out["table"] = {"simulations": 8192, "orientations": 16, "rows": len(tab), "photons": tab.n_photons,
+                    "seconds": dt, "rows_per_s": len(tab) / dt, "photons_per_s": tab.n_photons / dt}
+    bs = 8192
+    fl = RQNormFlow(RQNormFlowHParams(batch_size=bs))
+    fl.init_from_table(tab)
+    perm = torch.randperm(len(tab), device="cuda")
+    cond, tres = tab.cond[perm].contiguous(), tab.tres[perm].contiguous()
+    nh, has = tab.nhits[perm].contiguous(), tab.has_time[perm].contiguous()
+    torch.cuda.synchronize()
+    nb = len(tab) // bs
+
+    def tstep(i):
+        s = (i % nb) * bs
+        return fl.train_step(cond[s:s + bs], tres[s:s + bs], nh[s:s + bs], has[s:s + bs])
+
+    for i in range(20):
+        tstep(i)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    losses = [tstep(20 + i) for i in range(train_steps)]
+    torch.cuda.synchronize()
+    dt = time.perf_counter() - t0
+    fwd_flops = 2 * (5 * 256 + 2 * 256 * 256 + 256 * 188)
+    step_flops = 3 * fwd_flops * bs
+    peak = _measured_peak("bf16_tflops_sustained", 1700.0)
+    ach = step_flops * train_steps / dt / 1e12
+    out["training"] = {"batch": bs, "steps": train_steps, "ms_per_step": dt / train_steps * 1e3,
+                       "samples_per_s": bs * train_steps / dt,
+                       "loss_first_last": [float(losses[0]), float(np.nanmean(losses[-20:]))],
+                       "roofline": {"bound": "tensor", "achieved": ach, "peak": peak[0], "unit": "TFLOP/s",
+                                    "frac": ach / peak[0], "peak_source": peak[1],
+                                    "flops_per_step": step_flops}}
+    # inference: 1e8 tuples over 128000 conditions
+    n_cond = 8000 * 16
+    g = torch.Generator(device="cuda").manual_seed(5)
+    c = (torch.rand((n_cond, 5), device="cuda", generator=g) * 2 - 1).contiguous()
+    idx = torch.randint(0, n_cond, (n_tuples,), device="cuda", dtype=torch.int32, generator=g)
+    idx, _ = torch.sort(idx)
+    tt = (torch.rand(n_tuples, device="cuda", generator=g) * 300.0 - 20.0).contiguous()
+    fl.logpdf(c, idx[:1000], tt[:1000])
+    torch.cuda.synchronize()
+    reps = 3
+    t0 = time.perf_counter()
+    for _ in range(reps):
+        lp = fl.logpdf(c, idx, tt)
+    torch.cuda.synchronize()
+    dt = (time.perf_counter() - t0) / reps
+    bytes_per = 4 + 4 + 4
+    out["inference"] = {"tuples": n_tuples, "conditions": n_cond, "seconds": dt, "tuples_per_s": n_tuples / dt,
+                        "finite": bool(torch.isfinite(lp).all().item()),
+                        "hbm_gbs": n_tuples * bytes_per / dt / 1e9,
+                        "note": "time includes the conditioner pass over the 128000 conditions"}
+    hc, hi, ht = c.cpu().numpy(), idx.cpu().numpy(), tt.cpu().numpy()
+    t0 = time.perf_counter()
+    fl.logpdf(hc, hi, ht)
+    dt = time.perf_counter() - t0
+    out["inference"]["e2e"] = {"tuples_per_s": n_tuples / dt, "seconds": dt,
+                               "h2d_bytes": int(hc.nbytes + hi.nbytes + ht.nbytes), "d2h_bytes": 4 * n_tuples}
+    fl.close()
+    del tab, cond, tres, nh, has, c, idx, tt, lp
+    torch.cuda.empty_cache()
+    return out
+
+
+def _measured_peak(key: str, fallback: float):
+    try:
+        v = json.loads((ROOT / "MEASURED_PEAKS.json").read_text())[key]
+        return float(v), f"MEASURED_PEAKS.json {key} (measured)"
+    except Exception:
+        return fallback, "fallback"
 
 
 def dist_setup():
@@ -359,6 +459,8 @@ def main():
     torch.cuda.empty_cache()
     if args.serving_requests > 0 and not args.small:
         out["serving"] = serving_bench(args.serving_requests)
+    if args.flow and not args.small and rank == 0:
+        out["flow"] = flow_bench()
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         out["cpu_baseline"] = cpu_baseline(workloads.cascade_string_setup(N_CASCADES, WORKLOAD_SEED),
                                            args.cpu_seconds, os.cpu_count() or 1)

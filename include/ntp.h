@@ -331,16 +331,19 @@ ntp_status ntp_resample(ntp_ctx* ctx, const ntp_hit* hits, uint64_t n_hits, cons
  * N = Poisson(sum(w) * downsample) is not capped by the number of simulated
  * hits (with weights scaled up, fewer photons than the source's may have
  * been simulated); min(N, #hits with w > 0, max_rows_per_group) hits are
- * drawn without replacement, each a row: cond[5] (the group's condition
+ * drawn without replacement (see the cap below), each a row: cond[5] (the group's condition
  * features), tres (hit time minus (|source - module| - R) n800 / c,
- * calc_time_residual!), nhits = N, has_time = 1.  With zero_rows a group
- * with N = 0 gives one row with has_time = 0, nhits = 0.  Condition features of a group
+ * calc_time_residual!), nhits = N, has_time = 1, row_group (may be NULL) =
+ * the group's index.  With zero_rows a group with N = 0 gives one row with
+ * has_time = 0, nhits = 0.  The rows drawn from a group are also capped at a
+ * quarter of its effective sample size (sum w)^2 / sum w^2 plus one, so that
+ * they stay a weighted sample when N approaches the simulated hits.  Condition features of a group
  * (u = unit vector module -> source, a = PMT axis, v = source direction):
  * 2 ln(d)/ln(200) - 1, v.u, a.u, phi/pi - 1 with phi in [0, 2 pi) the angle
  * from the projection of v to that of a on the plane normal to u (around u),
  * (log10 E - 4)/2.  Outputs are device buffers; the group outputs (n_sims * R
  * * n_pmts entries: features, expected count sum(w) * downsample, drawn
- * count) may be NULL.  *n_rows receives the row count; above capacity
+ * count, simulated hits with w > 0) may be NULL.  *n_rows receives the row count; above capacity
  * nothing is written and NTP_ERR_OVERFLOW returned. */
 typedef struct ntp_table_spec {
     int32_t n_sims;             /* simulations = sources of the propagation launch          */
@@ -355,9 +358,10 @@ typedef struct ntp_table_spec {
 
 ntp_status ntp_make_table(ntp_ctx* ctx, const ntp_hit* hits, uint64_t n_hits, const double* weight,
                           const ntp_source* sims, const float* sim_log10_energy, const double* sim_weight_scale,
-                          const double* orientations, const ntp_table_spec* spec, float* cond, float* tres, float* nhits, int32_t* has_time,
-                          uint64_t capacity, uint64_t* n_rows, float* group_cond, double* group_expec,
-                          uint64_t* group_count, void* stream);
+                          const double* orientations, const ntp_table_spec* spec, float* cond, float* tres,
+                          float* nhits, int32_t* has_time, int32_t* row_group, uint64_t capacity, uint64_t* n_rows,
+                          float* group_cond, double* group_expec, uint64_t* group_count, uint64_t* group_hits,
+                          void* stream);
 
 /* ------------------------------------------------------------ tensor cores
  * C = A * B^T with BF16 A [M x K] and B [N x K] (row-major, K contiguous,
@@ -392,6 +396,7 @@ typedef struct ntp_flow_config {
     int32_t n_bins;         /* K, bins per spline: 10 (the reference's default) or 12        */
     float t_min, t_max;     /* spline range (ns); linear tails outside                        */
     float lr, beta1, beta2, eps; /* Adam                                                      */
+    float grad_clip;        /* per-sample bound on |dL/draw outputs| x batch (0 = none), e.g. 1e3 */
     uint64_t seed;          /* weight initialisation                                           */
 } ntp_flow_config;
 
@@ -401,6 +406,7 @@ const char* ntp_flow_last_error(const ntp_flow* flow);
 ntp_status ntp_flow_get_layout(const ntp_flow* flow, uint64_t* n_params, int32_t* n_outputs,
                                int32_t* n_outputs_padded);
 /* Replaces the weights (host FP32, n = n_params) and resets Adam. */
+ntp_status ntp_flow_set_lr(ntp_flow* flow, float lr);
 ntp_status ntp_flow_set_params(ntp_flow* flow, const float* host, uint64_t n);
 /* which: 0 weights, 1 gradient of the last training step, 2 / 3 Adam moments. */
 ntp_status ntp_flow_get_params(ntp_flow* flow, float* host, uint64_t n, int32_t which);
@@ -408,7 +414,9 @@ ntp_status ntp_flow_get_params(ntp_flow* flow, float* host, uint64_t n, int32_t 
    B samples (a multiple of 128): cond [B x 5], time residual tres [B],
    label hit count nhits [B], has_time [B] (0: the sample adds only the count
    term).  update = 0 computes loss and gradient without an Adam step.  All
-   inputs on the host, or on the device when on_device != 0. */
+   inputs on the host, or on the device when on_device != 0.  A step whose
+   gradient is not finite (an FP32 overflow) is skipped: the weights and Adam
+   state stay as they were and *loss is NaN. */
 ntp_status ntp_flow_train_step(ntp_flow* flow, const float* cond, const float* tres, const float* nhits,
                                const int32_t* has_time, int32_t B, int32_t on_device, int32_t update,
                                double* loss);

@@ -194,6 +194,7 @@ class NtpFlowConfig(C.Structure):
         ("beta1", C.c_float),
         ("beta2", C.c_float),
         ("eps", C.c_float),
+        ("grad_clip", C.c_float),
         ("seed", C.c_uint64),
     ]
 
@@ -257,6 +258,7 @@ EXPORTED = (
     "ntp_flow_get_layout",
     "ntp_flow_set_params",
     "ntp_flow_get_params",
+    "ntp_flow_set_lr",
     "ntp_flow_train_step",
     "ntp_flow_forward",
     "ntp_flow_head",
@@ -306,7 +308,7 @@ def _declare(lib: C.CDLL) -> None:
     lib.ntp_gemm_bf16.restype = C.c_int
     lib.ntp_make_table.argtypes = [vp, vp, u64, vp, C.POINTER(NtpSource), C.POINTER(C.c_float),
                                    C.POINTER(C.c_double), C.POINTER(C.c_double), C.POINTER(NtpTableSpec), vp, vp, vp,
-                                   vp, u64, C.POINTER(u64), vp, vp, vp, vp]
+                                   vp, vp, u64, C.POINTER(u64), vp, vp, vp, vp, vp]
     lib.ntp_make_table.restype = C.c_int
     lib.ntp_flow_create.argtypes = [i32, C.POINTER(NtpFlowConfig), C.POINTER(vp)]
     lib.ntp_flow_destroy.argtypes = [vp]
@@ -316,6 +318,8 @@ def _declare(lib: C.CDLL) -> None:
     lib.ntp_flow_get_layout.argtypes = [vp, C.POINTER(u64), C.POINTER(i32), C.POINTER(i32)]
     lib.ntp_flow_set_params.argtypes = [vp, vp, u64]
     lib.ntp_flow_get_params.argtypes = [vp, vp, u64, i32]
+    lib.ntp_flow_set_lr.argtypes = [vp, C.c_float]
+    lib.ntp_flow_set_lr.restype = C.c_int
     lib.ntp_flow_train_step.argtypes = [vp, vp, vp, vp, vp, i32, i32, i32, C.POINTER(C.c_double)]
     lib.ntp_flow_forward.argtypes = [vp, vp, i32, vp]
     lib.ntp_flow_head.argtypes = [vp, vp, vp, vp, vp, i32, C.POINTER(C.c_double), vp]

@@ -32,6 +32,7 @@
 #include <algorithm>
 #include <cmath>
 #include <cstring>
+#include <limits>
 #include <random>
 #include <string>
 #include <type_traits>
@@ -131,7 +132,10 @@ template <int N>
 __device__ __forceinline__ Dual<N> dsqrt(const Dual<N>& a) {
     Dual<N> r;
     r.v = sqrtf(a.v);
-    const float h = r.v > 0.0f ? 0.5f / r.v : 0.0f;
+    // the derivative of safe_quadratic_root's sqrt, held at zero where the
+    // discriminant is within FP32 rounding of zero (it is positive in exact
+    // arithmetic, rq_spline_flow.jl:215-244)
+    const float h = r.v > 1e-18f ? 0.5f / r.v : 0.0f;
 #pragma unroll
     for (int j = 0; j < N; ++j) r.g[j] = a.g[j] * h;
     return r;
@@ -271,6 +275,9 @@ __device__ __forceinline__ void inv_spline(const float* xp, const float* yp, con
 // expectation is used within [-30, 30] (expected counts 1e-13 to 1e13) and
 // the raw scale within [-20, 20] (scale >= 2e-7 ns); outside, the value is
 // held and the gradient is zero
+// the standardised residual of the base normal is held within +-1e6 (a
+// log-density below -5e11) so that the loss and its gradient stay finite
+constexpr float kMaxU = 1e6f;
 __device__ __forceinline__ float clamp_le(float x) { return fminf(fmaxf(x, -30.0f), 30.0f); }
 __device__ __forceinline__ float clamp_scale(float x) { return fminf(fmaxf(x, -20.0f), 20.0f); }
 
@@ -301,6 +308,7 @@ __host__ __device__ constexpr int head_smem_floats(int L, int K, int ldp) {
            + L * 32 * 14                              // dx/du, dlogdet/du for u = (y, x0, w, y0, h, d0, d1)
            + L * 32 * 7                               // adjoint dL/du
            + 32 * 4                                   // per sample: dL/dx innermost, shift, scale, log expectation
+           + L * 32 + 32                              // per layer and sample: squared gradient norm; clip factor
            + 32 * ldp / 2;                            // the block's rows of dL/dP in BF16
 }
 
@@ -315,7 +323,9 @@ __host__ __device__ constexpr int head_smem_floats(int L, int K, int ldp) {
 //                   d x / d u and d logdet / d u (linear tails in closed form)
 //   P4 (warp 0)     reverse chain: dL/du of every layer from dL/dx of the innermost
 //   P5 (all warps)  dL/du -> dL/draw through softmax / cumulative sum / softplus;
-//                   warp 0 adds shift, scale, log expectation and the padding
+//                   the sample's row of dL/dP scaled to an L2 norm of at most
+//                   clip / B; warp 0 adds shift, scale, log expectation and
+//                   the padding
 // Outputs: dL/dP as BF16 row-major dp [B x ldp] (rows staged in shared memory,
 // written as 16-byte vectors) and transposed dpt [ldp x B]; optionally FP32
 // row-major gf; the output layer's bias gradient into gbias (a warp-sum and
@@ -323,7 +333,7 @@ __host__ __device__ constexpr int head_smem_floats(int L, int K, int ldp) {
 template <int K>
 __global__ void __launch_bounds__(32 * kMaxLayers) head_grad_kernel(
     const float* __restrict__ P, int ldp, int L, const float* __restrict__ y, const float* __restrict__ nhits,
-    const int* __restrict__ has_y, int B, float r0, float r1, __nv_bfloat16* __restrict__ dp,
+    const int* __restrict__ has_y, int B, float r0, float r1, float clip, __nv_bfloat16* __restrict__ dp,
     __nv_bfloat16* __restrict__ dpt, float* __restrict__ gf, float* __restrict__ gbias, double* __restrict__ loss) {
     constexpr int NP = 3 * K + 1, NK = K + 1, KN = 3 * NK + 2 * K + NK;
     extern __shared__ float sm[];
@@ -335,7 +345,9 @@ __global__ void __launch_bounds__(32 * kMaxLayers) head_grad_kernel(
     float* s_d = s_y + 2 * S;                  // [L][32][14]
     float* s_g = s_d + S * 14;                 // [L][32][7]
     float* s_s = s_g + S * 7;                  // [32][4]
-    uint16_t* s_dp = reinterpret_cast<uint16_t*>(s_s + 32 * 4);  // [32][ldp]
+    float* s_n2 = s_s + 32 * 4;                // [L][32]
+    float* s_f = s_n2 + S;                     // [32]
+    uint16_t* s_dp = reinterpret_cast<uint16_t*>(s_f + 32);  // [32][ldp]
     const int b = blockIdx.x * 32 + lane;
     const bool act = b < B;
     const float* p = P + static_cast<size_t>(act ? b : 0) * ldp;
@@ -386,7 +398,8 @@ __global__ void __launch_bounds__(32 * kMaxLayers) head_grad_kernel(
             const float rs = p[o_scale];
             const float sg = 1.0f / (1.0f + expf(-clamp_scale(rs)));
             const float scale = 100.0f * sg;
-            const float u = (cur - p[o_shift]) / scale;
+            const float u_raw = (cur - p[o_shift]) / scale;
+            const float u = fminf(fmaxf(u_raw, -kMaxU), kMaxU);
             l -= -logf(scale) - 0.5f * (kLog2Pi + u * u) + ldsum;
             a = u / scale * inv_b;
             g_shift = -u / scale * inv_b;
@@ -450,8 +463,8 @@ __global__ void __launch_bounds__(32 * kMaxLayers) head_grad_kernel(
             if (lane == 0 && sum != 0.0f) atomicAdd(gbias + col, sum);
         }
     };
+    float g[NP];
     {
-        float g[NP];
 #pragma unroll
         for (int i = 0; i < NP; ++i) g[i] = 0.0f;
         if (timed) {
@@ -484,13 +497,31 @@ __global__ void __launch_bounds__(32 * kMaxLayers) head_grad_kernel(
                     g[2 * K + j] = ((j == k ? gu[5] : 0.0f) + (j == k + 1 ? gu[6] : 0.0f)) * sig[j];
             }
         }
-#pragma unroll
-        for (int i = 0; i < NP; ++i) emit(li * NP + i, g[i]);
     }
+    // per-sample clip of dL/dP to an L2 norm of clip / B: one extreme sample
+    // cannot overflow the FP32 / BF16 backward GEMMs
+    {
+        float n2 = 0.0f;
+#pragma unroll
+        for (int i = 0; i < NP; ++i) n2 += g[i] * g[i];
+        s_n2[slot] = n2;
+    }
+    __syncthreads();
     if (warp == 0) {
-        emit(o_shift, s_s[lane * 4 + 1]);
-        emit(o_scale, s_s[lane * 4 + 2]);
-        emit(o_le, s_s[lane * 4 + 3]);
+        float n2 = s_s[lane * 4 + 1] * s_s[lane * 4 + 1] + s_s[lane * 4 + 2] * s_s[lane * 4 + 2] +
+                   s_s[lane * 4 + 3] * s_s[lane * 4 + 3];
+        for (int k = 0; k < L; ++k) n2 += s_n2[k * 32 + lane];
+        const float lim = clip * inv_b;
+        s_f[lane] = (clip > 0.0f && n2 > lim * lim) ? lim * rsqrtf(n2) : 1.0f;
+    }
+    __syncthreads();
+    const float fs = s_f[lane];
+#pragma unroll
+    for (int i = 0; i < NP; ++i) emit(li * NP + i, g[i] * fs);
+    if (warp == 0) {
+        emit(o_shift, s_s[lane * 4 + 1] * fs);
+        emit(o_scale, s_s[lane * 4 + 2] * fs);
+        emit(o_le, s_s[lane * 4 + 3] * fs);
         if (act)
             for (int col = o_le + 1; col < ldp; ++col) {
                 s_dp[lane * ldp + col] = 0;
@@ -510,6 +541,15 @@ __global__ void __launch_bounds__(32 * kMaxLayers) head_grad_kernel(
     }
 }
 
+// Sets *flag if any of the n gradient values is not finite.
+__global__ void nonfinite_kernel(const float* __restrict__ g, long long n, int* __restrict__ flag) {
+    bool bad = false;
+    for (long long i = blockIdx.x * static_cast<long long>(blockDim.x) + threadIdx.x; i < n;
+         i += static_cast<long long>(gridDim.x) * blockDim.x)
+        bad |= !isfinite(g[i]);
+    if (__any_sync(0xffffffffu, bad) && (threadIdx.x & 31) == 0) atomicExch(flag, 1);
+}
+
 // The parameter blocks of the flat vector: offsets (blocks + 1 entries) and,
 // for weight matrices, the BF16 copy and its transpose [cols x rows].
 struct ParamBlocks {
@@ -524,7 +564,8 @@ struct ParamBlocks {
 // one launch; refreshes the BF16 weight copies and their transposes.
 __global__ void adam_kernel(float* __restrict__ w, float* __restrict__ m, float* __restrict__ v,
                             const float* __restrict__ g, const ParamBlocks pb, float lr, float b1, float b2,
-                            float eps, float c1, float c2) {
+                            float eps, float c1, float c2, const int* __restrict__ skip) {
+    if (*skip) return;  // a non-finite gradient: the step is skipped
     const long long total = pb.off[pb.n];
     for (long long i = blockIdx.x * static_cast<long long>(blockDim.x) + threadIdx.x; i < total;
          i += static_cast<long long>(gridDim.x) * blockDim.x) {
@@ -629,6 +670,7 @@ struct ntp_flow {
     int L = 1, K = 12, n_out = 0, n_pad = 0;
     float r0 = -20.0f, r1 = 1500.0f;
     float lr = 1e-3f, b1 = 0.9f, b2 = 0.999f, eps = 1e-8f;
+    float clip = 1e3f;  // per-sample bound on |dL/dP| times the batch size (0 = none)
     long long step = 0;
     std::string err;
     Block blk[8];  // W1 b1 W2 b2 W3 b3 W4 b4
@@ -643,6 +685,8 @@ struct ntp_flow {
     int* hy = nullptr;
     double* loss = nullptr;
     int* gemm_err = nullptr;
+    int* skip = nullptr;     // set when a step's gradient is not finite
+    long long skipped = 0;   // steps skipped for that reason
     // inference
     float* knots = nullptr;
     size_t knots_cap = 0;
@@ -747,7 +791,7 @@ ntp_status launch_head(ntp_flow* f, const float* y, const float* nh, const int* 
                                  static_cast<int>(smem));
         if (e == cudaSuccess) {
             ntp::head_grad_kernel<K><<<(B + 31) / 32, 32 * f->L, smem, f->stream>>>(
-                f->P, f->n_pad, f->L, y, nh, hy, B, f->r0, f->r1, f->dp, f->dpt, gf, gbias, f->loss);
+                f->P, f->n_pad, f->L, y, nh, hy, B, f->r0, f->r1, f->clip, f->dp, f->dpt, gf, gbias, f->loss);
             e = cudaGetLastError();
         }
     });
@@ -757,7 +801,7 @@ ntp_status launch_head(ntp_flow* f, const float* y, const float* nh, const int* 
 
 void free_all(ntp_flow* f) {
     void* ps[] = {f->theta, f->m, f->v, f->grad, f->x, f->xt, f->dp, f->dpt, f->P, f->cond, f->y, f->nh, f->hy,
-                  f->loss, f->gemm_err, f->knots};
+                  f->loss, f->gemm_err, f->skip, f->knots};
     for (void* p : ps)
         if (p) cudaFree(p);
     for (int l = 0; l < 4; ++l) {
@@ -783,7 +827,7 @@ ntp_status ntp_flow_create(int32_t device, const ntp_flow_config* cfg, ntp_flow*
         (cfg->n_bins != 10 && cfg->n_bins != 12) ||
         cfg->n_layers > ntp::kMaxLayers || !(cfg->t_max > cfg->t_min) || !(cfg->lr > 0.0f) ||
         !(cfg->beta1 >= 0.0f && cfg->beta1 < 1.0f) || !(cfg->beta2 >= 0.0f && cfg->beta2 < 1.0f) ||
-        !(cfg->eps > 0.0f))
+        !(cfg->eps > 0.0f) || !(cfg->grad_clip >= 0.0f))
         return NTP_ERR_INVALID;
     ntp_flow* f = new ntp_flow();
     f->device = device;
@@ -798,6 +842,7 @@ ntp_status ntp_flow_create(int32_t device, const ntp_flow_config* cfg, ntp_flow*
     f->b1 = cfg->beta1;
     f->b2 = cfg->beta2;
     f->eps = cfg->eps;
+    f->clip = cfg->grad_clip;
     const int dims[4][2] = {{kHid, kIn}, {kHid, kHid}, {kHid, kHid}, {f->n_pad, kHid}};
     size_t off = 0;
     for (int l = 0; l < 4; ++l) {
@@ -832,7 +877,8 @@ ntp_status ntp_flow_create(int32_t device, const ntp_flow_config* cfg, ntp_flow*
     const size_t np = static_cast<size_t>(f->n_pad);
     if ((e = dalloc(&f->dp, B * np)) || (e = dalloc(&f->dpt, B * np)) || (e = dalloc(&f->P, B * np)) ||
         (e = dalloc(&f->cond, B * kCond)) || (e = dalloc(&f->y, B)) || (e = dalloc(&f->nh, B)) ||
-        (e = dalloc(&f->hy, B)) || (e = dalloc(&f->loss, 1)) || (e = dalloc(&f->gemm_err, 1)))
+        (e = dalloc(&f->hy, B)) || (e = dalloc(&f->loss, 1)) || (e = dalloc(&f->gemm_err, 1)) ||
+        (e = dalloc(&f->skip, 1)))
         return fail(e);
     // He-uniform weights (seeded); zero biases, zero padding input columns of
     // W1 and zero padding rows of W4; the output layer scaled by 0.1
@@ -894,6 +940,12 @@ ntp_status ntp_flow_set_params(ntp_flow* f, const float* host, uint64_t n) {
     F_CUDA(f, cudaMemsetAsync(f->grad, 0, sizeof(float) * n, f->stream));
     F_CUDA(f, cudaStreamSynchronize(f->stream));
     f->step = 0;
+    return NTP_OK;
+}
+
+ntp_status ntp_flow_set_lr(ntp_flow* f, float lr) {
+    if (!f || !(lr > 0.0f)) return NTP_ERR_INVALID;
+    f->lr = lr;
     return NTP_OK;
 }
 
@@ -983,12 +1035,22 @@ ntp_status ntp_flow_train_step(ntp_flow* f, const float* cond, const float* tres
         }
         pb.off[8] = static_cast<long long>(f->n_params);
         const int grid = static_cast<int>(std::min<size_t>((f->n_params + 255) / 256, 152 * 8));
-        ntp::adam_kernel<<<grid, 256, 0, st>>>(f->theta, f->m, f->v, g, pb, f->lr, f->b1, f->b2, f->eps, c1, c2);
+        F_CUDA(f, cudaMemsetAsync(f->skip, 0, sizeof(int), st));
+        ntp::nonfinite_kernel<<<grid, 256, 0, st>>>(g, static_cast<long long>(f->n_params), f->skip);
+        ntp::adam_kernel<<<grid, 256, 0, st>>>(f->theta, f->m, f->v, g, pb, f->lr, f->b1, f->b2, f->eps, c1, c2,
+                                               f->skip);
         F_CUDA(f, cudaGetLastError());
     }
     double hl = 0.0;
+    int skipped = 0;
     F_CUDA(f, cudaMemcpyAsync(&hl, f->loss, sizeof(double), cudaMemcpyDeviceToHost, st));
+    if (update) F_CUDA(f, cudaMemcpyAsync(&skipped, f->skip, sizeof(int), cudaMemcpyDeviceToHost, st));
     F_OK(check_gemm(f));
+    if (skipped) {
+        --f->step;  // Adam's bias correction counts the steps taken
+        ++f->skipped;
+        hl = std::numeric_limits<double>::quiet_NaN();
+    }
     if (loss_out) *loss_out = hl;
     return NTP_OK;
 }

@@ -967,9 +967,10 @@ ntp_status ntp_calc_time_residual(ntp_ctx* ctx, const ntp_hit* hits, uint64_t n,
 
 ntp_status ntp_make_table(ntp_ctx* ctx, const ntp_hit* hits, uint64_t n, const double* weight,
                           const ntp_source* sims, const float* sim_log10_energy, const double* sim_weight_scale,
-                          const double* orientations, const ntp_table_spec* spec, float* cond, float* tres, float* nhits, int32_t* has_time,
-                          uint64_t capacity, uint64_t* n_rows, float* group_cond, double* group_expec,
-                          uint64_t* group_count, void* stream) {
+                          const double* orientations, const ntp_table_spec* spec, float* cond, float* tres,
+                          float* nhits, int32_t* has_time, int32_t* row_group, uint64_t capacity, uint64_t* n_rows,
+                          float* group_cond, double* group_expec, uint64_t* group_count, uint64_t* group_hits,
+                          void* stream) {
     if (!ctx) return NTP_ERR_INVALID;
     if (n_rows) *n_rows = 0;
     if (!ctx->have_targets) {
@@ -1055,9 +1056,9 @@ ntp_status ntp_make_table(ntp_ctx* ctx, const ntp_hit* hits, uint64_t n, const d
     auto take = [&](size_t bytes) { size_t o = off; off += (bytes + 255) / 256 * 256; return o; };
     const size_t o_axes = take(4 * 3 * g), o_gcond = take(4 * 5 * g), o_tgeo = take(8 * S), o_tres = take(8 * n);
     const size_t o_scale = take(8 * S);
-    const size_t o_wsum = take(8 * g), o_npos = take(8 * g), o_nall = take(8 * g), o_nsel = take(8 * g);
-    const size_t o_fill = take(8 * g), o_start = take(8 * (g + 1)), o_ostart = take(8 * (g + 1));
-    const size_t o_want = take(8 * (g + 1));
+    const size_t o_wsum = take(8 * g), o_w2 = take(8 * g), o_npos = take(8 * g), o_nall = take(8 * g);
+    const size_t o_nsel = take(8 * g), o_fill = take(8 * g), o_start = take(8 * (g + 1));
+    const size_t o_ostart = take(8 * (g + 1)), o_want = take(8 * (g + 1));
     NTP_CUDA(ctx, ensure(ctx->d_scratch, ctx->scratch_bytes, off));
     unsigned char* sc = static_cast<unsigned char*>(ctx->d_scratch);
     auto u64p = [&](size_t o) { return reinterpret_cast<unsigned long long*>(sc + o); };
@@ -1073,9 +1074,10 @@ ntp_status ntp_make_table(ntp_ctx* ctx, const ntp_hit* hits, uint64_t n, const d
     if (sim_weight_scale) scale.assign(sim_weight_scale, sim_weight_scale + S);
     double* d_scale = reinterpret_cast<double*>(sc + o_scale);
     NTP_CUDA(ctx, cudaMemcpyAsync(d_scale, scale.data(), 8 * S, cudaMemcpyHostToDevice, st));
-    NTP_CUDA(ctx, cudaMemsetAsync(sc + o_wsum, 0, o_start - o_wsum, st));  // wsum, npos, nall, nsel, fill
-    NTP_CUDA(ctx, ntp::launch_table_count(hits, n, weight, d_scale, S, R, P, center, d_axes, cos_open, d_wsum, u64p(o_npos),
-                                          u64p(o_nall), st));
+    NTP_CUDA(ctx, cudaMemsetAsync(sc + o_wsum, 0, o_start - o_wsum, st));  // wsum, w2, npos, nall, nsel, fill
+    double* d_w2 = reinterpret_cast<double*>(sc + o_w2);
+    NTP_CUDA(ctx, ntp::launch_table_count(hits, n, weight, d_scale, S, R, P, center, d_axes, cos_open, d_wsum, d_w2,
+                                          u64p(o_npos), u64p(o_nall), st));
     // the group count N = Poisson(sum(w) * downsample), not capped by the simulated hits (the
     // oversampling factor may be below 1); the no-cap bound goes through the draw's cap argument
     NTP_CUDA(ctx, cudaMemsetAsync(u64p(o_want), 0xFF, 8 * (g + 1), st));
@@ -1083,17 +1085,21 @@ ntp_status ntp_make_table(ntp_ctx* ctx, const ntp_hit* hits, uint64_t n, const d
                                             u64p(o_nsel), st));
     std::vector<unsigned long long> nall(g), npos(g), nsel(g), start(g + 1), ostart(g + 1), want(g + 1, 0);
     NTP_CUDA(ctx, cudaMemcpyAsync(npos.data(), u64p(o_npos), 8 * g, cudaMemcpyDeviceToHost, st));
-    std::vector<double> wsum(g);
+    std::vector<double> wsum(g), w2(g);
     NTP_CUDA(ctx, cudaMemcpyAsync(nall.data(), u64p(o_nall), 8 * g, cudaMemcpyDeviceToHost, st));
     NTP_CUDA(ctx, cudaMemcpyAsync(nsel.data(), u64p(o_nsel), 8 * g, cudaMemcpyDeviceToHost, st));
-    if (group_expec) NTP_CUDA(ctx, cudaMemcpyAsync(wsum.data(), d_wsum, 8 * g, cudaMemcpyDeviceToHost, st));
+    NTP_CUDA(ctx, cudaMemcpyAsync(wsum.data(), d_wsum, 8 * g, cudaMemcpyDeviceToHost, st));
+    NTP_CUDA(ctx, cudaMemcpyAsync(w2.data(), d_w2, 8 * g, cudaMemcpyDeviceToHost, st));
     NTP_CUDA(ctx, cudaStreamSynchronize(st));
     std::vector<int32_t> zero;
     start[0] = ostart[0] = 0;
     const unsigned long long cap_rows = static_cast<unsigned long long>(spec->max_rows_per_group);
     for (size_t i = 0; i < g; ++i) {
         start[i + 1] = start[i] + nall[i];
-        want[i] = std::min(std::min(nsel[i], cap_rows), npos[i]);
+        // rows: at most max_rows_per_group and a quarter of the effective sample size
+        const double ess = w2[i] > 0.0 ? wsum[i] * wsum[i] / w2[i] : 0.0;
+        const unsigned long long ess_cap = static_cast<unsigned long long>(ess / 4.0) + 1ull;
+        want[i] = std::min(std::min(std::min(nsel[i], cap_rows), npos[i]), ess_cap);
         ostart[i + 1] = ostart[i] + want[i];
         if (nsel[i] == 0 && spec->zero_rows) zero.push_back(static_cast<int32_t>(i));
     }
@@ -1129,9 +1135,10 @@ ntp_status ntp_make_table(ntp_ctx* ctx, const ntp_hit* hits, uint64_t n, const d
     NTP_CUDA(ctx, ntp::launch_table_rows(hit_rows, reinterpret_cast<const int32_t*>(s2 + o_og),
                                          reinterpret_cast<const double*>(s2 + o_ot), zero.size(),
                                          reinterpret_cast<const int32_t*>(s2 + o_zero), u64p(o_nsel), d_gcond, cond,
-                                         tres, nhits, has_time, st));
+                                         tres, nhits, has_time, row_group, st));
     if (group_cond) NTP_CUDA(ctx, cudaMemcpyAsync(group_cond, d_gcond, 4 * 5 * g, cudaMemcpyDeviceToDevice, st));
     if (group_count) NTP_CUDA(ctx, cudaMemcpyAsync(group_count, u64p(o_nsel), 8 * g, cudaMemcpyDeviceToDevice, st));
+    if (group_hits) NTP_CUDA(ctx, cudaMemcpyAsync(group_hits, u64p(o_npos), 8 * g, cudaMemcpyDeviceToDevice, st));
     if (group_expec) {
         for (double& w : wsum) w *= spec->downsample;
         NTP_CUDA(ctx, cudaMemcpyAsync(group_expec, wsum.data(), 8 * g, cudaMemcpyHostToDevice, st));

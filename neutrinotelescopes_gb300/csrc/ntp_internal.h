@@ -157,7 +157,8 @@ cudaError_t gemm_bf16(const void* A, int lda, const void* B, int ldb, void* C, i
 // training-table generator passes (tables.cu)
 cudaError_t launch_table_count(const ntp_hit* hits, unsigned long long n, const double* w, const double* scale,
                                int n_sims, int R, int P, float3 center, const float* axes, float cos_open,
-                               double* wsum, unsigned long long* npos, unsigned long long* nall, cudaStream_t st);
+                               double* wsum, double* w2sum, unsigned long long* npos, unsigned long long* nall,
+                               cudaStream_t st);
 cudaError_t launch_table_bucket(const ntp_hit* hits, unsigned long long n, const double* w, const double* scale,
                                 int n_sims, int R, int P, float3 center, const float* axes, float cos_open, uint2 key,
                                 const unsigned long long* start, unsigned long long* fill, unsigned long long* order,
@@ -167,7 +168,7 @@ cudaError_t launch_table_tres(const ntp_hit* hits, unsigned long long n, const d
 cudaError_t launch_table_rows(unsigned long long n_hit_rows, const int32_t* og, const double* ot,
                               unsigned long long n_zero, const int32_t* zero_groups, const unsigned long long* ndraw,
                               const float* gcond, float* cond, float* tres, float* nhits, int32_t* has_time,
-                              cudaStream_t st);
+                              int32_t* row_group, cudaStream_t st);
 
 // resample_simulation passes (resample.cu)
 cudaError_t launch_resample_group(const ntp_hit* hits, unsigned long long n, const int32_t* pmt, const double* w,

@@ -10,9 +10,13 @@
 // rotated module, detection.jl:72-104) and resampled per (simulation,
 // orientation, PMT) as resample_simulation does (pmt_frontend/pipeline.jl:
 // 86-116), with the count N = Poisson(sum(w) * downsample) not capped by the
-// simulated hits, and min(N, #hits with w > 0, max_rows_per_group) hits
-// drawn without replacement with probability proportional to w (the cap on
-// rows is create_pmt_table's limit of 200, extended_cascade_model.jl:298-311).
+// simulated hits, and min(N, max_rows_per_group, ESS/4 + 1) hits drawn
+// without replacement with probability proportional to w, where ESS =
+// (sum w)^2 / sum w^2 is the group's effective sample size (the cap on rows
+// is create_pmt_table's limit of 200, extended_cascade_model.jl:298-311).
+// The ESS cap keeps the drawn times a weighted sample: with weights scaled up
+// (fewer photons simulated than the source emits) N can reach the number of
+// simulated hits, and a draw of nearly all hits would ignore their weights.
 // A drawn hit becomes one row (condition of its group, time residual, N).
 //
 // A hit can fall into a PMT of several orientations, so the unit of the
@@ -72,7 +76,8 @@ __device__ __forceinline__ HitDir hit_dir(const ntp_hit* hits, unsigned long lon
 __global__ void count_kernel(const ntp_hit* __restrict__ hits, unsigned long long n, const double* __restrict__ w,
                              const double* __restrict__ scale, int n_sims, int R, int P, float3 c,
                              const float* __restrict__ axes, float cos_open, double* __restrict__ wsum,
-                             unsigned long long* __restrict__ npos, unsigned long long* __restrict__ nall) {
+                             double* __restrict__ w2sum, unsigned long long* __restrict__ npos,
+                             unsigned long long* __restrict__ nall) {
     for (unsigned long long i = blockIdx.x * static_cast<unsigned long long>(blockDim.x) + threadIdx.x; i < n;
          i += static_cast<unsigned long long>(gridDim.x) * blockDim.x) {
         const HitDir h = hit_dir(hits, i, c);
@@ -83,6 +88,7 @@ __global__ void count_kernel(const ntp_hit* __restrict__ hits, unsigned long lon
             if (j < 0) continue;
             const size_t g = (static_cast<size_t>(h.s) * R + r) * P + j;
             atomicAdd(wsum + g, wi);
+            atomicAdd(w2sum + g, wi * wi);
             atomicAdd(nall + g, 1ull);
             if (wi > 0.0) atomicAdd(npos + g, 1ull);
         }
@@ -91,7 +97,8 @@ __global__ void count_kernel(const ntp_hit* __restrict__ hits, unsigned long lon
 
 __global__ void bucket_kernel(const ntp_hit* __restrict__ hits, unsigned long long n, const double* __restrict__ w,
                               const double* __restrict__ scale, int n_sims, int R, int P, float3 c,
-                              const float* __restrict__ axes, float cos_open, uint2 key, const unsigned long long* __restrict__ start,
+                              const float* __restrict__ axes, float cos_open, uint2 key,
+                              const unsigned long long* __restrict__ start,
                               unsigned long long* __restrict__ fill, unsigned long long* __restrict__ order,
                               unsigned long long* __restrict__ okey) {
     for (unsigned long long i = blockIdx.x * static_cast<unsigned long long>(blockDim.x) + threadIdx.x; i < n;
@@ -134,7 +141,7 @@ __global__ void rows_kernel(unsigned long long n_hit_rows, const int32_t* __rest
                             const double* __restrict__ ot, unsigned long long n_zero,
                             const int32_t* __restrict__ zero_groups, const unsigned long long* __restrict__ ndraw,
                             const float* __restrict__ gcond, float* __restrict__ cond, float* __restrict__ tres,
-                            float* __restrict__ nhits, int32_t* __restrict__ has_time) {
+                            float* __restrict__ nhits, int32_t* __restrict__ has_time, int32_t* __restrict__ row_group) {
     const unsigned long long total = n_hit_rows + n_zero;
     for (unsigned long long q = blockIdx.x * static_cast<unsigned long long>(blockDim.x) + threadIdx.x; q < total;
          q += static_cast<unsigned long long>(gridDim.x) * blockDim.x) {
@@ -145,6 +152,7 @@ __global__ void rows_kernel(unsigned long long n_hit_rows, const int32_t* __rest
         tres[q] = hit ? static_cast<float>(ot[q]) : 0.0f;
         nhits[q] = static_cast<float>(ndraw[g]);
         has_time[q] = hit ? 1 : 0;
+        if (row_group) row_group[q] = g;
     }
 }
 
@@ -157,9 +165,11 @@ int grid_for(unsigned long long n) {
 
 cudaError_t launch_table_count(const ntp_hit* hits, unsigned long long n, const double* w, const double* scale,
                                int n_sims, int R, int P, float3 center, const float* axes, float cos_open,
-                               double* wsum, unsigned long long* npos, unsigned long long* nall, cudaStream_t st) {
+                               double* wsum, double* w2sum, unsigned long long* npos, unsigned long long* nall,
+                               cudaStream_t st) {
     if (n == 0) return cudaSuccess;
-    count_kernel<<<grid_for(n), kBlock, 0, st>>>(hits, n, w, scale, n_sims, R, P, center, axes, cos_open, wsum, npos, nall);
+    count_kernel<<<grid_for(n), kBlock, 0, st>>>(hits, n, w, scale, n_sims, R, P, center, axes, cos_open, wsum, w2sum,
+                                                 npos, nall);
     return cudaGetLastError();
 }
 
@@ -183,10 +193,10 @@ cudaError_t launch_table_tres(const ntp_hit* hits, unsigned long long n, const d
 cudaError_t launch_table_rows(unsigned long long n_hit_rows, const int32_t* og, const double* ot,
                               unsigned long long n_zero, const int32_t* zero_groups, const unsigned long long* ndraw,
                               const float* gcond, float* cond, float* tres, float* nhits, int32_t* has_time,
-                              cudaStream_t st) {
+                              int32_t* row_group, cudaStream_t st) {
     if (n_hit_rows + n_zero == 0) return cudaSuccess;
     rows_kernel<<<grid_for(n_hit_rows + n_zero), kBlock, 0, st>>>(n_hit_rows, og, ot, n_zero, zero_groups, ndraw,
-                                                                  gcond, cond, tres, nhits, has_time);
+                                                                  gcond, cond, tres, nhits, has_time, row_group);
     return cudaGetLastError();
 }
 

@@ -51,6 +51,7 @@ class RQNormFlowHParams:
     beta1: float = 0.9
     beta2: float = 0.999
     eps: float = 1e-8
+    grad_clip: float = 1e3   # per-sample bound on |dL/draw outputs| x batch size; 0 = none
     seed: int = 31338
 
 
@@ -72,7 +73,7 @@ class RQNormFlow:
         cfg = _abi.NtpFlowConfig(batch_capacity=cap, n_layers=int(hp.n_layers), n_bins=int(hp.K),
                                  t_min=float(hp.range_min), t_max=float(hp.range_max), lr=float(hp.lr),
                                  beta1=float(hp.beta1), beta2=float(hp.beta2), eps=float(hp.eps),
-                                 seed=int(hp.seed) & (2 ** 64 - 1))
+                                 grad_clip=float(hp.grad_clip), seed=int(hp.seed) & (2 ** 64 - 1))
         h = C.c_void_p()
         st = self.lib.ntp_flow_create(int(device), C.byref(cfg), C.byref(h))
         if st != 0:
@@ -134,6 +135,10 @@ class RQNormFlow:
 
     def gradient(self) -> np.ndarray:
         return self.get_params(1)
+
+    def set_lr(self, lr: float) -> None:
+        """The Adam step size of the following steps (for schedules)."""
+        self._check(self.lib.ntp_flow_set_lr(self._h, float(lr)))
 
     # ---------------------------------------------------------------- training
     def train_step(self, cond, tres, nhits, has_time=None, *, update: bool = True) -> float:

@@ -63,13 +63,15 @@ class FlowTable:
     n_photons: int = 0
     n_hits: int = 0
     meta: dict = field(default_factory=dict)
+    row_group: object = None   # group index of every row
 
     def __len__(self) -> int:
         return int(self.tres.shape[0])
 
     def save(self, path) -> None:
         np.savez(path, **{k: getattr(self, k).cpu().numpy() for k in
-                          ("cond", "tres", "nhits", "has_time", "group_cond", "group_expec", "group_count")},
+                          ("cond", "tres", "nhits", "has_time", "group_cond", "group_expec", "group_count",
+                           "row_group") if getattr(self, k) is not None},
                  n_photons=self.n_photons, n_hits=self.n_hits,
                  meta=np.array([repr(sorted(self.meta.items()))]))
 
@@ -78,7 +80,8 @@ class FlowTable:
         import torch
         z = np.load(path)
         t = {k: torch.as_tensor(z[k]).to(device) for k in
-             ("cond", "tres", "nhits", "has_time", "group_cond", "group_expec", "group_count")}
+             ("cond", "tres", "nhits", "has_time", "group_cond", "group_expec", "group_count", "row_group")
+             if k in z.files}
         return cls(**t, n_photons=int(z["n_photons"]), n_hits=int(z["n_hits"]))
 
 
@@ -176,6 +179,7 @@ def make_flow_table(cfg: TableConfig | None = None, medium=None, spectrum=None, 
     gcond = torch.empty((G, 5), dtype=torch.float32, device=dev)
     gexp = torch.empty(G, dtype=torch.float64, device=dev)
     gcnt = torch.empty(G, dtype=torch.int64, device=dev)
+    ghit = torch.empty(G, dtype=torch.int64, device=dev)
     cap = max(G + n, 1)
     dp = C.POINTER(C.c_double)
     while True:
@@ -183,12 +187,13 @@ def make_flow_table(cfg: TableConfig | None = None, medium=None, spectrum=None, 
         tres = torch.empty(cap, dtype=torch.float32, device=dev)
         nh = torch.empty(cap, dtype=torch.float32, device=dev)
         has = torch.empty(cap, dtype=torch.int32, device=dev)
+        rg = torch.empty(cap, dtype=torch.int32, device=dev)
         torch.cuda.synchronize()
         n_rows = C.c_uint64()
         st = lib.ntp_make_table(ctx, hits.data_ptr(), n, w.data_ptr(), srcs, _abi.fptr(le), scale.ctypes.data_as(dp),
                                 orient.ctypes.data_as(dp), C.byref(spec), cond.data_ptr(), tres.data_ptr(),
-                                nh.data_ptr(), has.data_ptr(), cap, C.byref(n_rows), gcond.data_ptr(),
-                                gexp.data_ptr(), gcnt.data_ptr(), None)
+                                nh.data_ptr(), has.data_ptr(), rg.data_ptr(), cap, C.byref(n_rows), gcond.data_ptr(),
+                                gexp.data_ptr(), gcnt.data_ptr(), ghit.data_ptr(), None)
         if st == _abi.NTP_ERR_OVERFLOW:
             cap = int(n_rows.value)
             continue
@@ -196,11 +201,12 @@ def make_flow_table(cfg: TableConfig | None = None, medium=None, spectrum=None, 
         break
     m = int(n_rows.value)
     meta = dict(n_sims=cfg.n_sims, n_orientations=R, seed=cfg.seed, photons_per_gev=cfg.photons_per_gev)
-    table = FlowTable(cond[:m], tres[:m], nh[:m], has[:m], gcond, gexp, gcnt, n_phot, n, meta)
+    table = FlowTable(cond[:m], tres[:m], nh[:m], has[:m], gcond, gexp, gcnt, n_phot, n, meta, rg[:m])
     table.sims = sims
     table.hits = hits[: n * 64]
     table.weights = w[:n]
     table.orientations = orient.reshape(-1, 3, 3)
+    table.group_hits = ghit
     return table
 
 

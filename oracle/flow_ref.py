@@ -30,9 +30,11 @@ import torch
 F = torch.nn.functional
 DT = torch.float64
 # the kernels' FP32 range guards: log expectation within [-30, 30], raw scale
-# within [-20, 20] (held, zero gradient outside); inactive for ordinary values
+# within [-20, 20], standardised residual within +-1e6 (held, zero gradient
+# outside); inactive for ordinary values
 LE_CLAMP = 30.0
 SCALE_CLAMP = 20.0
+MAX_U = 1e6
 
 
 def normalize_bin_sizes(u: torch.Tensor, total: float, min_bin: float = 1e-4) -> torch.Tensor:
@@ -143,7 +145,8 @@ def flow_logpdf(y, raw, n_layers: int, r0: float, r1: float, K: int | None = Non
         ldsum = ldsum + ld
     shift = raw[:, L * NP]
     scale = torch.sigmoid(torch.clamp(raw[:, L * NP + 1], -SCALE_CLAMP, SCALE_CLAMP)) * 100.0
-    normal = -torch.log(scale) - 0.5 * (math.log(2 * math.pi) + ((cur - shift) / scale) ** 2)
+    u = torch.clamp((cur - shift) / scale, -MAX_U, MAX_U)
+    normal = -torch.log(scale) - 0.5 * (math.log(2 * math.pi) + u ** 2)
     return normal + ldsum
 
 

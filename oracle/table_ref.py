@@ -89,6 +89,13 @@ def pair_key(philox, photon_index: int, source_index: int, r: int, w: float, see
     return math.log(u01_53(x[0], x[1])) / w
 
 
+def rows_wanted(n_drawn: int, n_pos: int, max_rows: int, wsum: float, w2sum: float) -> int:
+    """Rows drawn from a group: min(N, hits with w > 0, max_rows, ESS/4 + 1)
+    with ESS = (sum w)^2 / sum w^2."""
+    ess = wsum * wsum / w2sum if w2sum > 0 else 0.0
+    return min(n_drawn, n_pos, max_rows, int(ess / 4.0) + 1)
+
+
 def select(keys: list[tuple[float, int]], want: int) -> set[int]:
     """The hit indices with the `want` largest keys."""
     return {i for _, i in sorted(keys, reverse=True)[:want]}

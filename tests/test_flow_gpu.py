@@ -15,6 +15,8 @@ Tolerances, and why:
   transposed weights to BF16; per parameter block relative L2 error <= 3e-2
   and cosine similarity >= 0.999 against the float64 autograd gradient.
 * Adam: the update itself is FP32 elementwise: 1e-6 relative.
+The parity tests run without the per-sample gradient clip (the oracle has
+none); a separate test checks the clip.
 """
 import math
 
@@ -35,8 +37,11 @@ CASES = [  # (n_layers, K, range): the reference's default model and the 5-layer
 ]
 
 
-def make(L, K, r0, r1, cap=2048, seed=1):
-    return RQNormFlow(RQNormFlowHParams(K=K, n_layers=L, range_min=r0, range_max=r1, batch_size=cap, seed=seed))
+def make(L, K, r0, r1, cap=2048, seed=1, clip=0.0):
+    """A flow without the per-sample gradient clip unless asked for: the
+    oracle computes the unclipped gradient."""
+    return RQNormFlow(RQNormFlowHParams(K=K, n_layers=L, range_min=r0, range_max=r1, batch_size=cap, seed=seed,
+                                        grad_clip=clip))
 
 
 def batch(rng, B, r0, r1, frac_count_only=0.1):
@@ -69,6 +74,31 @@ def test_head_loss_and_gradient(L, K, r0, r1):
     err = np.linalg.norm(grad - g_ref, axis=1) / (np.linalg.norm(g_ref, axis=1) + 1e-12)
     assert np.quantile(err, 0.99) < 2e-3, np.sort(err)[-5:]
     assert np.linalg.norm(grad - g_ref) / np.linalg.norm(g_ref) < 2e-3
+
+
+def test_head_gradient_clip():
+    """With grad_clip = c every row of dL/dP has an L2 norm of at most c / B and
+    points along the unclipped row; rows below the bound are unchanged."""
+    L, K, r0, r1 = 5, 12, -20.0, 1500.0
+    rng = np.random.default_rng(15)
+    B, c = 1024, 50.0
+    NP = 3 * K + 1
+    with make(L, K, r0, r1) as fl0, make(L, K, r0, r1, clip=c) as fl1:
+        raw = (rng.standard_normal((B, fl0.n_outputs)) * 0.8).astype(np.float32)
+        raw[:, L * NP] = rng.uniform(r0, r0 + 0.5 * (r1 - r0), B)
+        raw[:, L * NP + 2] = rng.standard_normal(B) * 2.0
+        _, tres, nhits, has = batch(rng, B, r0, r1)
+        l0, g0 = fl0.head(raw, tres, nhits, has)
+        l1, g1 = fl1.head(raw, tres, nhits, has)
+    assert l0 == l1
+    n0 = np.linalg.norm(g0.astype(np.float64), axis=1)
+    n1 = np.linalg.norm(g1.astype(np.float64), axis=1)
+    assert np.all(n1 <= c / B * (1 + 1e-5))
+    big = n0 > c / B
+    assert big.any() and (~big).any()
+    np.testing.assert_array_equal(g1[~big], g0[~big])
+    cos = np.sum(g0[big] * g1[big], axis=1) / (n0[big] * n1[big])
+    assert np.all(cos > 1 - 1e-5)
 
 
 @pytest.mark.parametrize("L,K,r0,r1", CASES)
@@ -113,7 +143,8 @@ def test_full_gradient(L, K, r0, r1):
 def test_adam_steps_and_weight_copies():
     L, K, r0, r1 = 5, 12, -20.0, 1500.0
     rng = np.random.default_rng(30)
-    hp = RQNormFlowHParams(K=K, n_layers=L, range_min=r0, range_max=r1, batch_size=512, seed=9, lr=1e-3)
+    hp = RQNormFlowHParams(K=K, n_layers=L, range_min=r0, range_max=r1, batch_size=512, seed=9, lr=1e-3,
+                           grad_clip=0.0)
     with RQNormFlow(hp) as fl:
         th = fl.get_params().astype(np.float64)
         m = np.zeros_like(th)
@@ -220,7 +251,7 @@ def test_invalid_arguments():
     lib = _abi.load_library()
     import ctypes as C
     bad = _abi.NtpFlowConfig(batch_capacity=1024, n_layers=1, n_bins=11, t_min=-20, t_max=100, lr=1e-3, beta1=0.9,
-                             beta2=0.999, eps=1e-8, seed=0)
+                             beta2=0.999, eps=1e-8, grad_clip=0.0, seed=0)
     h = C.c_void_p()
     assert lib.ntp_flow_create(0, C.byref(bad), C.byref(h)) == _abi.NTP_ERR_INVALID
     assert not h.value

@@ -1,0 +1,95 @@
+"""What the trained flow gains over plain MC.
+
+The flow is trained on a table the MC kernel generates (make_flow_table),
+then compared on held-out simulations with a high-statistics MC run of the
+same conditions: per-PMT expected hits and arrival-time quantiles.  The gain
+is the GPU time plain MC needs to reach the flow's count precision on those
+PMTs (hits scale with photons, so precision e needs about 1/e^2 hits) over
+the flow's evaluation time for the same conditions.  The measured numbers are
+printed (pytest -s)."""
+import math
+import time
+
+import numpy as np
+import pytest
+
+torch = pytest.importorskip("torch")
+
+from neutrinotelescopes_gb300.flow import RQNormFlow, RQNormFlowHParams  # noqa: E402
+from neutrinotelescopes_gb300.tables import TableConfig, make_flow_table  # noqa: E402
+
+pytestmark = pytest.mark.gpu
+
+
+def _train(tab, steps: int, lr0: float = 1e-3) -> RQNormFlow:
+    fl = RQNormFlow(RQNormFlowHParams(batch_size=8192, lr=lr0))
+    fl.init_from_table(tab)
+    per_epoch = len(tab) // 8192
+    done, ep = 0, 0
+    while done < steps:
+        fl.set_lr(1e-5 + 0.5 * (lr0 - 1e-5) * (1 + math.cos(math.pi * done / steps)))
+        done += len(fl.fit_table(tab, epochs=1, seed=ep, max_steps=min(per_epoch, steps - done)))
+        ep += 1
+    return fl
+
+
+def test_surrogate_gains_over_plain_mc():
+    tab = make_flow_table(TableConfig(n_sims=4096, n_orientations=16, target_hits=300, max_photons=10_000_000,
+                                      seed=1))
+    fl = _train(tab, 12000)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    ho = make_flow_table(TableConfig(n_sims=16, n_orientations=16, target_hits=100_000, max_photons=1_000_000_000,
+                                     max_rows_per_group=5000, seed=99))
+    torch.cuda.synchronize()
+    t_mc = time.perf_counter() - t0
+    gc = ho.group_cond.cpu().numpy()
+    lam = ho.group_expec.cpu().numpy()
+    hits = ho.group_hits.cpu().numpy()
+    cond_dev = ho.group_cond.contiguous()
+    idx = torch.zeros(1, dtype=torch.int32, device="cuda")
+    tt = torch.zeros(1, dtype=torch.float32, device="cuda")
+    fl.logpdf(cond_dev, idx, tt, log_expec=True)  # warm-up
+    torch.cuda.synchronize()
+    t1 = time.perf_counter()
+    reps = 20
+    for _ in range(reps):
+        _, le = fl.logpdf(cond_dev, idx, tt, log_expec=True)
+    torch.cuda.synchronize()
+    t_flow = (time.perf_counter() - t1) / reps
+    le = le.cpu().numpy()
+
+    # expected hits per PMT against the high-statistics MC
+    m = (hits >= 1000) & (lam > 0)
+    rel = np.abs(np.exp(le[m].astype(np.float64)) / lam[m] - 1.0)
+    e_count = float(np.median(rel))
+    # arrival-time quantiles of PMTs with at least 300 drawn times
+    rg = ho.row_group.cpu().numpy()
+    tres = ho.tres.cpu().numpy()
+    has = ho.has_time.cpu().numpy().astype(bool)
+    grid = np.concatenate([np.linspace(-20.0, 200.0, 22001), np.linspace(200.1, 1500.0, 13000)]).astype(np.float32)
+    dq = []
+    for g in np.unique(rg[has]):
+        ts = tres[has & (rg == g)]
+        if ts.size < 300:
+            continue
+        lp = fl.logpdf(gc[g:g + 1], np.zeros(grid.size, np.int32), grid)
+        pdf = np.exp(lp.astype(np.float64))
+        cdf = np.concatenate([[0.0], np.cumsum((pdf[1:] + pdf[:-1]) * 0.5 * np.diff(grid))])
+        cdf /= cdf[-1]
+        q = [0.1, 0.5, 0.9]
+        dq.append(np.abs(np.interp(q, cdf, grid) - np.quantile(ts, q)))
+        if len(dq) >= 60:
+            break
+    dq = np.array(dq)
+    # plain MC at the flow's count precision: about 1/e^2 hits per PMT
+    n_eq = 1.0 / max(e_count, 1e-3) ** 2
+    t_mc_eq = t_mc * float(np.median(n_eq / hits[m]))
+    gain = t_mc_eq / t_flow
+    print(f"\nflow surrogate: {m.sum()} PMTs with >= 1000 MC hits: median |lambda_flow/lambda_MC - 1| = {e_count:.3f}; "
+          f"{len(dq)} PMTs: median |quantile error| (10/50/90%) = {np.median(dq, axis=0).round(2)} ns; "
+          f"flow {len(gc)} conditions in {t_flow * 1e3:.3f} ms; MC run {t_mc:.2f} s, at equal count precision "
+          f"{t_mc_eq:.3f} s; gain {gain:.0f}x")
+    assert e_count < 0.3
+    assert len(dq) >= 20 and np.median(dq[:, 1]) < 2.0
+    assert gain >= 50.0

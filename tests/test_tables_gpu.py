@@ -74,6 +74,8 @@ def test_rows_are_the_oracle_draws(small_table, oracle_lib):
     scale = t.sims["weight_scale"]
     N = t.group_count.cpu().numpy()
     by_group: dict[int, list] = {}
+    wsum: dict[int, float] = {}
+    w2: dict[int, float] = {}
     for i, g in pairs:
         s = int(rec["source_index"][i])
         wi = w[i] * scale[s]
@@ -81,18 +83,15 @@ def test_rows_are_the_oracle_draws(small_table, oracle_lib):
             r = (g // P) % R
             by_group.setdefault(g, []).append((T.pair_key(oracle_lib.philox, int(rec["photon_index"][i]), s, r, wi,
                                                           SMALL.seed), i))
-    # time residuals per hit
-    c_n800 = None
-    cond = t.cond.cpu().numpy()
+            wsum[g] = wsum.get(g, 0.0) + wi
+            w2[g] = w2.get(g, 0.0) + wi * wi
     tres = t.tres.cpu().numpy()
     nh = t.nhits.cpu().numpy()
     has = t.has_time.cpu().numpy()
-    gc = t.group_cond.cpu().numpy()
-    # map each timed row back to its group through its condition and count
+    rg = t.row_group.cpu().numpy()
     rows_by_group: dict[int, list] = {}
-    keyed = {tuple(np.round(gc[g], 6)): g for g in range(len(gc))}
     for q in range(len(tres)):
-        g = keyed[tuple(np.round(cond[q], 6))]
+        g = int(rg[q])
         assert nh[q] == N[g]
         if has[q]:
             rows_by_group.setdefault(g, []).append(tres[q])
@@ -103,7 +102,7 @@ def test_rows_are_the_oracle_draws(small_table, oracle_lib):
     tgeo = (src_d - np.float32(0.21)).astype(np.float64) / (T.C_VAC / n800)
     checked = 0
     for g, keys in by_group.items():
-        want = min(int(N[g]), len(keys), SMALL.max_rows_per_group)
+        want = T.rows_wanted(int(N[g]), len(keys), SMALL.max_rows_per_group, wsum[g], w2[g])
         sel = T.select(keys, want)
         s = g // (R * P)
         exp_t = np.sort(np.array([rec["time"][i] - tgeo[s] for i in sel], np.float32))
@@ -113,14 +112,15 @@ def test_rows_are_the_oracle_draws(small_table, oracle_lib):
         checked += 1
     assert checked >= 0.97 * len(by_group), (checked, len(by_group))
     # every group is represented: rows with a time, or a count-only row
-    assert set(rows_by_group) | {g for g in range(len(gc)) if N[g] == 0} == set(range(len(gc)))
+    G = len(N)
+    assert set(rows_by_group) | {g for g in range(G) if N[g] == 0} == set(range(G))
 
 
 def test_table_save_load_roundtrip(small_table, tmp_path):
     p = tmp_path / "table.npz"
     small_table.save(p)
     t2 = FlowTable.load(p)
-    for k in ("cond", "tres", "nhits", "has_time", "group_cond", "group_expec", "group_count"):
+    for k in ("cond", "tres", "nhits", "has_time", "group_cond", "group_expec", "group_count", "row_group"):
         assert torch.equal(getattr(small_table, k).cpu(), getattr(t2, k).cpu()), k
     assert t2.n_photons == small_table.n_photons
 
