@@ -48,6 +48,12 @@ def algo_ops_per_step(n_strings: int) -> int:
     return OPS_BASE + OPS_PER_GEOMETRY_TEST * n_strings
 
 
+def step_seed(rank: int, i: int) -> int:
+    """Philox key of step i on a rank: distinct across ranks and steps, so
+    replicas never simulate the same photons."""
+    return 0x5EED0000 + 1 + rank * 1_000_003 + i
+
+
 def parse():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -60,6 +66,8 @@ def parse():
     ap.add_argument("--serving-requests", type=int, default=4096,
                     help="requests of the serving measurement (0 = skip)")
     ap.add_argument("--flow", type=int, default=1, help="1: include the flow surrogate measurement")
+    ap.add_argument("--legs", default="propagation,serving,flow",
+                    help="comma list of the measurements to run: propagation (the headline line), serving, flow")
     ap.add_argument("--small", action="store_true",
                     help="profiling case: one cascade at 1% of its photons, 64 MB hit buffer, 256 MB L2 flush")
     return ap.parse_args()
@@ -374,6 +382,16 @@ def main():
     from neutrinotelescopes_gb300.photon_prop import pack_sources
 
     torch.cuda.set_device(local)
+    legs = set(args.legs.split(","))
+    if "propagation" not in legs:
+        out = {"metric": METRIC, "value": None, "unit": METRIC, "n_gpus": world, "legs": sorted(legs)}
+        if "serving" in legs and args.serving_requests > 0:
+            out["serving"] = serving_bench(args.serving_requests)
+        if "flow" in legs and args.flow and rank == 0:
+            out["flow"] = flow_bench()
+        if rank == 0:
+            print(json.dumps(out))
+        return
     if args.small:
         setup = workloads.cascade_string_setup(1, WORKLOAD_SEED, photon_scale=0.01, device=local)
     else:
@@ -391,7 +409,7 @@ def main():
     stats = _abi.NtpRunStats()
 
     def step(i: int) -> None:
-        seed = workloads.SEED_BASE + 1 + rank * 1_000_003 + i
+        seed = step_seed(rank, i)
         st = lib.ntp_propagate(ctx, srcs, n_src, seed, C.byref(opts), hits.data_ptr(), cap, 1, C.byref(nh),
                                C.byref(ns))
         if st != _abi.NTP_OK:
@@ -457,9 +475,9 @@ def main():
     setup.close()
     del hits, flush
     torch.cuda.empty_cache()
-    if args.serving_requests > 0 and not args.small:
+    if args.serving_requests > 0 and not args.small and "serving" in legs:
         out["serving"] = serving_bench(args.serving_requests)
-    if args.flow and not args.small and rank == 0:
+    if args.flow and not args.small and rank == 0 and "flow" in legs:
         out["flow"] = flow_bench()
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         out["cpu_baseline"] = cpu_baseline(workloads.cascade_string_setup(N_CASCADES, WORKLOAD_SEED),
