@@ -66,8 +66,9 @@ def parse():
     ap.add_argument("--serving-requests", type=int, default=4096,
                     help="requests of the serving measurement (0 = skip)")
     ap.add_argument("--flow", type=int, default=1, help="1: include the flow surrogate measurement")
-    ap.add_argument("--legs", default="propagation,serving,flow",
-                    help="comma list of the measurements to run: propagation (the headline line), serving, flow")
+    ap.add_argument("--legs", default="propagation,serving,flow,hybrid",
+                    help="comma list of the measurements to run: propagation (the headline line), serving, flow, "
+                         "hybrid")
     ap.add_argument("--small", action="store_true",
                     help="profiling case: one cascade at 1% of its photons, 64 MB hit buffer, 256 MB L2 flush")
     return ap.parse_args()
@@ -275,6 +276,110 @@ def flow_bench(train_steps: int = 300, n_tuples: int = 100_000_000) -> dict:
     return out
 
 
+def hybrid_bench(n_events: int = 10_000, batch: int = 256, train_steps: int = 12_000) -> dict:
+    """Hybrid serving workload: 10 x 10 strings x 80 POM modules x 16 PMTs
+    (50 m, 15 m spacing), n_events cascades with E log-uniform 1e2-1e6 GeV,
+    vertex uniform in the detector's bounding box, isotropic direction.  The
+    flow (trained here on an MC table of 4096 simulations) supplies every
+    PMT within 1-200 m of the vertex; events with a module closer than 1 m go
+    to plain MC.  Reported: events/s and per-event latency of the saturated
+    stream (batches of `batch` events), plain MC's events/s on the same
+    stream (its photons/s measured on sample events of this detector, times
+    the stream's mean photons per event), and the error against MC on sample
+    events (expected hits per module, arrival-time KS per module and pooled)."""
+    import math as _m
+
+    import numpy as np
+    import torch
+
+    from neutrinotelescopes_gb300 import workloads
+    from neutrinotelescopes_gb300.flow import RQNormFlow, RQNormFlowHParams
+    from neutrinotelescopes_gb300.surrogate import HybridSimulator, compare, hybrid_events, mc_truth
+    from neutrinotelescopes_gb300.tables import TableConfig, make_flow_table
+
+    out = {"workload": f"{n_events} cascades 1e2-1e6 GeV, 10 x 10 strings x 80 modules x 16 PMTs (50 m, 15 m), "
+                       "simple water; flow for PMTs 1-200 m from the vertex, MC for events with a module < 1 m"}
+    tab = make_flow_table(TableConfig(n_sims=4096, n_orientations=16, target_hits=300, max_photons=10_000_000, seed=1))
+    fl = RQNormFlow(RQNormFlowHParams(batch_size=8192), batch_capacity=65536)
+    fl.init_from_table(tab)
+    per = len(tab) // 8192
+    done, ep = 0, 0
+    t0 = time.perf_counter()
+    while done < train_steps:
+        fl.set_lr(1e-5 + 0.5 * (1e-3 - 1e-5) * (1 + _m.cos(_m.pi * done / train_steps)))
+        done += len(fl.fit_table(tab, epochs=1, seed=ep, max_steps=min(per, train_steps - done)))
+        ep += 1
+    out["training"] = {"table_rows": len(tab), "steps": done, "seconds": time.perf_counter() - t0}
+    del tab
+    torch.cuda.empty_cache()
+    setup = workloads.hybrid_setup()
+    sim = HybridSimulator(setup, fl, seed=workloads.SEED_BASE + 4)
+    events = hybrid_events(n_events, setup)
+    sim.simulate(events[:8])  # warm-up
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    lat, n_flow, n_mc, n_hits = [], 0, 0, 0
+    for s in range(0, n_events, batch):
+        res = sim.simulate(events[s:s + batch])
+        torch.cuda.synchronize()
+        t = time.perf_counter() - t0
+        for r in res:
+            lat.append(t)
+            n_flow += r.method == "flow"
+            n_mc += r.method == "mc"
+            n_hits += r.n_hits
+    dt = time.perf_counter() - t0
+    lat = np.array(lat)
+    out["saturated"] = {"events_per_s": n_events / dt, "seconds": dt, "events_flow": n_flow, "events_mc": n_mc,
+                        "hits": n_hits, "latency_p50_ms": float(np.percentile(lat, 50) * 1e3),
+                        "latency_p99_ms": float(np.percentile(lat, 99) * 1e3),
+                        "note": "all events queued at t = 0 and served in batches; latency = completion time"}
+    # one batch alone: the latency of an event served on arrival with a batch of its own
+    torch.cuda.synchronize()
+    t1 = time.perf_counter()
+    sim.simulate(events[:1])
+    torch.cuda.synchronize()
+    out["single_event_latency_ms"] = (time.perf_counter() - t1) * 1e3
+    # plain MC serving on the same GPU and detector: the continuous-batching
+    # server's photons/s on a sample of the stream, events/s of the stream
+    from neutrinotelescopes_gb300.serving import EventServer
+    mean_photons = float(np.mean([e[1].photons for e in events]))
+    sample = [e for e in events if 3.0 <= e[2] <= 4.0][:16]
+    srv = EventServer(setup, hbm_budget_bytes=60 * 10 ** 9, seed=workloads.SEED_BASE + 5,
+                      reserve_hits_per_photon=5e-3, min_reserve_hits=4096, max_batch_photons=2_000_000_000)
+    for e in sample:
+        srv.submit(e[0], e[1])
+    t_a = srv.stats().clock
+    res_mc = srv.run_all()
+    mc_dt = max(r.t_done for r in res_mc) - t_a
+    srv.close()
+    ph = sum(e[1].photons for e in sample)
+    mc_rate = ph / mc_dt
+    out["plain_mc"] = {"photons_per_s": mc_rate, "mean_photons_per_event": mean_photons,
+                       "events_per_s": mc_rate / mean_photons,
+                       "sample": f"{len(sample)} events of 1e3-1e4 GeV ({ph:.3g} photons) through the MC event "
+                                 f"server, hits kept on the device"}
+    out["speedup_vs_plain_mc"] = out["saturated"]["events_per_s"] / out["plain_mc"]["events_per_s"]
+    # error against MC on sample events
+    errs, ksm, ksp = [], [], []
+    for e in [e for e in events if 3.0 <= e[2] <= 4.0][:6]:
+        c = compare(sim, e[1], e[2], e[0], seed=e[0])
+        if c.get("modules"):
+            errs.extend(list(c["expected_rel_err"]))
+            ksm.extend(list(c["ks_modules"]))
+            ksp.append(c["ks_pooled"])
+    errs, ksm = np.abs(np.array(errs)), np.array(ksm)
+    out["error_vs_mc"] = {"ks_threshold_of_the_mc_fallback": 0.02,
+                          "events": len(ksp), "modules_expected_ge_100": int(errs.size),
+                          "expected_hits_rel_err_median": float(np.median(errs)) if errs.size else None,
+                          "expected_hits_rel_err_p90": float(np.quantile(errs, 0.9)) if errs.size else None,
+                          "ks_per_module_median": float(np.median(ksm)) if ksm.size else None,
+                          "ks_pooled_median": float(np.median(ksp)) if ksp else None}
+    setup.close()
+    fl.close()
+    return out
+
+
 def _measured_peak(key: str, fallback: float):
     try:
         v = json.loads((ROOT / "MEASURED_PEAKS.json").read_text())[key]
@@ -389,6 +494,8 @@ def main():
             out["serving"] = serving_bench(args.serving_requests)
         if "flow" in legs and args.flow and rank == 0:
             out["flow"] = flow_bench()
+        if "hybrid" in legs and rank == 0:
+            out["hybrid"] = hybrid_bench()
         if rank == 0:
             print(json.dumps(out))
         return
@@ -479,6 +586,8 @@ def main():
         out["serving"] = serving_bench(args.serving_requests)
     if args.flow and not args.small and rank == 0 and "flow" in legs:
         out["flow"] = flow_bench()
+    if not args.small and rank == 0 and "hybrid" in legs:
+        out["hybrid"] = hybrid_bench()
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         out["cpu_baseline"] = cpu_baseline(workloads.cascade_string_setup(N_CASCADES, WORKLOAD_SEED),
                                            args.cpu_seconds, os.cpu_count() or 1)

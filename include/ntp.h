@@ -363,6 +363,26 @@ ntp_status ntp_make_table(ntp_ctx* ctx, const ntp_hit* hits, uint64_t n_hits, co
                           float* group_cond, double* group_expec, uint64_t* group_count, uint64_t* group_hits,
                           void* stream);
 
+/* Flow conditions of every (event, module, PMT) with the module within
+   [d_min, d_max] of the event's vertex (the surrogate's domain): events are
+   cascades (position, direction of each ntp_source; log10_energy per event;
+   event_id may be NULL = the index).  Per row: cond[5] (the features of
+   ntp_make_table), cond_key = event_id << 32 | target_index << 8 | pmt
+   (the sampler's stream key), cond_tgeo = (|vertex - module| - R) n800 / c
+   (time = time residual + tgeo + event time), and the event index, target
+   index and 1-based PMT (these three may be NULL).  Modules are upright.
+   Rows are grouped by event: event_first (host, n_events + 1) are the
+   offsets; event_close (host, may be NULL) counts the modules closer than
+   d_min (outside the domain) per event.  Outputs device buffers; *n_cond
+   receives the total, above capacity nothing is written and
+   NTP_ERR_OVERFLOW returned.  No reference counterpart (the reference builds
+   flow inputs on the host, extended_cascade_model.jl:367-437). */
+ntp_status ntp_event_conditions(ntp_ctx* ctx, const ntp_source* events, const float* log10_energy,
+                                const uint32_t* event_id, int32_t n_events, float d_min, float d_max, float n800,
+                                float* cond, uint64_t* cond_key, float* cond_tgeo, int32_t* cond_event,
+                                int32_t* cond_target, int32_t* cond_pmt, uint64_t capacity, uint64_t* n_cond,
+                                uint64_t* event_first, int32_t* event_close, void* stream);
+
 /* ------------------------------------------------------------ tensor cores
  * C = A * B^T with BF16 A [M x K] and B [N x K] (row-major, K contiguous,
  * device pointers, 16-byte aligned rows: lda, ldb multiples of 8, K a
@@ -432,6 +452,21 @@ ntp_status ntp_flow_head(ntp_flow* flow, const float* params, const float* tres,
 ntp_status ntp_flow_evaluate(ntp_flow* flow, const float* cond, int32_t n_cond, const int32_t* cond_index,
                              const float* times, uint64_t n_tuples, float* logpdf, float* log_expec,
                              int32_t on_device);
+/* Sampling from the surrogate (the hits a PMT sees, as the MC would give
+   them after resample_simulation): per condition c a count N_c ~
+   Poisson(exp(log expectation)), then N_c times drawn from the flow (a
+   normal draw through the forward splines, rqs_univariate,
+   rq_spline_flow.jl:262-324).  Draws come from Philox streams keyed by seed
+   and cond_key[c], so a condition's hits do not depend on the other
+   conditions of the call.  Outputs grouped by condition in increasing c:
+   hit_cond (the condition index) and hit_time; counts (may be NULL) per
+   condition.  *n_hits receives the total; above capacity nothing is written
+   and NTP_ERR_OVERFLOW returned.  n_cond <= 1048576.  All buffers on the
+   host, or on the device when on_device != 0.  No reference counterpart:
+   the reference only evaluates the density. */
+ntp_status ntp_flow_sample(ntp_flow* flow, const float* cond, int32_t n_cond, const uint64_t* cond_key, uint64_t seed,
+                           uint64_t* counts, int32_t* hit_cond, float* hit_time, uint64_t capacity, uint64_t* n_hits,
+                           int32_t on_device);
 
 /* ------------------------------------------------------------------ serving
  * Continuous-batching event server (no reference counterpart; the reference

@@ -251,6 +251,7 @@ EXPORTED = (
     "ntp_pmt_summary",
     "ntp_resample",
     "ntp_make_table",
+    "ntp_event_conditions",
     "ntp_gemm_bf16",
     "ntp_flow_create",
     "ntp_flow_destroy",
@@ -263,6 +264,7 @@ EXPORTED = (
     "ntp_flow_forward",
     "ntp_flow_head",
     "ntp_flow_evaluate",
+    "ntp_flow_sample",
     "ntp_server_create",
     "ntp_server_destroy",
     "ntp_server_submit",
@@ -310,6 +312,10 @@ def _declare(lib: C.CDLL) -> None:
                                    C.POINTER(C.c_double), C.POINTER(C.c_double), C.POINTER(NtpTableSpec), vp, vp, vp,
                                    vp, vp, u64, C.POINTER(u64), vp, vp, vp, vp, vp]
     lib.ntp_make_table.restype = C.c_int
+    lib.ntp_event_conditions.argtypes = [vp, C.POINTER(NtpSource), C.POINTER(C.c_float), vp, i32, C.c_float,
+                                         C.c_float, C.c_float, vp, vp, vp, vp, vp, vp, u64, C.POINTER(u64), vp, vp,
+                                         vp]
+    lib.ntp_event_conditions.restype = C.c_int
     lib.ntp_flow_create.argtypes = [i32, C.POINTER(NtpFlowConfig), C.POINTER(vp)]
     lib.ntp_flow_destroy.argtypes = [vp]
     lib.ntp_flow_destroy.restype = None
@@ -324,8 +330,10 @@ def _declare(lib: C.CDLL) -> None:
     lib.ntp_flow_forward.argtypes = [vp, vp, i32, vp]
     lib.ntp_flow_head.argtypes = [vp, vp, vp, vp, vp, i32, C.POINTER(C.c_double), vp]
     lib.ntp_flow_evaluate.argtypes = [vp, vp, i32, vp, vp, u64, vp, vp, i32]
+    lib.ntp_flow_sample.argtypes = [vp, vp, i32, vp, u64, vp, vp, vp, u64, C.POINTER(u64), i32]
     for name in ("ntp_flow_create", "ntp_flow_get_layout", "ntp_flow_set_params", "ntp_flow_get_params",
-                 "ntp_flow_train_step", "ntp_flow_forward", "ntp_flow_head", "ntp_flow_evaluate"):
+                 "ntp_flow_train_step", "ntp_flow_forward", "ntp_flow_head", "ntp_flow_evaluate",
+                 "ntp_flow_sample"):
         getattr(lib, name).restype = C.c_int
     lib.ntp_server_create.argtypes = [vp, C.POINTER(NtpServerConfig), C.POINTER(vp)]
     lib.ntp_server_destroy.argtypes = [vp]

@@ -38,6 +38,7 @@
 #include <type_traits>
 #include <vector>
 
+#include "ntp_device.cuh"
 #include "ntp_internal.h"
 
 namespace ntp {
@@ -646,6 +647,99 @@ __global__ void logpdf_kernel(const float* __restrict__ knots, int L, int n_cond
     }
 }
 
+// ------------------------------------------------------------ sampling
+// rqs_univariate (rq_spline_flow.jl:262-324) on constrained knots: the
+// forward spline, linear outside the range
+template <int K>
+__device__ __forceinline__ float fwd_spline(const float* xp, const float* yp, const float* d, float x) {
+    if (x <= xp[0]) return (x - xp[0]) * d[0] + yp[0];
+    if (x >= xp[K]) return (x - xp[K]) * d[K] + yp[K];
+    const int k = find_bin<K>(xp, x);
+    const float w = xp[k + 1] - xp[k], h = yp[k + 1] - yp[k], s = h / w;
+    const float z = fminf(fmaxf((x - xp[k]) / w, 0.0f), 1.0f);
+    const float z1mz = z - z * z;
+    const float num = h * (s * z * z + d[k] * z1mz);
+    const float den = s + (d[k + 1] + d[k] - 2.0f * s) * z1mz;
+    return yp[k] + num / den;
+}
+
+constexpr uint32_t kDrawSample = 0x534D504Cu;  // "SMPL": time draws of the surrogate
+
+// Expected count exp(log expectation) -> Poisson count per condition, from the
+// stream of the condition's 64-bit key.
+__global__ void sample_count_kernel(const float* __restrict__ knots, int L, int K, int n,
+                                    const unsigned long long* __restrict__ ckey, uint2 key,
+                                    unsigned long long* __restrict__ counts) {
+    const int c = blockIdx.x * blockDim.x + threadIdx.x;
+    if (c >= n) return;
+    const float le = knots[static_cast<size_t>(c) * knot_row(L, K) + L * 3 * (K + 1) + 2];
+    const unsigned long long k = ckey[c];
+    counts[c] = static_cast<unsigned long long>(
+        poisson_draw(exp(static_cast<double>(le)), key, static_cast<uint32_t>(k), static_cast<uint32_t>(k >> 32)));
+}
+
+// Exclusive scan of n counts: per block of 1024 an in-block scan, the block
+// totals scanned by one block, then added (n <= 1024 * 1024).
+__global__ void scan_block_kernel(const unsigned long long* __restrict__ in, int n,
+                                  unsigned long long* __restrict__ out, unsigned long long* __restrict__ block_sum) {
+    __shared__ unsigned long long s[1024];
+    const int i = blockIdx.x * 1024 + threadIdx.x;
+    const unsigned long long v = i < n ? in[i] : 0ull;
+    s[threadIdx.x] = v;
+    __syncthreads();
+    for (int off = 1; off < 1024; off <<= 1) {
+        const unsigned long long t = threadIdx.x >= off ? s[threadIdx.x - off] : 0ull;
+        __syncthreads();
+        s[threadIdx.x] += t;
+        __syncthreads();
+    }
+    if (i < n) out[i] = s[threadIdx.x] - v;
+    if (threadIdx.x == 1023) block_sum[blockIdx.x] = s[1023];
+}
+
+__global__ void scan_add_kernel(unsigned long long* __restrict__ out, int n, const unsigned long long* __restrict__ block_off,
+                                unsigned long long* __restrict__ total, int n_blocks) {
+    const int i = blockIdx.x * 1024 + threadIdx.x;
+    if (i < n) out[i] += block_off[blockIdx.x];
+    if (i == 0) *total = block_off[n_blocks];
+}
+
+// One thread per drawn hit: its condition by binary search on the offsets,
+// x ~ Normal(shift, scale) (Box-Muller on the stream of the condition's key
+// and the draw index), then the forward splines of layers 0 .. L-1.
+template <int K>
+__global__ void sample_draw_kernel(const float* __restrict__ knots, int L, int n,
+                                   const unsigned long long* __restrict__ ckey, uint2 key,
+                                   const unsigned long long* __restrict__ offsets, unsigned long long total,
+                                   int32_t* __restrict__ hit_cond, float* __restrict__ hit_time) {
+    const int row = knot_row(L, K);
+    for (unsigned long long h = blockIdx.x * static_cast<unsigned long long>(blockDim.x) + threadIdx.x; h < total;
+         h += static_cast<unsigned long long>(gridDim.x) * blockDim.x) {
+        int lo = 0, hi = n - 1;  // last condition with offsets[c] <= h
+        while (lo < hi) {
+            const int mid = (lo + hi + 1) >> 1;
+            if (offsets[mid] <= h) lo = mid;
+            else hi = mid - 1;
+        }
+        const int c = lo;
+        const unsigned long long j = h - offsets[c];
+        const unsigned long long k = ckey[c];
+        const uint4 r = philox4x32_10(make_uint4(kDrawSample ^ static_cast<uint32_t>(j >> 32), static_cast<uint32_t>(j),
+                                                 static_cast<uint32_t>(k), static_cast<uint32_t>(k >> 32)),
+                                      key);
+        const float u1 = u01(r.x), u2 = u01(r.y);
+        const float z = sqrtf(-2.0f * logf(u1)) * cospif(2.0f * u2);
+        const float* o = knots + static_cast<size_t>(c) * row;
+        float y = o[L * 3 * (K + 1)] + o[L * 3 * (K + 1) + 1] * z;
+        for (int li = 0; li < L; ++li) {
+            const float* xp = o + li * 3 * (K + 1);
+            y = fwd_spline<K>(xp, xp + K + 1, xp + 2 * (K + 1), y);
+        }
+        hit_cond[h] = c;
+        hit_time[h] = y;
+    }
+}
+
 int blocks_for(long long n, int t = 256) { return static_cast<int>((n + t - 1) / t); }
 
 }  // namespace
@@ -1166,6 +1260,85 @@ ntp_status ntp_flow_evaluate(ntp_flow* f, const float* cond, int32_t n_cond, con
         }
     }
     return check_gemm(f);
+}
+
+
+ntp_status ntp_flow_sample(ntp_flow* f, const float* cond, int32_t n_cond, const uint64_t* cond_key, uint64_t seed,
+                           uint64_t* counts, int32_t* hit_cond, float* hit_time, uint64_t capacity, uint64_t* n_hits,
+                           int32_t on_device) {
+    if (n_hits) *n_hits = 0;
+    if (!f || !cond || !cond_key || n_cond <= 0) return NTP_ERR_INVALID;
+    if (n_cond > (1 << 20)) {
+        f->err = "ntp_flow_sample: at most 1048576 conditions per call";
+        return NTP_ERR_INVALID;
+    }
+    F_CUDA(f, cudaSetDevice(f->device));
+    cudaStream_t st = f->stream;
+    // knots of every condition (the inference pass of ntp_flow_evaluate)
+    F_OK(ntp_flow_evaluate(f, cond, n_cond, nullptr, nullptr, 0, nullptr, nullptr, on_device));
+    const int nb = (n_cond + 1023) / 1024;
+    // scratch: keys u64[n] | counts u64[n] | offsets u64[n] | block sums u64[nb + 1] x 2 | total
+    const size_t n = static_cast<size_t>(n_cond);
+    unsigned long long* scratch = nullptr;
+    F_CUDA(f, dalloc(&scratch, 3 * n + 2 * (nb + 1) + 1));
+    auto run = [&]() -> ntp_status {
+        unsigned long long* d_key = scratch;
+        unsigned long long* d_cnt = scratch + n;
+        unsigned long long* d_off = scratch + 2 * n;
+        unsigned long long* d_bs = scratch + 3 * n;
+        unsigned long long* d_bo = d_bs + nb + 1;
+        unsigned long long* d_tot = d_bo + nb + 1;
+        F_CUDA(f, cudaMemcpyAsync(d_key, cond_key, 8 * n, on_device ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice,
+                                  st));
+        const uint2 key = make_uint2(static_cast<uint32_t>(seed), static_cast<uint32_t>(seed >> 32));
+        ntp::sample_count_kernel<<<ntp::blocks_for(n_cond), 256, 0, st>>>(f->knots, f->L, f->K, n_cond, d_key, key,
+                                                                          d_cnt);
+        F_CUDA(f, cudaGetLastError());
+        ntp::scan_block_kernel<<<nb, 1024, 0, st>>>(d_cnt, n_cond, d_off, d_bs);
+        ntp::scan_block_kernel<<<1, 1024, 0, st>>>(d_bs, nb, d_bo, d_bs + nb);  // nb <= 1024
+        F_CUDA(f, cudaMemcpyAsync(d_bo + nb, d_bs + nb, 8, cudaMemcpyDeviceToDevice, st));
+        ntp::scan_add_kernel<<<nb, 1024, 0, st>>>(d_off, n_cond, d_bo, d_tot, nb);
+        F_CUDA(f, cudaGetLastError());
+        unsigned long long total = 0;
+        F_CUDA(f, cudaMemcpyAsync(&total, d_tot, 8, cudaMemcpyDeviceToHost, st));
+        if (counts)
+            F_CUDA(f, cudaMemcpyAsync(counts, d_cnt, 8 * n, on_device ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost,
+                                      st));
+        F_CUDA(f, cudaStreamSynchronize(st));
+        if (n_hits) *n_hits = total;
+        if (total > capacity) {
+            f->err = "ntp_flow_sample: capacity " + std::to_string(capacity) + " below " + std::to_string(total);
+            return NTP_ERR_OVERFLOW;
+        }
+        if (total == 0) return NTP_OK;
+        if (!hit_cond || !hit_time) return NTP_ERR_INVALID;
+        int32_t* d_hc = hit_cond;
+        float* d_ht = hit_time;
+        void* stage = nullptr;
+        if (!on_device) {
+            F_CUDA(f, cudaMalloc(&stage, 8 * total));
+            d_hc = static_cast<int32_t*>(stage);
+            d_ht = reinterpret_cast<float*>(static_cast<int32_t*>(stage) + total);
+        }
+        const int grid = static_cast<int>(std::min<unsigned long long>((total + 255) / 256, 152ull * 32));
+        cudaError_t e = cudaSuccess;
+        with_bins(f->K, [&](auto kc) {
+            ntp::sample_draw_kernel<decltype(kc)::value>
+                <<<grid, 256, 0, st>>>(f->knots, f->L, n_cond, d_key, key, d_off, total, d_hc, d_ht);
+            e = cudaGetLastError();
+        });
+        if (e == cudaSuccess && !on_device) {
+            e = cudaMemcpyAsync(hit_cond, d_hc, 4 * total, cudaMemcpyDeviceToHost, st);
+            if (e == cudaSuccess) e = cudaMemcpyAsync(hit_time, d_ht, 4 * total, cudaMemcpyDeviceToHost, st);
+        }
+        if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+        if (stage) cudaFree(stage);
+        if (e != cudaSuccess) return ferr(f, e, "ntp_flow_sample");
+        return NTP_OK;
+    };
+    const ntp_status s2 = run();
+    cudaFree(scratch);
+    return s2;
 }
 
 }  // extern "C"

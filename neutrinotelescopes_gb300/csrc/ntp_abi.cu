@@ -1147,4 +1147,85 @@ ntp_status ntp_make_table(ntp_ctx* ctx, const ntp_hit* hits, uint64_t n, const d
     return NTP_OK;
 }
 
+
+ntp_status ntp_event_conditions(ntp_ctx* ctx, const ntp_source* events, const float* log10_energy,
+                                const uint32_t* event_id, int32_t n_events, float d_min, float d_max, float n800,
+                                float* cond, uint64_t* cond_key, float* cond_tgeo, int32_t* cond_event,
+                                int32_t* cond_target, int32_t* cond_pmt, uint64_t capacity, uint64_t* n_cond,
+                                uint64_t* event_first, int32_t* event_close, void* stream) {
+    if (!ctx) return NTP_ERR_INVALID;
+    if (n_cond) *n_cond = 0;
+    if (!ctx->have_targets) {
+        ctx->err = "ntp_event_conditions: targets must be set first";
+        return NTP_ERR_NOT_READY;
+    }
+    if (n_events <= 0 || !events || !log10_energy || !(d_max >= d_min) || !(n800 > 0.0f))
+        return invalid(ctx, "ntp_event_conditions: need events, energies, d_max >= d_min, n800 > 0");
+    cudaSetDevice(ctx->device);
+    cudaStream_t st = pick_stream(ctx, stream);
+    const size_t ne = static_cast<size_t>(n_events);
+    // host: packed events and the PMT axes of upright modules
+    struct EventIn {
+        float px, py, pz, dx, dy, dz, log10e;
+        uint32_t id;
+    };
+    static_assert(sizeof(EventIn) == 32, "event record");
+    if (ntp::event_in_size() != sizeof(EventIn)) return invalid(ctx, "ntp_event_conditions: event layout");
+    std::vector<EventIn> ev(ne);
+    for (size_t e = 0; e < ne; ++e) {
+        const ntp_source& s = events[e];
+        ev[e] = EventIn{s.position[0], s.position[1], s.position[2], s.direction[0], s.direction[1], s.direction[2],
+                        log10_energy[e], event_id ? event_id[e] : static_cast<uint32_t>(e)};
+    }
+    const size_t npc = ctx->pmt_coords.size() / 2;
+    std::vector<float> axes(3 * std::max<size_t>(npc, 1), 0.0f);
+    for (size_t j = 0; j < npc; ++j) {
+        const float th = ctx->pmt_coords[2 * j], ph = ctx->pmt_coords[2 * j + 1];
+        axes[3 * j] = std::cos(ph) * std::sin(th);
+        axes[3 * j + 1] = std::sin(ph) * std::sin(th);
+        axes[3 * j + 2] = std::cos(th);
+    }
+    // scratch: events | axes | rows u64[ne] | fill u64[ne] | first u64[ne+1] | close i32[ne]
+    size_t off = 0;
+    auto take = [&](size_t bytes) { size_t o = off; off += (bytes + 255) / 256 * 256; return o; };
+    const size_t o_ev = take(sizeof(EventIn) * ne), o_ax = take(4 * axes.size()), o_rows = take(8 * ne);
+    const size_t o_fill = take(8 * ne), o_first = take(8 * (ne + 1)), o_close = take(4 * ne);
+    NTP_CUDA(ctx, ensure(ctx->d_scratch, ctx->scratch_bytes, off));
+    unsigned char* sc = static_cast<unsigned char*>(ctx->d_scratch);
+    auto u64p = [&](size_t o) { return reinterpret_cast<unsigned long long*>(sc + o); };
+    NTP_CUDA(ctx, cudaMemcpyAsync(sc + o_ev, ev.data(), sizeof(EventIn) * ne, cudaMemcpyHostToDevice, st));
+    NTP_CUDA(ctx, cudaMemcpyAsync(sc + o_ax, axes.data(), 4 * axes.size(), cudaMemcpyHostToDevice, st));
+    NTP_CUDA(ctx, cudaMemsetAsync(sc + o_rows, 0, o_first - o_rows, st));  // rows, fill
+    NTP_CUDA(ctx, cudaMemsetAsync(sc + o_close, 0, 4 * ne, st));
+    NTP_CUDA(ctx, ntp::launch_event_conditions_count(sc + o_ev, n_events, ctx->d_tgt, ctx->d_kind, ctx->d_npmt,
+                                                     ctx->n_tgt, d_min, d_max, u64p(o_rows),
+                                                     reinterpret_cast<int*>(sc + o_close), st));
+    std::vector<unsigned long long> rows(ne), first(ne + 1);
+    std::vector<int32_t> close(ne);
+    NTP_CUDA(ctx, cudaMemcpyAsync(rows.data(), u64p(o_rows), 8 * ne, cudaMemcpyDeviceToHost, st));
+    NTP_CUDA(ctx, cudaMemcpyAsync(close.data(), sc + o_close, 4 * ne, cudaMemcpyDeviceToHost, st));
+    NTP_CUDA(ctx, cudaStreamSynchronize(st));
+    first[0] = 0;
+    for (size_t e = 0; e < ne; ++e) first[e + 1] = first[e] + rows[e];
+    if (event_first) std::copy(first.begin(), first.end(), event_first);
+    if (event_close) std::copy(close.begin(), close.end(), event_close);
+    const unsigned long long total = first[ne];
+    if (n_cond) *n_cond = total;
+    if (total > capacity) {
+        ctx->err = "ntp_event_conditions: capacity " + std::to_string(capacity) + " below " + std::to_string(total);
+        return NTP_ERR_OVERFLOW;
+    }
+    if (total == 0) return NTP_OK;
+    if (!cond || !cond_key) return invalid(ctx, "ntp_event_conditions: NULL output");
+    NTP_CUDA(ctx, cudaMemcpyAsync(u64p(o_first), first.data(), 8 * (ne + 1), cudaMemcpyHostToDevice, st));
+    const float tgeo_scale = n800 / 0.299792458f;
+    NTP_CUDA(ctx, ntp::launch_event_conditions_fill(sc + o_ev, n_events, ctx->d_tgt, ctx->d_radius, ctx->d_kind,
+                                                    ctx->d_npmt, ctx->d_pmtoff, reinterpret_cast<float*>(sc + o_ax),
+                                                    ctx->n_tgt, d_min, d_max, tgeo_scale, u64p(o_first), u64p(o_fill),
+                                                    cond, reinterpret_cast<unsigned long long*>(cond_key), cond_tgeo,
+                                                    cond_event, cond_target, cond_pmt, st));
+    NTP_CUDA(ctx, cudaStreamSynchronize(st));
+    return NTP_OK;
+}
+
 }  // extern "C"

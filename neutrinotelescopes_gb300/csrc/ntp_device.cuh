@@ -50,6 +50,47 @@ __device__ __forceinline__ float u01(uint32_t w) {
     return (static_cast<float>(w >> 9) + 0.5f) * (1.0f / 8388608.0f);
 }
 
+// 53 random bits from two Philox words: a double on the open interval (0, 1).
+__device__ __forceinline__ double u01_53(uint32_t a, uint32_t b) {
+    const unsigned long long m = (static_cast<unsigned long long>(a) << 21) ^ (b >> 11);
+    return (static_cast<double>(m & ((1ull << 53) - 1)) + 0.5) * (1.0 / 9007199254740992.0);
+}
+
+constexpr uint32_t kDrawPoisson = 0x504F4953u;  // "POIS": Poisson counts
+constexpr int kPoissonAttempts = 64;
+
+// Poisson(lam) from the Philox stream (kDrawPoisson, lo, attempt, hi) under
+// key: inversion below a mean of 30, above the transformed rejection of
+// Hormann (1993, "PTRS") with at most kPoissonAttempts tries (then the
+// rounded mean).
+__device__ __forceinline__ double poisson_draw(double lam, uint2 key, uint32_t lo, uint32_t hi) {
+    if (!(lam > 0.0)) return 0.0;
+    if (lam < 30.0) {
+        const uint4 r = philox4x32_10(make_uint4(kDrawPoisson, lo, 0u, hi), key);
+        const double u = u01_53(r.x, r.y);
+        double p = exp(-lam), F = p, k = 0.0;
+        while (u > F && k < 1000.0) {
+            k += 1.0;
+            p *= lam / k;
+            F += p;
+        }
+        return k;
+    }
+    const double slam = sqrt(lam), loglam = log(lam);
+    const double b = 0.931 + 2.53 * slam, a = -0.059 + 0.02483 * b;
+    const double invalpha = 1.1239 + 1.1328 / (b - 3.4), vr = 0.9277 - 3.6224 / (b - 2.0);
+    for (int t = 0; t < kPoissonAttempts; ++t) {
+        const uint4 r = philox4x32_10(make_uint4(kDrawPoisson, lo, static_cast<uint32_t>(t) + 1u, hi), key);
+        const double U = u01_53(r.x, r.y) - 0.5, V = u01_53(r.z, r.w);
+        const double us = 0.5 - fabs(U);
+        const double k = floor((2.0 * a / us + b) * U + lam + 0.43);
+        if (us >= 0.07 && V <= vr) return k;
+        if (k < 0.0 || (us < 0.013 && V > us)) continue;
+        if (log(V) + log(invalpha) - log(a / (us * us) + b) <= -lam + k * loglam - lgamma(k + 1.0)) return k;
+    }
+    return floor(lam + 0.5);
+}
+
 struct V3 {
     float x, y, z;
 };

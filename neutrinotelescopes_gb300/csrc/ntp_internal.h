@@ -170,6 +170,19 @@ cudaError_t launch_table_rows(unsigned long long n_hit_rows, const int32_t* og, 
                               const float* gcond, float* cond, float* tres, float* nhits, int32_t* has_time,
                               int32_t* row_group, cudaStream_t st);
 
+// flow conditions of (event, module, PMT) triples (surrogate.cu); events are
+// packed as {position[3], direction[3], log10 E, id (u32)} (event_in_size bytes)
+size_t event_in_size();
+cudaError_t launch_event_conditions_count(const void* events, int n_events, const float4* tg, const int* kind,
+                                          const int* npmt, int n_targets, float d_min, float d_max,
+                                          unsigned long long* ev_rows, int* ev_close, cudaStream_t st);
+cudaError_t launch_event_conditions_fill(const void* events, int n_events, const float4* tg, const float* radius,
+                                         const int* kind, const int* npmt, const int* pmt_off, const float* axes,
+                                         int n_targets, float d_min, float d_max, float tgeo_scale,
+                                         const unsigned long long* ev_first, unsigned long long* ev_fill, float* cond,
+                                         unsigned long long* ckey, float* ctgeo, int32_t* cev, int32_t* ctgt,
+                                         int32_t* cpmt, cudaStream_t st);
+
 // resample_simulation passes (resample.cu)
 cudaError_t launch_resample_group(const ntp_hit* hits, unsigned long long n, const int32_t* pmt, const double* w,
                                   const uint2* sorted_ids, int n_targets, int max_pmts, int32_t* group, double* wsum,

@@ -30,46 +30,10 @@ namespace {
 
 constexpr int kBlock = 256;
 constexpr uint32_t kDrawResampleKey = 0x52534B59u;  // "RSKY": per-hit key stream
-constexpr uint32_t kDrawPoisson = 0x504F4953u;      // "POIS": per-group count stream
-constexpr int kPoissonAttempts = 64;
-
-__device__ __forceinline__ double u01_53(uint32_t a, uint32_t b) {
-    // 53 random bits, open interval (0, 1)
-    const unsigned long long m = (static_cast<unsigned long long>(a) << 21) ^ (b >> 11);
-    return (static_cast<double>(m & ((1ull << 53) - 1)) + 0.5) * (1.0 / 9007199254740992.0);
-}
 
 __device__ __forceinline__ unsigned long long ordered(double x) {
     const unsigned long long b = static_cast<unsigned long long>(__double_as_longlong(x));
     return (b >> 63) ? ~b : (b | 0x8000000000000000ull);
-}
-
-__device__ double poisson(double lam, uint2 key, uint32_t group) {
-    if (!(lam > 0.0)) return 0.0;
-    if (lam < 30.0) {
-        const uint4 r = philox4x32_10(make_uint4(kDrawPoisson, group, 0u, 0u), key);
-        const double u = u01_53(r.x, r.y);
-        double p = exp(-lam), F = p, k = 0.0;
-        while (u > F && k < 1000.0) {
-            k += 1.0;
-            p *= lam / k;
-            F += p;
-        }
-        return k;
-    }
-    const double slam = sqrt(lam), loglam = log(lam);
-    const double b = 0.931 + 2.53 * slam, a = -0.059 + 0.02483 * b;
-    const double invalpha = 1.1239 + 1.1328 / (b - 3.4), vr = 0.9277 - 3.6224 / (b - 2.0);
-    for (int t = 0; t < kPoissonAttempts; ++t) {
-        const uint4 r = philox4x32_10(make_uint4(kDrawPoisson, group, static_cast<uint32_t>(t) + 1u, 0u), key);
-        const double U = u01_53(r.x, r.y) - 0.5, V = u01_53(r.z, r.w);
-        const double us = 0.5 - fabs(U);
-        const double k = floor((2.0 * a / us + b) * U + lam + 0.43);
-        if (us >= 0.07 && V <= vr) return k;
-        if (k < 0.0 || (us < 0.013 && V > us)) continue;
-        if (log(V) + log(invalpha) - log(a / (us * us) + b) <= -lam + k * loglam - lgamma(k + 1.0)) return k;
-    }
-    return floor(lam + 0.5);
 }
 
 __device__ __forceinline__ double hit_key(const ntp_hit* hits, unsigned long long i, double w, uint2 key) {
@@ -109,7 +73,7 @@ __global__ void draw_kernel(int n_groups, const double* __restrict__ wsum, const
                             double downsample, uint2 key, unsigned long long* __restrict__ nsel) {
     const int g = blockIdx.x * blockDim.x + threadIdx.x;
     if (g >= n_groups) return;
-    const double k = poisson(wsum[g] * downsample, key, static_cast<uint32_t>(g));
+    const double k = poisson_draw(wsum[g] * downsample, key, static_cast<uint32_t>(g), 0u);
     const unsigned long long m = npos[g];
     nsel[g] = k < static_cast<double>(m) ? static_cast<unsigned long long>(k) : m;
 }

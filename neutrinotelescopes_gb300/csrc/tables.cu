@@ -43,11 +43,6 @@ __device__ __forceinline__ unsigned long long ordered_key(double x) {
     return (b >> 63) ? ~b : (b | 0x8000000000000000ull);
 }
 
-__device__ __forceinline__ double u01_53(uint32_t a, uint32_t b) {
-    const unsigned long long m = (static_cast<unsigned long long>(a) << 21) ^ (b >> 11);
-    return (static_cast<double>(m & ((1ull << 53) - 1)) + 0.5) * (1.0 / 9007199254740992.0);
-}
-
 // First PMT (0-based) of orientation r of simulation s whose cone contains the
 // unit direction (ux, uy, uz) from the module centre; -1 for none.
 __device__ __forceinline__ int table_pmt(const float* __restrict__ axes, int s, int r, int R, int P, float ux,

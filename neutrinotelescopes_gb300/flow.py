@@ -281,6 +281,62 @@ class RQNormFlow:
                                                    le.ctypes.data if le is not None else None, 0))
         return (out, le) if log_expec else out
 
+    MAX_SAMPLE_CONDITIONS = 1 << 20
+
+    def sample_hits(self, cond, keys, seed: int = 0, capacity: int | None = None):
+        """Hits the surrogate predicts: per condition a Poisson count of its
+        expectation and that many times drawn from its density.  keys:
+        64-bit stream key per condition.  Returns (counts, hit condition
+        index, hit time) -- numpy arrays, or CUDA tensors for CUDA inputs.
+        More than 2^20 conditions are sampled in pieces (the draws are keyed
+        by condition, so the result is the same)."""
+        n = int(cond.shape[0])
+        step = self.MAX_SAMPLE_CONDITIONS
+        if n > step:
+            parts = [self.sample_hits(cond[s:s + step], keys[s:s + step], seed, capacity) for s in range(0, n, step)]
+            if _is_device(cond):
+                import torch
+                offs = [s for s in range(0, n, step)]
+                return (torch.cat([p[0] for p in parts]), torch.cat([p[1] + o for p, o in zip(parts, offs)]),
+                        torch.cat([p[2] for p in parts]))
+            offs = [s for s in range(0, n, step)]
+            return (np.concatenate([p[0] for p in parts]),
+                    np.concatenate([p[1] + np.int32(o) for p, o in zip(parts, offs)]),
+                    np.concatenate([p[2] for p in parts]))
+        dev = _is_device(cond)
+        n_hits = C.c_uint64()
+        if dev:
+            import torch
+            cnt = torch.empty(n, dtype=torch.int64, device=cond.device)
+            cap = int(capacity if capacity is not None else 1 << 20)
+            while True:
+                hc = torch.empty(max(cap, 1), dtype=torch.int32, device=cond.device)
+                ht = torch.empty(max(cap, 1), dtype=torch.float32, device=cond.device)
+                torch.cuda.synchronize()
+                st = self.lib.ntp_flow_sample(self._h, cond.data_ptr(), n, keys.data_ptr(), int(seed) & (2 ** 64 - 1),
+                                              cnt.data_ptr(), hc.data_ptr(), ht.data_ptr(), cap, C.byref(n_hits), 1)
+                if st == _abi.NTP_ERR_OVERFLOW and capacity is None:
+                    cap = int(n_hits.value)
+                    continue
+                self._check(st)
+                m = int(n_hits.value)
+                return cnt, hc[:m], ht[:m]
+        cond = _f32(cond)
+        keys = np.ascontiguousarray(keys, np.uint64)
+        cnt = np.empty(n, np.uint64)
+        cap = int(capacity if capacity is not None else 1 << 20)
+        while True:
+            hc = np.empty(max(cap, 1), np.int32)
+            ht = np.empty(max(cap, 1), np.float32)
+            st = self.lib.ntp_flow_sample(self._h, cond.ctypes.data, n, keys.ctypes.data, int(seed) & (2 ** 64 - 1),
+                                          cnt.ctypes.data, hc.ctypes.data, ht.ctypes.data, cap, C.byref(n_hits), 0)
+            if st == _abi.NTP_ERR_OVERFLOW and capacity is None:
+                cap = int(n_hits.value)
+                continue
+            self._check(st)
+            m = int(n_hits.value)
+            return cnt, hc[:m], ht[:m]
+
     def __call__(self, x, cond, pred_log_expec: bool = False):
         """The reference's model call (extended_cascade_model.jl:110-125):
         per sample i the log-pdf of x[i] under cond[i], and with

@@ -7,7 +7,7 @@ point_cone:      1e6 photons from the origin on a 41.2 degree cone around +z,
 string_grid:     nx x ny vertical strings spaced `spacing` m on a square grid,
                  n_modules per string spaced dz m (the serving detector is
                  10 x 10 strings, 50 m, 20 modules 15 m apart; the hybrid
-                 detector 100 strings x 80 modules).
+                 detector 10 x 10 strings, 50 m, 80 modules 15 m apart).
 cascade_string:  electromagnetic cascades, energy log-uniform 1e3-1e5 GeV,
                  1.3e5 photons/GeV, gamma longitudinal profile a = 2 + 0.6 ln E,
                  b = 0.63, radiation length 0.36 m, isotropic direction, vertex
@@ -96,6 +96,14 @@ def serving_requests(n: int = 4096, seed: int = 2, rate_hz: float = 200.0, ph_lo
         src = ExtendedCherenkovEmitter(pos, (st * np.cos(phi), st * np.sin(phi), ct), 0.0, photons, lp)
         out.append((float(t[i]), i + 1, src))
     return out
+
+
+def hybrid_setup(**kw) -> PhotonPropSetup:
+    """The hybrid detector: 10 x 10 strings, 50 m apart, 80 modules 15 m apart (8000 POM modules x 16 PMTs),
+    simple water."""
+    return PhotonPropSetup([], string_grid(10, 10, 50.0, 80, 15.0), make_simple_water(),
+                           InverseSquareSpectrum(300.0, 600.0),
+                           wavelength_acceptance=p_one_pmt_acc.resampled(300.0, 600.0, 31), **kw)
 
 
 def serving_setup(**kw) -> PhotonPropSetup:

@@ -1,0 +1,125 @@
+"""The surrogate path: flow conditions of (event, module, PMT) triples
+(ntp_event_conditions) against a numpy computation, the sampler
+(ntp_flow_sample) against the flow's own density and count head, sampling
+keyed by condition (independent of the batch), and the hybrid simulator's
+domain split (flow inside, MC outside)."""
+import math
+
+import numpy as np
+import pytest
+
+torch = pytest.importorskip("torch")
+
+from neutrinotelescopes_gb300 import workloads  # noqa: E402
+from neutrinotelescopes_gb300.detection import MultiPMTDetector, make_pom_pmt_coordinates  # noqa: E402
+from neutrinotelescopes_gb300.flow import RQNormFlow, RQNormFlowHParams, flow_features  # noqa: E402
+from neutrinotelescopes_gb300.lightyield import ExtendedCherenkovEmitter, LongitudinalParameterisation  # noqa: E402
+from neutrinotelescopes_gb300.medium import make_simple_water  # noqa: E402
+from neutrinotelescopes_gb300.photon_prop import PhotonPropSetup  # noqa: E402
+from neutrinotelescopes_gb300.spectrum import InverseSquareSpectrum  # noqa: E402
+from neutrinotelescopes_gb300.surrogate import HybridSimulator  # noqa: E402
+
+pytestmark = pytest.mark.gpu
+
+
+def _cascade(pos, d, e=1e3):
+    lp = LongitudinalParameterisation(a=float(np.float32(2.0 + 0.6 * math.log(e))), b=0.63, lrad=0.36)
+    return ExtendedCherenkovEmitter(pos, d, 0.0, int(1.3e5 * e), lp)
+
+
+def _setup():
+    coords = make_pom_pmt_coordinates()
+    targets = [MultiPMTDetector((x, 0.0, z), 0.21, workloads.PMT_AREA, coords, 1 + i)
+               for i, (x, z) in enumerate([(0.0, 0.0), (0.0, 15.0), (0.0, 30.0), (40.0, 0.0), (40.0, 15.0)])]
+    return PhotonPropSetup([], targets, make_simple_water(), InverseSquareSpectrum(300.0, 600.0))
+
+
+def _flow(log_expec: float):
+    fl = RQNormFlow(RQNormFlowHParams(batch_size=4096, seed=3))
+    fl.init_output_bias(shift=20.0, log_expec=log_expec)
+    return fl
+
+
+def test_event_conditions_match_numpy():
+    setup = _setup()
+    d = np.array([0.3, -0.5, 0.81])
+    d /= np.linalg.norm(d)
+    events = [_cascade((5.0, 3.0, 10.0), tuple(d)), _cascade((0.0, 0.2, 15.5), (0.0, 0.0, 1.0)),
+              _cascade((300.0, 0.0, 0.0), (1.0, 0.0, 0.0))]
+    le = [3.0, 4.5, 2.5]
+    with _flow(1.0) as fl:
+        sim = HybridSimulator(setup, fl, d_range=(1.0, 200.0))
+        cond, key, tgeo, tgt, pmt, first, close = sim.conditions(events, le, [7, 8, 9])
+    cond, key, tgeo = cond.cpu().numpy(), key.cpu().numpy(), tgeo.cpu().numpy()
+    tgt, pmt = tgt.cpu().numpy(), pmt.cpu().numpy()
+    # event 0 sees all 5 modules, event 1 is 0.55 m from module 2 (outside the domain), event 2 is beyond 200 m
+    assert list(first) == [0, 80, 144, 144] and list(close) == [0, 1, 0]
+    coords = make_pom_pmt_coordinates().astype(np.float32)
+    th, ph = coords[0], coords[1]
+    axes = np.stack([np.cos(ph) * np.sin(th), np.sin(ph) * np.sin(th), np.cos(th)], -1).astype(np.float64)
+    for r in range(len(key)):
+        e = 0 if r < 80 else 1
+        src = events[e]
+        k, j = int(tgt[r]), int(pmt[r]) - 1
+        assert key[r] == ((7 + e) << 32) | (k << 8) | j
+        u = np.asarray(src.position, np.float64) - np.asarray(setup.targets[k].position)
+        dist = np.linalg.norm(u)
+        u /= dist
+        v = np.asarray(src.direction, np.float64)
+        a = axes[j]
+        e1, e2 = v - (v @ u) * u, a - (a @ u) * u
+        phi = math.atan2(np.cross(e1, e2) @ u, e1 @ e2) % (2 * math.pi)
+        want = flow_features([dist], [v @ u], [a @ u], [phi], [le[e]])[0]
+        if abs(phi - 2 * math.pi) < 1e-4 or phi < 1e-4:
+            want[3] = cond[r, 3]  # the azimuth wraps at 0 / 2 pi
+        np.testing.assert_allclose(cond[r], want, atol=2e-5)
+        assert tgeo[r] == pytest.approx((dist - 0.21) * 1.35 / 0.299792458, rel=1e-5)
+
+
+def test_sampler_follows_the_density_and_counts():
+    with _flow(math.log(40.0)) as fl:
+        n = 2000
+        c = np.repeat(np.array([[0.1, -0.3, 0.6, 0.2, -0.1]], np.float32), n, axis=0)
+        keys = np.arange(n, dtype=np.uint64) + (np.uint64(5) << np.uint64(32))
+        cnt, hc, ht = fl.sample_hits(c, keys, seed=11)
+        _, le = fl.logpdf(c[:1], np.zeros(1, np.int32), np.zeros(1, np.float32), log_expec=True)
+        lam = math.exp(float(le[0]))
+        grid = np.linspace(-200.0, 1700.0, 380001).astype(np.float32)
+        lp = fl.logpdf(c[:1], np.zeros(grid.size, np.int32), grid).astype(np.float64)
+    cnt = cnt.astype(np.float64)
+    assert abs(cnt.mean() - lam) < 5 * math.sqrt(lam / n)
+    assert abs(cnt.var() / lam - 1) < 0.15
+    assert hc.size == cnt.sum() and np.all(np.diff(hc) >= 0)
+    pdf = np.exp(lp)
+    cdf = np.concatenate([[0.0], np.cumsum((pdf[1:] + pdf[:-1]) * 0.5 * np.diff(grid))])
+    s = np.sort(ht.astype(np.float64))
+    F = np.interp(s, grid, cdf / cdf[-1])
+    ks = np.max(np.maximum(np.arange(1, s.size + 1) / s.size - F, F - np.arange(s.size) / s.size))
+    assert ks < 1.63 / math.sqrt(s.size) + 2e-3, ks   # 1 % level plus grid error
+
+
+def test_sampling_is_keyed_by_condition():
+    with _flow(math.log(8.0)) as fl:
+        rng = np.random.default_rng(2)
+        c = rng.uniform(-1, 1, (300, 5)).astype(np.float32)
+        keys = rng.integers(0, 2 ** 62, 300).astype(np.uint64)
+        cnt1, hc1, ht1 = fl.sample_hits(c, keys, seed=4)
+        sel = np.arange(100, 200)
+        cnt2, hc2, ht2 = fl.sample_hits(c[sel][::-1].copy(), keys[sel][::-1].copy(), seed=4)
+    for i_new, i_old in enumerate(sel[::-1]):
+        a = ht1[hc1 == i_old]
+        b = ht2[hc2 == i_new]
+        assert cnt1[i_old] == cnt2[i_new]
+        np.testing.assert_array_equal(a, b)
+
+
+def test_hybrid_domain_split():
+    setup = _setup()
+    events = [(0, _cascade((5.0, 3.0, 10.0), (0.0, 0.0, 1.0), e=200.0), 2.3),
+              (1, _cascade((0.0, 0.3, 15.0), (0.0, 0.0, 1.0), e=200.0), 2.3)]
+    with _flow(math.log(3.0)) as fl:
+        sim = HybridSimulator(setup, fl)
+        out = sim.simulate(events)
+    assert [o.method for o in out] == ["flow", "mc"]
+    assert out[0].n_hits == int(out[0].time.numel())
+    assert np.all(out[0].target.cpu().numpy() < 5) and np.all((out[0].pmt.cpu().numpy() >= 1))
