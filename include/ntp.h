@@ -417,6 +417,7 @@ typedef struct ntp_flow_config {
     float t_min, t_max;     /* spline range (ns); linear tails outside                        */
     float lr, beta1, beta2, eps; /* Adam                                                      */
     float grad_clip;        /* per-sample bound on |dL/draw outputs| x batch (0 = none), e.g. 1e3 */
+    float count_weight;     /* weight of the Poisson count term in the loss (1 = the reference's)  */
     uint64_t seed;          /* weight initialisation                                           */
 } ntp_flow_config;
 

@@ -195,6 +195,7 @@ class NtpFlowConfig(C.Structure):
         ("beta2", C.c_float),
         ("eps", C.c_float),
         ("grad_clip", C.c_float),
+        ("count_weight", C.c_float),
         ("seed", C.c_uint64),
     ]
 

@@ -193,6 +193,15 @@ __device__ __forceinline__ void constrain(const float* __restrict__ p, float r0,
     }
     kn.xp[K] = r1;
     kn.yp[K] = r1;
+    // The FP32 running sum can reach the pinned last knot when the last bins
+    // are at the minimum width (11 roundings of up to half an ulp near r1
+    // exceed kMinBin): keep the knots strictly increasing (the reference sums
+    // in Float64, where this cannot happen)
+#pragma unroll
+    for (int i = K - 1; i >= 1; --i) {
+        kn.xp[i] = fminf(kn.xp[i], nextafterf(kn.xp[i + 1], -INFINITY));
+        kn.yp[i] = fminf(kn.yp[i], nextafterf(kn.yp[i + 1], -INFINITY));
+    }
 #pragma unroll
     for (int i = 0; i <= K; ++i) {
         const float t = p[2 * K + i] + kSlopeOffset;
@@ -334,7 +343,8 @@ __host__ __device__ constexpr int head_smem_floats(int L, int K, int ldp) {
 template <int K>
 __global__ void __launch_bounds__(32 * kMaxLayers) head_grad_kernel(
     const float* __restrict__ P, int ldp, int L, const float* __restrict__ y, const float* __restrict__ nhits,
-    const int* __restrict__ has_y, int B, float r0, float r1, float clip, __nv_bfloat16* __restrict__ dp,
+    const int* __restrict__ has_y, int B, float r0, float r1, float clip, float count_w,
+    __nv_bfloat16* __restrict__ dp,
     __nv_bfloat16* __restrict__ dpt, float* __restrict__ gf, float* __restrict__ gbias, double* __restrict__ loss) {
     constexpr int NP = 3 * K + 1, NK = K + 1, KN = 3 * NK + 2 * K + NK;
     extern __shared__ float sm[];
@@ -383,7 +393,7 @@ __global__ void __launch_bounds__(32 * kMaxLayers) head_grad_kernel(
         const float le_raw = p[o_le], n = act ? nhits[b] : 0.0f;
         const float le = clamp_le(le_raw);
         const float lam = expf(le);
-        if (act) l -= n * le - lam - lgammaf(n + 1.0f);
+        if (act) l -= count_w * (n * le - lam - lgammaf(n + 1.0f));
         float a = 0.0f, g_shift = 0.0f, g_scale = 0.0f;
         if (timed) {
             float cur = y[b], ldsum = 0.0f;
@@ -409,7 +419,7 @@ __global__ void __launch_bounds__(32 * kMaxLayers) head_grad_kernel(
         s_s[lane * 4 + 0] = a;
         s_s[lane * 4 + 1] = g_shift;
         s_s[lane * 4 + 2] = g_scale;
-        s_s[lane * 4 + 3] = act && le_raw == le ? (lam - n) * inv_b : 0.0f;
+        s_s[lane * 4 + 3] = act && le_raw == le ? count_w * (lam - n) * inv_b : 0.0f;
         l = warp_sum(l);
         if (lane == 0 && l != 0.0f) atomicAdd(loss, static_cast<double>(l) / B);
     }
@@ -765,6 +775,7 @@ struct ntp_flow {
     float r0 = -20.0f, r1 = 1500.0f;
     float lr = 1e-3f, b1 = 0.9f, b2 = 0.999f, eps = 1e-8f;
     float clip = 1e3f;  // per-sample bound on |dL/dP| times the batch size (0 = none)
+    float count_w = 1.0f;  // weight of the Poisson count term (1 = log_likelihood_with_poisson)
     long long step = 0;
     std::string err;
     Block blk[8];  // W1 b1 W2 b2 W3 b3 W4 b4
@@ -885,7 +896,8 @@ ntp_status launch_head(ntp_flow* f, const float* y, const float* nh, const int* 
                                  static_cast<int>(smem));
         if (e == cudaSuccess) {
             ntp::head_grad_kernel<K><<<(B + 31) / 32, 32 * f->L, smem, f->stream>>>(
-                f->P, f->n_pad, f->L, y, nh, hy, B, f->r0, f->r1, f->clip, f->dp, f->dpt, gf, gbias, f->loss);
+                f->P, f->n_pad, f->L, y, nh, hy, B, f->r0, f->r1, f->clip, f->count_w, f->dp, f->dpt, gf, gbias,
+                f->loss);
             e = cudaGetLastError();
         }
     });
@@ -921,7 +933,7 @@ ntp_status ntp_flow_create(int32_t device, const ntp_flow_config* cfg, ntp_flow*
         (cfg->n_bins != 10 && cfg->n_bins != 12) ||
         cfg->n_layers > ntp::kMaxLayers || !(cfg->t_max > cfg->t_min) || !(cfg->lr > 0.0f) ||
         !(cfg->beta1 >= 0.0f && cfg->beta1 < 1.0f) || !(cfg->beta2 >= 0.0f && cfg->beta2 < 1.0f) ||
-        !(cfg->eps > 0.0f) || !(cfg->grad_clip >= 0.0f))
+        !(cfg->eps > 0.0f) || !(cfg->grad_clip >= 0.0f) || !(cfg->count_weight >= 0.0f))
         return NTP_ERR_INVALID;
     ntp_flow* f = new ntp_flow();
     f->device = device;
@@ -937,6 +949,7 @@ ntp_status ntp_flow_create(int32_t device, const ntp_flow_config* cfg, ntp_flow*
     f->b2 = cfg->beta2;
     f->eps = cfg->eps;
     f->clip = cfg->grad_clip;
+    f->count_w = cfg->count_weight;
     const int dims[4][2] = {{kHid, kIn}, {kHid, kHid}, {kHid, kHid}, {f->n_pad, kHid}};
     size_t off = 0;
     for (int l = 0; l < 4; ++l) {

@@ -52,6 +52,7 @@ class RQNormFlowHParams:
     beta2: float = 0.999
     eps: float = 1e-8
     grad_clip: float = 1e3   # per-sample bound on |dL/draw outputs| x batch size; 0 = none
+    count_weight: float = 1.0  # weight of the Poisson count term (1 = log_likelihood_with_poisson)
     seed: int = 31338
 
 
@@ -73,7 +74,8 @@ class RQNormFlow:
         cfg = _abi.NtpFlowConfig(batch_capacity=cap, n_layers=int(hp.n_layers), n_bins=int(hp.K),
                                  t_min=float(hp.range_min), t_max=float(hp.range_max), lr=float(hp.lr),
                                  beta1=float(hp.beta1), beta2=float(hp.beta2), eps=float(hp.eps),
-                                 grad_clip=float(hp.grad_clip), seed=int(hp.seed) & (2 ** 64 - 1))
+                                 grad_clip=float(hp.grad_clip), count_weight=float(hp.count_weight),
+                                 seed=int(hp.seed) & (2 ** 64 - 1))
         h = C.c_void_p()
         st = self.lib.ntp_flow_create(int(device), C.byref(cfg), C.byref(h))
         if st != 0:

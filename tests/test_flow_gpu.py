@@ -101,6 +101,25 @@ def test_head_gradient_clip():
     assert np.all(cos > 1 - 1e-5)
 
 
+def test_degenerate_knots_stay_finite():
+    """Raw widths that put all the range in the first bin leave the other
+    bins at the minimum width; their FP32 running sum passes the pinned last
+    knot unless the knots are kept strictly increasing."""
+    L, K, r0, r1 = 5, 12, -20.0, 1500.0
+    NP = 3 * K + 1
+    B = 256
+    raw = np.zeros((B, L * NP + 3), np.float32)
+    for li in range(L):
+        raw[:, li * NP] = 60.0             # bin 0 takes the whole width ...
+        raw[:, li * NP + K] = 60.0         # ... and the whole height
+        raw[:, li * NP + 2 * K:(li + 1) * NP] = -12.0   # slopes near the minimum
+    raw[:, L * NP] = 1400.0
+    tres = np.linspace(1495.0, 1500.5, B).astype(np.float32)
+    with make(L, K, r0, r1) as fl:
+        loss, grad = fl.head(raw, tres, np.ones(B, np.float32), np.ones(B, np.int32))
+    assert np.isfinite(loss) and np.all(np.isfinite(grad))
+
+
 @pytest.mark.parametrize("L,K,r0,r1", CASES)
 def test_conditioner_forward(L, K, r0, r1):
     rng = np.random.default_rng(3)
@@ -251,7 +270,7 @@ def test_invalid_arguments():
     lib = _abi.load_library()
     import ctypes as C
     bad = _abi.NtpFlowConfig(batch_capacity=1024, n_layers=1, n_bins=11, t_min=-20, t_max=100, lr=1e-3, beta1=0.9,
-                             beta2=0.999, eps=1e-8, grad_clip=0.0, seed=0)
+                             beta2=0.999, eps=1e-8, grad_clip=0.0, count_weight=1.0, seed=0)
     h = C.c_void_p()
     assert lib.ntp_flow_create(0, C.byref(bad), C.byref(h)) == _abi.NTP_ERR_INVALID
     assert not h.value
