@@ -215,7 +215,7 @@ def flow_bench(train_steps: int = 300, n_tuples: int = 100_000_000) -> dict:
     out["table"] = {"simulations": 8192, "orientations": 16, "rows": len(tab), "photons": tab.n_photons,
                     "seconds": dt, "rows_per_s": len(tab) / dt, "photons_per_s": tab.n_photons / dt}
     bs = 8192
-    fl = RQNormFlow(RQNormFlowHParams(batch_size=bs))
+    fl = RQNormFlow(RQNormFlowHParams(batch_size=bs), batch_capacity=131072)
     fl.init_from_table(tab)
     perm = torch.randperm(len(tab), device="cuda")
     cond, tres = tab.cond[perm].contiguous(), tab.tres[perm].contiguous()
@@ -244,34 +244,45 @@ def flow_bench(train_steps: int = 300, n_tuples: int = 100_000_000) -> dict:
                        "roofline": {"bound": "tensor", "achieved": ach, "peak": peak[0], "unit": "TFLOP/s",
                                     "frac": ach / peak[0], "peak_source": peak[1],
                                     "flops_per_step": step_flops}}
-    # inference: 1e8 tuples over 128000 conditions
+    # inference: 1e8 (condition, time) log-pdf tuples over 128000 conditions:
+    # (a) as a 781-point time grid per condition (the reference's per-module
+    # evaluation), (b) as arbitrary (condition index, time) pairs
     n_cond = 8000 * 16
+    n_t = n_tuples // n_cond
     g = torch.Generator(device="cuda").manual_seed(5)
     c = (torch.rand((n_cond, 5), device="cuda", generator=g) * 2 - 1).contiguous()
+    times = torch.linspace(-20.0, 280.0, n_t, device="cuda")
+    fl.logpdf_grid(c[:128], times)
+    torch.cuda.synchronize()
+    reps = 3
+    t0 = time.perf_counter()
+    for _ in range(reps):
+        lpg = fl.logpdf_grid(c, times)
+    torch.cuda.synchronize()
+    dt_g = (time.perf_counter() - t0) / reps
     idx = torch.randint(0, n_cond, (n_tuples,), device="cuda", dtype=torch.int32, generator=g)
     idx, _ = torch.sort(idx)
     tt = (torch.rand(n_tuples, device="cuda", generator=g) * 300.0 - 20.0).contiguous()
     fl.logpdf(c, idx[:1000], tt[:1000])
     torch.cuda.synchronize()
-    reps = 3
     t0 = time.perf_counter()
     for _ in range(reps):
         lp = fl.logpdf(c, idx, tt)
     torch.cuda.synchronize()
     dt = (time.perf_counter() - t0) / reps
-    bytes_per = 4 + 4 + 4
-    out["inference"] = {"tuples": n_tuples, "conditions": n_cond, "seconds": dt, "tuples_per_s": n_tuples / dt,
-                        "finite": bool(torch.isfinite(lp).all().item()),
-                        "hbm_gbs": n_tuples * bytes_per / dt / 1e9,
-                        "note": "time includes the conditioner pass over the 128000 conditions"}
-    hc, hi, ht = c.cpu().numpy(), idx.cpu().numpy(), tt.cpu().numpy()
+    out["inference"] = {"tuples": n_cond * n_t, "conditions": n_cond, "times_per_condition": n_t,
+                        "grid_seconds": dt_g, "tuples_per_s": n_cond * n_t / dt_g,
+                        "finite": bool(torch.isfinite(lpg).all().item() and torch.isfinite(lp).all().item()),
+                        "pairs": {"tuples": n_tuples, "seconds": dt, "tuples_per_s": n_tuples / dt},
+                        "note": "times include the conditioner pass over the 128000 conditions"}
+    hc, ht = c.cpu().numpy(), times.cpu().numpy()
     t0 = time.perf_counter()
-    fl.logpdf(hc, hi, ht)
+    fl.logpdf_grid(hc, ht)
     dt = time.perf_counter() - t0
-    out["inference"]["e2e"] = {"tuples_per_s": n_tuples / dt, "seconds": dt,
-                               "h2d_bytes": int(hc.nbytes + hi.nbytes + ht.nbytes), "d2h_bytes": 4 * n_tuples}
+    out["inference"]["e2e"] = {"tuples_per_s": n_cond * n_t / dt, "seconds": dt,
+                               "h2d_bytes": int(hc.nbytes + ht.nbytes), "d2h_bytes": 4 * n_cond * n_t}
     fl.close()
-    del tab, cond, tres, nh, has, c, idx, tt, lp
+    del tab, cond, tres, nh, has, c, idx, tt, lp, lpg
     torch.cuda.empty_cache()
     return out
 
@@ -334,6 +345,29 @@ def hybrid_bench(n_events: int = 10_000, batch: int = 256, train_steps: int = 12
                         "hits": n_hits, "latency_p50_ms": float(np.percentile(lat, 50) * 1e3),
                         "latency_p99_ms": float(np.percentile(lat, 99) * 1e3),
                         "note": "all events queued at t = 0 and served in batches; latency = completion time"}
+    # real time: Poisson arrivals at 1000 events/s, each batch the events arrived so far
+    rng = np.random.default_rng(9)
+    n_rt = min(n_events, 4000)
+    arr = np.cumsum(rng.exponential(1e-3, n_rt))
+    res_rt = sim.serve([(float(arr[i]), *events[i]) for i in range(n_rt)], max_batch=64)
+    lat_rt = np.array([r[2] for r in res_rt])
+    out["realtime"] = {"arrival_rate_hz": 1000.0, "events": n_rt,
+                       "events_per_s": n_rt / (float(arr[-1]) + lat_rt[-1]),
+                       "latency_p50_ms": float(np.percentile(lat_rt, 50) * 1e3),
+                       "latency_p99_ms": float(np.percentile(lat_rt, 99) * 1e3)}
+    # the KS check of the hybrid mode: every 50th flow event also through MC,
+    # plain MC from the first check above 0.02 on
+    chk = HybridSimulator(setup, fl, seed=workloads.SEED_BASE + 6, ks_check_every=50, ks_threshold=0.02)
+    chk_events = [e for e in events if e[2] <= 4.0][:200]
+    t1 = time.perf_counter()
+    res_chk = []
+    for s0 in range(0, len(chk_events), 25):
+        res_chk += chk.simulate(chk_events[s0:s0 + 25])
+    out["ks_check"] = {"threshold": 0.02, "every": 50, "events": len(chk_events),
+                       "checks": [{"event": int(a), "ks": float(b)} for a, b in chk.checks],
+                       "fell_back_to_mc": chk.fallback,
+                       "events_mc": int(sum(r.method == "mc" for r in res_chk)),
+                       "seconds": time.perf_counter() - t1}
     # one batch alone: the latency of an event served on arrival with a batch of its own
     torch.cuda.synchronize()
     t1 = time.perf_counter()

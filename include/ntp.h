@@ -453,6 +453,14 @@ ntp_status ntp_flow_head(ntp_flow* flow, const float* params, const float* tres,
 ntp_status ntp_flow_evaluate(ntp_flow* flow, const float* cond, int32_t n_cond, const int32_t* cond_index,
                              const float* times, uint64_t n_tuples, float* logpdf, float* log_expec,
                              int32_t on_device);
+/* The model call on a time grid shared by the conditions, as the reference
+   evaluates a module's density (`model(repeat(times), repeat(input))` on a
+   111-point grid, extended_cascade_model.jl:416-437 and the scripts):
+   logpdf[c * n_times + j] = log p(times[j] | cond[c]); log_expec as in
+   ntp_flow_evaluate (may be NULL).  Host, or device buffers with on_device. */
+ntp_status ntp_flow_evaluate_grid(ntp_flow* flow, const float* cond, int32_t n_cond, const float* times,
+                                  int32_t n_times, float* logpdf, float* log_expec, int32_t on_device);
+
 /* Sampling from the surrogate (the hits a PMT sees, as the MC would give
    them after resample_simulation): per condition c a count N_c ~
    Poisson(exp(log expectation)), then N_c times drawn from the flow (a

@@ -281,6 +281,41 @@ __device__ __forceinline__ void inv_spline(const float* xp, const float* yp, con
     }
 }
 
+// The same inverse for inference: hardware reciprocal / logarithm
+// (__fdividef, __logf, relative error ~1e-6) and the three logarithms of the
+// log-determinant folded into one, log(den^2 / (s^2 q)).
+__device__ __forceinline__ void inv_bin_fast(float y, float x0, float w, float y0, float h, float d0, float d1,
+                                             float& x, float& logdet) {
+    const float s = __fdividef(h, w);
+    const float ww = fminf(fmaxf(__fdividef(y - y0, h), 0.0f), 1.0f);
+    const float st = d1 + d0 - 2.0f * s;
+    const float c = -s * ww, b = d0 - st * ww, a = s - b;
+    const float disc = b * b - 4.0f * a * c;
+    const float sq = disc > 0.0f ? sqrtf(disc) : 0.0f;
+    float z = b >= 0.0f ? __fdividef(2.0f * c, -b - sq) : __fdividef(-b + sq, 2.0f * a);
+    z = fminf(fmaxf(z, 0.0f), 1.0f);
+    x = w * z + x0;
+    const float z1mz = z - z * z, omz = 1.0f - z;
+    const float den = s + st * z1mz;
+    const float q = d1 * z * z + 2.0f * s * z1mz + d0 * omz * omz;
+    logdet = __logf(__fdividef(den * den, s * s * q));
+}
+
+template <int K>
+__device__ __forceinline__ void inv_spline_fast(const float* xp, const float* yp, const float* d, float y, float& x,
+                                                float& logdet) {
+    if (y <= yp[0]) {
+        x = __fdividef(y - yp[0], d[0]) + xp[0];
+        logdet = -__logf(d[0]);
+    } else if (y >= yp[K]) {
+        x = __fdividef(y - yp[K], d[K]) + xp[K];
+        logdet = -__logf(d[K]);
+    } else {
+        const int k = find_bin<K>(yp, y);
+        inv_bin_fast(y, xp[k], xp[k + 1] - xp[k], yp[k], yp[k + 1] - yp[k], d[k], d[k + 1], x, logdet);
+    }
+}
+
 // FP32 range guards of the head (the reference computes in Float64): the log
 // expectation is used within [-30, 30] (expected counts 1e-13 to 1e13) and
 // the raw scale within [-20, 20] (scale >= 2e-7 ns); outside, the value is
@@ -647,13 +682,42 @@ __global__ void logpdf_kernel(const float* __restrict__ knots, int L, int n_cond
         for (int li = L - 1; li >= 0; --li) {
             const float* xp = o + li * (3 * (K + 1));
             float x, ld;
-            inv_spline<K>(xp, xp + K + 1, xp + 2 * (K + 1), cur, x, ld);
+            inv_spline_fast<K>(xp, xp + K + 1, xp + 2 * (K + 1), cur, x, ld);
             cur = x;
             ldsum += ld;
         }
         const float scale = o[L * (3 * (K + 1)) + 1];
-        const float u = (cur - o[L * (3 * (K + 1))]) / scale;
-        out[i] = -logf(scale) - 0.5f * (kLog2Pi + u * u) + ldsum;
+        const float u = (cur - o[L * (3 * (K + 1))]) * __fdividef(1.0f, scale);
+        out[i] = -__logf(scale) - 0.5f * (kLog2Pi + u * u) + ldsum;
+    }
+}
+
+// log p(t_j | condition c) on a time grid shared by all conditions: out[c *
+// n_times + j].  One block per condition (grid-stride), its knot row staged in
+// shared memory; the threads sweep the grid.
+template <int K>
+__global__ void logpdf_grid_kernel(const float* __restrict__ knots, int L, int n_cond,
+                                   const float* __restrict__ times, int n_times, float* __restrict__ out) {
+    extern __shared__ float s_row[];
+    const int row = knot_row(L, K);
+    for (int c = blockIdx.x; c < n_cond; c += gridDim.x) {
+        __syncthreads();
+        for (int i = threadIdx.x; i < row; i += blockDim.x) s_row[i] = knots[static_cast<size_t>(c) * row + i];
+        __syncthreads();
+        const float shift = s_row[L * 3 * (K + 1)], scale = s_row[L * 3 * (K + 1) + 1];
+        const float inv_scale = __fdividef(1.0f, scale), log_scale = __logf(scale);
+        for (int j = threadIdx.x; j < n_times; j += blockDim.x) {
+            float cur = __ldg(times + j), ldsum = 0.0f;
+            for (int li = L - 1; li >= 0; --li) {
+                const float* xp = s_row + li * 3 * (K + 1);
+                float x, ld;
+                inv_spline_fast<K>(xp, xp + K + 1, xp + 2 * (K + 1), cur, x, ld);
+                cur = x;
+                ldsum += ld;
+            }
+            const float u = (cur - shift) * inv_scale;
+            out[static_cast<size_t>(c) * n_times + j] = -log_scale - 0.5f * (kLog2Pi + u * u) + ldsum;
+        }
     }
 }
 
@@ -1351,6 +1415,43 @@ ntp_status ntp_flow_sample(ntp_flow* f, const float* cond, int32_t n_cond, const
     };
     const ntp_status s2 = run();
     cudaFree(scratch);
+    return s2;
+}
+
+
+ntp_status ntp_flow_evaluate_grid(ntp_flow* f, const float* cond, int32_t n_cond, const float* times, int32_t n_times,
+                                  float* logpdf, float* log_expec, int32_t on_device) {
+    if (!f || !cond || n_cond <= 0 || n_times <= 0 || !times || !logpdf) return NTP_ERR_INVALID;
+    F_OK(ntp_flow_evaluate(f, cond, n_cond, nullptr, nullptr, 0, nullptr, log_expec, on_device));
+    cudaStream_t st = f->stream;
+    const size_t n_out = static_cast<size_t>(n_cond) * n_times;
+    const float* d_t = times;
+    float* d_out = logpdf;
+    void* stage = nullptr;
+    if (!on_device) {
+        F_CUDA(f, cudaMalloc(&stage, sizeof(float) * (n_times + n_out)));
+        d_t = static_cast<float*>(stage);
+        d_out = static_cast<float*>(stage) + n_times;
+    }
+    auto run = [&]() -> ntp_status {
+        if (!on_device)
+            F_CUDA(f, cudaMemcpyAsync(const_cast<float*>(d_t), times, sizeof(float) * n_times, cudaMemcpyHostToDevice,
+                                      st));
+        const int row = ntp::knot_row(f->L, f->K);
+        const int grid = std::min(n_cond, 152 * 16);
+        cudaError_t e = cudaSuccess;
+        with_bins(f->K, [&](auto kc) {
+            ntp::logpdf_grid_kernel<decltype(kc)::value>
+                <<<grid, 256, sizeof(float) * row, st>>>(f->knots, f->L, n_cond, d_t, n_times, d_out);
+            e = cudaGetLastError();
+        });
+        if (e != cudaSuccess) return ferr(f, e, "ntp_flow_evaluate_grid");
+        if (!on_device) F_CUDA(f, cudaMemcpyAsync(logpdf, d_out, sizeof(float) * n_out, cudaMemcpyDeviceToHost, st));
+        F_CUDA(f, cudaStreamSynchronize(st));
+        return NTP_OK;
+    };
+    const ntp_status s2 = run();
+    if (stage) cudaFree(stage);
     return s2;
 }
 

@@ -283,6 +283,27 @@ class RQNormFlow:
                                                    le.ctypes.data if le is not None else None, 0))
         return (out, le) if log_expec else out
 
+    def logpdf_grid(self, cond, times, *, log_expec: bool = False):
+        """log p(times[j] | cond[c]) as an [n_cond x n_times] array (the
+        reference's per-module evaluation on a time grid)."""
+        dev = _is_device(cond)
+        n_cond, n_t = int(cond.shape[0]), int(times.shape[0])
+        if dev:
+            import torch
+            out = torch.empty((n_cond, n_t), dtype=torch.float32, device=cond.device)
+            le = torch.empty(n_cond, dtype=torch.float32, device=cond.device) if log_expec else None
+            self._check(self.lib.ntp_flow_evaluate_grid(self._h, cond.data_ptr(), n_cond, times.data_ptr(), n_t,
+                                                        out.data_ptr(), le.data_ptr() if le is not None else None,
+                                                        1))
+        else:
+            cond, times = _f32(cond), _f32(times)
+            out = np.empty((n_cond, n_t), np.float32)
+            le = np.empty(n_cond, np.float32) if log_expec else None
+            self._check(self.lib.ntp_flow_evaluate_grid(self._h, cond.ctypes.data, n_cond, times.ctypes.data, n_t,
+                                                        out.ctypes.data, le.ctypes.data if le is not None else None,
+                                                        0))
+        return (out, le) if log_expec else out
+
     MAX_SAMPLE_CONDITIONS = 1 << 20
 
     def sample_hits(self, cond, keys, seed: int = 0, capacity: int | None = None):

@@ -43,12 +43,22 @@ class HybridSimulator:
     """Flow surrogate with an MC fallback on the detector of ``setup``."""
 
     def __init__(self, setup: PhotonPropSetup, flow: RQNormFlow, *, d_range=(1.0, 200.0),
-                 log10_energy_range=(2.0, 6.0), seed: int = 0):
+                 log10_energy_range=(2.0, 6.0), seed: int = 0, ks_check_every: int = 0,
+                 ks_threshold: float = 0.02):
+        """ks_check_every > 0: every that many flow-served events one is also
+        simulated with plain MC and the two hit-time samples compared (KS,
+        pooled over the event); a KS above ks_threshold hands every later
+        event to plain MC."""
         self.setup = setup
         self.flow = flow
         self.d_range = (float(d_range[0]), float(d_range[1]))
         self.e_range = log10_energy_range
         self.seed = int(seed)
+        self.ks_check_every = int(ks_check_every)
+        self.ks_threshold = float(ks_threshold)
+        self.fallback = False
+        self.checks: list[tuple[int, float]] = []
+        self._served = 0
         self.lib, self.ctx = setup.context()
         self.n800 = float(np.float32(np.asarray(setup.medium.refractive_index(np.array([800.0])))[0]))
 
@@ -92,8 +102,8 @@ class HybridSimulator:
         le = np.array([float(e[2]) for e in events])
         cond, key, tgeo, tgt, pmt, first, close = self.conditions(srcs, le, ids)
         out: list[EventHits | None] = [None] * len(events)
-        in_domain = (close == 0) & (le >= self.e_range[0]) & (le <= self.e_range[1])
-        if cond.shape[0]:
+        in_domain = (close == 0) & (le >= self.e_range[0]) & (le <= self.e_range[1]) & (not self.fallback)
+        if cond.shape[0] and in_domain.any():
             cnt, hc, ht = self.flow.sample_hits(cond, key, seed=self.seed)
             hc64 = hc.long()
             times = ht + tgeo[hc64]
@@ -111,6 +121,39 @@ class HybridSimulator:
         for i in range(len(events)):
             if out[i] is None:
                 out[i] = self.mc_event(ids[i], srcs[i])
+            elif self.ks_check_every > 0:
+                self._served += 1
+                if self._served % self.ks_check_every == 0:
+                    mc = self.mc_event(ids[i], srcs[i])
+                    ks = ks_statistic(mc.time, out[i].time.cpu().numpy())
+                    self.checks.append((ids[i], ks))
+                    if not (ks <= self.ks_threshold):
+                        self.fallback = True
+        return out
+
+    def serve(self, arrivals, *, max_batch: int = 64) -> list[tuple[int, str, float]]:
+        """Real-time replay: events (arrival time in s, event_id, source,
+        log10 E) are served in arrival order, each batch holding the events
+        arrived so far (at most max_batch); returns (event_id, method,
+        latency in s) per event."""
+        import time as _t
+
+        import torch
+        t0 = _t.perf_counter()
+        i, out = 0, []
+        while i < len(arrivals):
+            now = _t.perf_counter() - t0
+            if arrivals[i][0] > now:
+                _t.sleep(min(arrivals[i][0] - now, 1e-3))
+                continue
+            j = i
+            while j < len(arrivals) and j - i < max_batch and arrivals[j][0] <= now:
+                j += 1
+            res = self.simulate([(a[1], a[2], a[3]) for a in arrivals[i:j]])
+            torch.cuda.synchronize()
+            done = _t.perf_counter() - t0
+            out.extend((r.event_id, r.method, done - a[0]) for r, a in zip(res, arrivals[i:j]))
+            i = j
         return out
 
     def mc_event(self, event_id: int, source) -> EventHits:

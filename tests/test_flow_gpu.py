@@ -214,6 +214,22 @@ def test_evaluate_matches_oracle_on_the_same_parameters(L, K, r0, r1):
     assert ll == pytest.approx(want, rel=1e-4)
 
 
+def test_grid_evaluation_equals_tuples():
+    L, K, r0, r1 = 5, 12, -20.0, 1500.0
+    rng = np.random.default_rng(70)
+    with make(L, K, r0, r1, seed=6) as fl:
+        cond = rng.uniform(-1, 1, (37, 5)).astype(np.float32)
+        times = np.concatenate([rng.uniform(-60, 1700, 200), [-20.0, 1500.0]]).astype(np.float32)
+        g, le = fl.logpdf_grid(cond, times, log_expec=True)
+        idx = np.repeat(np.arange(37, dtype=np.int32), times.size)
+        t = np.tile(times, 37)
+        lp, le2 = fl.logpdf(cond, idx, t, log_expec=True)
+        gd = fl.logpdf_grid(torch.as_tensor(cond, device="cuda"), torch.as_tensor(times, device="cuda")).cpu().numpy()
+    np.testing.assert_allclose(g.ravel(), lp, rtol=2e-6, atol=2e-6)
+    np.testing.assert_array_equal(le, le2)
+    np.testing.assert_array_equal(gd, g)
+
+
 def test_density_integrates_to_one_on_device():
     # a size-independent property at a full-size evaluation (16.8 M tuples)
     L, K, r0, r1 = 5, 12, -20.0, 1500.0
