@@ -42,6 +42,13 @@ METRIC = "photons/s"
 # a module radius, which is rare enough not to count).
 OPS_BASE = 70 + 50 + 5
 OPS_PER_GEOMETRY_TEST = 12
+# Algorithmic lane-operations of one extended-cascade photon's start (once per
+# photon): two Philox4x32-10 blocks (initial uniforms, track smearing) and one
+# per gamma attempt (~1 on average), 140 + 70; wavelength and medium-table
+# lookup 15; the gamma variate (Box-Muller, Marsaglia-Tsang test) 20; the
+# Cherenkov cone 10; the track smearing (log, power, sine, cosine) 15; two
+# rotations 40; the position and time along the shower axis 10.
+OPS_PHOTON_INIT = 140 + 70 + 15 + 20 + 10 + 15 + 40 + 10
 
 
 def algo_ops_per_step(n_strings: int) -> int:
@@ -357,13 +364,13 @@ def hybrid_bench(n_events: int = 10_000, batch: int = 256, train_steps: int = 12
                        "latency_p99_ms": float(np.percentile(lat_rt, 99) * 1e3)}
     # the KS check of the hybrid mode: every 50th flow event also through MC,
     # plain MC from the first check above 0.02 on
-    chk = HybridSimulator(setup, fl, seed=workloads.SEED_BASE + 6, ks_check_every=50, ks_threshold=0.02)
-    chk_events = [e for e in events if e[2] <= 4.0][:200]
+    chk = HybridSimulator(setup, fl, seed=workloads.SEED_BASE + 6, ks_check_every=25, ks_threshold=0.02)
+    chk_events = [e for e in events if e[2] <= 4.0][:100]
     t1 = time.perf_counter()
     res_chk = []
     for s0 in range(0, len(chk_events), 25):
         res_chk += chk.simulate(chk_events[s0:s0 + 25])
-    out["ks_check"] = {"threshold": 0.02, "every": 50, "events": len(chk_events),
+    out["ks_check"] = {"threshold": 0.02, "every": 25, "events": len(chk_events),
                        "checks": [{"event": int(a), "ks": float(b)} for a, b in chk.checks],
                        "fell_back_to_mc": chk.fallback,
                        "events_mc": int(sum(r.method == "mc" for r in res_chk)),
@@ -581,13 +588,14 @@ def main():
     # roofline of the propagation kernel: algorithmic lane-ops / kernel time
     n_strings = len({(float(t.position[0]), float(t.position[1])) for t in setup.targets})
     ops_step = algo_ops_per_step(n_strings)
-    achieved = sum(steps_taken) * ops_step / (sum(ms) / 1e3) / 1e9
+    achieved = (sum(steps_taken) * ops_step + photons * args.steps * OPS_PHOTON_INIT) / (sum(ms) / 1e3) / 1e9
     sm_mhz = clocks.get("sm_mhz") or 2070.0
     peak = 152 * 4 * 32 * sm_mhz * 1e6 / 1e9  # lane-instructions issued per second at the sampled clock
     roofline = {"bound": "issue", "achieved": achieved, "peak": peak, "unit": "Gop/s",
                 "frac": achieved / peak,
                 "peak_source": f"nominal issue rate 152 SM x 4 schedulers x 32 lanes at the sampled {sm_mhz:.0f} MHz",
-                "ops_per_photon_step": ops_step, "photon_steps_per_step": int(statistics.mean(steps_taken)),
+                "ops_per_photon_step": ops_step, "ops_per_photon_init": OPS_PHOTON_INIT,
+                "photon_steps_per_step": int(statistics.mean(steps_taken)),
                 "traffic": None}
 
     # e2e through the public call with host buffers

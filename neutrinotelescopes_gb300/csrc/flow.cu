@@ -31,6 +31,7 @@
 
 #include <algorithm>
 #include <cmath>
+#include <cstdlib>
 #include <cstring>
 #include <limits>
 #include <random>
@@ -607,11 +608,17 @@ struct ParamBlocks {
 };
 
 // Adam (Flux's: bias-corrected moments) over the whole flat FP32 vector in
-// one launch; refreshes the BF16 weight copies and their transposes.
+// one launch; refreshes the BF16 weight copies and their transposes.  The
+// step size and the step count are read from device memory, so a captured
+// training step replays with the current values.
 __global__ void adam_kernel(float* __restrict__ w, float* __restrict__ m, float* __restrict__ v,
-                            const float* __restrict__ g, const ParamBlocks pb, float lr, float b1, float b2,
-                            float eps, float c1, float c2, const int* __restrict__ skip) {
+                            const float* __restrict__ g, const ParamBlocks pb, const float* __restrict__ lr_dev,
+                            float b1, float b2, float eps, const int* __restrict__ step_dev,
+                            const int* __restrict__ skip) {
     if (*skip) return;  // a non-finite gradient: the step is skipped
+    const float t = static_cast<float>(*step_dev + 1);
+    const float c1 = 1.0f - powf(b1, t), c2 = 1.0f - powf(b2, t);
+    const float lr = *lr_dev;
     const long long total = pb.off[pb.n];
     for (long long i = blockIdx.x * static_cast<long long>(blockDim.x) + threadIdx.x; i < total;
          i += static_cast<long long>(gridDim.x) * blockDim.x) {
@@ -631,6 +638,11 @@ __global__ void adam_kernel(float* __restrict__ w, float* __restrict__ m, float*
             pb.wt[k][(j % pb.cols[k]) * pb.rows[k] + j / pb.cols[k]] = h;
         }
     }
+}
+
+// Counts the step Adam took (after adam_kernel, in stream order).
+__global__ void step_count_kernel(int* __restrict__ step_dev, const int* __restrict__ skip) {
+    if (!*skip) ++*step_dev;
 }
 
 __global__ void to_bf16_kernel(const float* __restrict__ w, int n, int cols, int rows,
@@ -856,6 +868,12 @@ struct ntp_flow {
     int* gemm_err = nullptr;
     int* skip = nullptr;     // set when a step's gradient is not finite
     long long skipped = 0;   // steps skipped for that reason
+    int* step_dev = nullptr;  // Adam's step count on the device
+    float* lr_dev = nullptr;  // Adam's step size on the device
+    // the training step captured as a CUDA graph (per batch size and update flag)
+    bool use_graph = true;
+    cudaGraphExec_t gexec = nullptr;
+    int g_B = 0, g_update = -1;
     // inference
     float* knots = nullptr;
     size_t knots_cap = 0;
@@ -956,8 +974,11 @@ ntp_status launch_head(ntp_flow* f, const float* y, const float* nh, const int* 
     cudaError_t e = cudaSuccess;
     with_bins(f->K, [&](auto kc) {
         constexpr int K = decltype(kc)::value;
-        e = cudaFuncSetAttribute(ntp::head_grad_kernel<K>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                 static_cast<int>(smem));
+        cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+        e = cudaStreamIsCapturing(f->stream, &cs);
+        if (e == cudaSuccess && cs == cudaStreamCaptureStatusNone)  // set before a capture by prepare_kernels
+            e = cudaFuncSetAttribute(ntp::head_grad_kernel<K>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                     static_cast<int>(smem));
         if (e == cudaSuccess) {
             ntp::head_grad_kernel<K><<<(B + 31) / 32, 32 * f->L, smem, f->stream>>>(
                 f->P, f->n_pad, f->L, y, nh, hy, B, f->r0, f->r1, f->clip, f->count_w, f->dp, f->dpt, gf, gbias,
@@ -971,7 +992,7 @@ ntp_status launch_head(ntp_flow* f, const float* y, const float* nh, const int* 
 
 void free_all(ntp_flow* f) {
     void* ps[] = {f->theta, f->m, f->v, f->grad, f->x, f->xt, f->dp, f->dpt, f->P, f->cond, f->y, f->nh, f->hy,
-                  f->loss, f->gemm_err, f->skip, f->knots};
+                  f->loss, f->gemm_err, f->skip, f->step_dev, f->lr_dev, f->knots};
     for (void* p : ps)
         if (p) cudaFree(p);
     for (int l = 0; l < 4; ++l) {
@@ -984,6 +1005,84 @@ void free_all(ntp_flow* f) {
         if (f->dz[l]) cudaFree(f->dz[l]);
         if (f->dzt[l]) cudaFree(f->dzt[l]);
     }
+}
+
+// Every device operation of one training step on the staged batch (f->cond,
+// f->y, f->nh, f->hy): no host synchronisation, so it can be captured.
+ntp_status record_step(ntp_flow* f, int B, bool update) {
+    cudaStream_t st = f->stream;
+    F_CUDA(f, cudaMemsetAsync(f->gemm_err, 0, sizeof(int), st));
+    F_OK(pack(f, f->cond, B, B, 1));
+    F_OK(forward(f, B, true));
+    F_CUDA(f, cudaMemsetAsync(f->loss, 0, sizeof(double), st));
+    F_CUDA(f, cudaMemsetAsync(f->grad, 0, sizeof(float) * f->n_params, st));
+    float* g = f->grad;
+    auto gw = [&](int l) { return g + f->blk[2 * l].off; };
+    auto gb = [&](int l) { return g + f->blk[2 * l + 1].off; };
+    F_OK(launch_head(f, f->y, f->nh, f->hy, B, nullptr, gb(3)));
+    // output layer: dW4 = dP^T H3
+    ntp::GemmEpilogue ew{};
+    ew.out_kind = 2;
+    ew.ldc = kHid;
+    ew.c = gw(3);
+    F_OK(gemm(f, f->dpt, B, f->ht[2], B, f->n_pad, kHid, B, ew, 0));
+    const bf16* dnext = f->dp;
+    int k_next = f->n_pad;
+    for (int l = 2; l >= 0; --l) {
+        // dZ_l = (dZ_{l+1} W_{l+1}) masked by H_l > 0, its transpose, and its
+        // column sums (the bias gradient of layer l)
+        ntp::GemmEpilogue ed{};
+        ed.c = f->dz[l];
+        ed.ldc = kHid;
+        ed.out_kind = 1;
+        ed.ct = f->dzt[l];
+        ed.ldct = B;
+        ed.mask = f->h[l];
+        ed.ldm = kHid;
+        ed.colsum = gb(l);
+        F_OK(gemm(f, dnext, k_next, f->wt[l + 1], k_next, B, kHid, k_next, ed));
+        // dW_l = dZ_l^T X_l with X_l = H_{l-1} or the packed input
+        ntp::GemmEpilogue eg{};
+        eg.out_kind = 2;
+        eg.c = gw(l);
+        eg.ldc = l == 0 ? kIn : kHid;
+        const bf16* xt = l == 0 ? f->xt : f->ht[l - 1];
+        F_OK(gemm(f, f->dzt[l], B, xt, B, kHid, l == 0 ? kIn : kHid, B, eg, 0));
+        dnext = f->dz[l];
+        k_next = kHid;
+    }
+    if (update) {
+        ntp::ParamBlocks pb{};
+        pb.n = 8;
+        for (int i = 0; i < 8; ++i) {
+            pb.off[i] = static_cast<long long>(f->blk[i].off);
+            pb.rows[i] = f->blk[i].rows;
+            pb.cols[i] = f->blk[i].cols;
+            pb.wb[i] = (i % 2) == 0 ? f->wb[i / 2] : nullptr;
+            pb.wt[i] = (i % 2) == 0 ? f->wt[i / 2] : nullptr;
+        }
+        pb.off[8] = static_cast<long long>(f->n_params);
+        const int grid = static_cast<int>(std::min<size_t>((f->n_params + 255) / 256, 152 * 8));
+        F_CUDA(f, cudaMemsetAsync(f->skip, 0, sizeof(int), st));
+        ntp::nonfinite_kernel<<<grid, 256, 0, st>>>(g, static_cast<long long>(f->n_params), f->skip);
+        ntp::adam_kernel<<<grid, 256, 0, st>>>(f->theta, f->m, f->v, g, pb, f->lr_dev, f->b1, f->b2, f->eps,
+                                               f->step_dev, f->skip);
+        ntp::step_count_kernel<<<1, 1, 0, st>>>(f->step_dev, f->skip);
+        F_CUDA(f, cudaGetLastError());
+    }
+    return NTP_OK;
+}
+
+// Function attributes the step's kernels need, set before a capture.
+cudaError_t prepare_kernels(ntp_flow* f) {
+    cudaError_t e = ntp::gemm_prepare();
+    if (e != cudaSuccess) return e;
+    const size_t smem = sizeof(float) * ntp::head_smem_floats(f->L, f->K, f->n_pad);
+    with_bins(f->K, [&](auto kc) {
+        e = cudaFuncSetAttribute(ntp::head_grad_kernel<decltype(kc)::value>,
+                                 cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem));
+    });
+    return e;
 }
 
 }  // namespace
@@ -1013,6 +1112,10 @@ ntp_status ntp_flow_create(int32_t device, const ntp_flow_config* cfg, ntp_flow*
     f->b2 = cfg->beta2;
     f->eps = cfg->eps;
     f->clip = cfg->grad_clip;
+    {
+        const char* eg = std::getenv("NTP_FLOW_GRAPH");
+        f->use_graph = !(eg && eg[0] == '0');
+    }
     f->count_w = cfg->count_weight;
     const int dims[4][2] = {{kHid, kIn}, {kHid, kHid}, {kHid, kHid}, {f->n_pad, kHid}};
     size_t off = 0;
@@ -1049,7 +1152,7 @@ ntp_status ntp_flow_create(int32_t device, const ntp_flow_config* cfg, ntp_flow*
     if ((e = dalloc(&f->dp, B * np)) || (e = dalloc(&f->dpt, B * np)) || (e = dalloc(&f->P, B * np)) ||
         (e = dalloc(&f->cond, B * kCond)) || (e = dalloc(&f->y, B)) || (e = dalloc(&f->nh, B)) ||
         (e = dalloc(&f->hy, B)) || (e = dalloc(&f->loss, 1)) || (e = dalloc(&f->gemm_err, 1)) ||
-        (e = dalloc(&f->skip, 1)))
+        (e = dalloc(&f->skip, 1)) || (e = dalloc(&f->step_dev, 1)) || (e = dalloc(&f->lr_dev, 1)))
         return fail(e);
     // He-uniform weights (seeded); zero biases, zero padding input columns of
     // W1 and zero padding rows of W4; the output layer scaled by 0.1
@@ -1080,6 +1183,7 @@ void ntp_flow_destroy(ntp_flow* f) {
     if (!f) return;
     cudaSetDevice(f->device);
     if (f->stream) cudaStreamSynchronize(f->stream);
+    if (f->gexec) cudaGraphExecDestroy(f->gexec);
     free_all(f);
     if (f->stream) cudaStreamDestroy(f->stream);
     delete f;
@@ -1109,6 +1213,8 @@ ntp_status ntp_flow_set_params(ntp_flow* f, const float* host, uint64_t n) {
     F_CUDA(f, cudaMemsetAsync(f->m, 0, sizeof(float) * n, f->stream));
     F_CUDA(f, cudaMemsetAsync(f->v, 0, sizeof(float) * n, f->stream));
     F_CUDA(f, cudaMemsetAsync(f->grad, 0, sizeof(float) * n, f->stream));
+    F_CUDA(f, cudaMemsetAsync(f->step_dev, 0, sizeof(int), f->stream));
+    F_CUDA(f, cudaMemcpyAsync(f->lr_dev, &f->lr, sizeof(float), cudaMemcpyHostToDevice, f->stream));
     F_CUDA(f, cudaStreamSynchronize(f->stream));
     f->step = 0;
     return NTP_OK;
@@ -1117,6 +1223,9 @@ ntp_status ntp_flow_set_params(ntp_flow* f, const float* host, uint64_t n) {
 ntp_status ntp_flow_set_lr(ntp_flow* f, float lr) {
     if (!f || !(lr > 0.0f)) return NTP_ERR_INVALID;
     f->lr = lr;
+    F_CUDA(f, cudaSetDevice(f->device));
+    F_CUDA(f, cudaMemcpyAsync(f->lr_dev, &f->lr, sizeof(float), cudaMemcpyHostToDevice, f->stream));
+    F_CUDA(f, cudaStreamSynchronize(f->stream));
     return NTP_OK;
 }
 
@@ -1139,88 +1248,51 @@ ntp_status ntp_flow_train_step(ntp_flow* f, const float* cond, const float* tres
     }
     F_CUDA(f, cudaSetDevice(f->device));
     cudaStream_t st = f->stream;
-    const float* dy = tres;
-    const float* dn = nhits;
-    const int* dh = has_time;
-    if (!on_device) {
-        F_CUDA(f, cudaMemcpyAsync(f->y, tres, sizeof(float) * B, cudaMemcpyHostToDevice, st));
-        F_CUDA(f, cudaMemcpyAsync(f->nh, nhits, sizeof(float) * B, cudaMemcpyHostToDevice, st));
-        F_CUDA(f, cudaMemcpyAsync(f->hy, has_time, sizeof(int) * B, cudaMemcpyHostToDevice, st));
-        dy = f->y;
-        dn = f->nh;
-        dh = f->hy;
-    }
-    F_CUDA(f, cudaMemsetAsync(f->gemm_err, 0, sizeof(int), st));
-    F_OK(pack(f, cond, B, B, on_device));
-    F_OK(forward(f, B, true));
-    F_CUDA(f, cudaMemsetAsync(f->loss, 0, sizeof(double), st));
-    F_CUDA(f, cudaMemsetAsync(f->grad, 0, sizeof(float) * f->n_params, st));
-    float* g = f->grad;
-    auto gw = [&](int l) { return g + f->blk[2 * l].off; };
-    auto gb = [&](int l) { return g + f->blk[2 * l + 1].off; };
-    F_OK(launch_head(f, dy, dn, dh, B, nullptr, gb(3)));
-    F_CUDA(f, cudaGetLastError());
-    // output layer: dW4 = dP^T H3
-    ntp::GemmEpilogue ew{};
-    ew.out_kind = 2;
-    ew.ldc = kHid;
-    ew.c = gw(3);
-    F_OK(gemm(f, f->dpt, B, f->ht[2], B, f->n_pad, kHid, B, ew, 0));
-    const bf16* dnext = f->dp;
-    int k_next = f->n_pad;
-    for (int l = 2; l >= 0; --l) {
-        // dZ_l = (dZ_{l+1} W_{l+1}) masked by H_l > 0, its transpose, and its
-        // column sums (the bias gradient of layer l)
-        ntp::GemmEpilogue ed{};
-        ed.c = f->dz[l];
-        ed.ldc = kHid;
-        ed.out_kind = 1;
-        ed.ct = f->dzt[l];
-        ed.ldct = B;
-        ed.mask = f->h[l];
-        ed.ldm = kHid;
-        ed.colsum = gb(l);
-        F_OK(gemm(f, dnext, k_next, f->wt[l + 1], k_next, B, kHid, k_next, ed));
-        // dW_l = dZ_l^T X_l with X_l = H_{l-1} or the packed input
-        ntp::GemmEpilogue eg{};
-        eg.out_kind = 2;
-        eg.c = gw(l);
-        eg.ldc = l == 0 ? kIn : kHid;
-        const bf16* xt = l == 0 ? f->xt : f->ht[l - 1];
-        F_OK(gemm(f, f->dzt[l], B, xt, B, kHid, l == 0 ? kIn : kHid, B, eg, 0));
-        dnext = f->dz[l];
-        k_next = kHid;
-    }
-    if (update) {
-        ++f->step;
-        const float c1 = 1.0f - std::pow(f->b1, static_cast<float>(f->step));
-        const float c2 = 1.0f - std::pow(f->b2, static_cast<float>(f->step));
-        ntp::ParamBlocks pb{};
-        pb.n = 8;
-        for (int i = 0; i < 8; ++i) {
-            pb.off[i] = static_cast<long long>(f->blk[i].off);
-            pb.rows[i] = f->blk[i].rows;
-            pb.cols[i] = f->blk[i].cols;
-            pb.wb[i] = (i % 2) == 0 ? f->wb[i / 2] : nullptr;
-            pb.wt[i] = (i % 2) == 0 ? f->wt[i / 2] : nullptr;
+    // the batch into the staging buffers the step reads
+    const cudaMemcpyKind kind = on_device ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice;
+    F_CUDA(f, cudaMemcpyAsync(f->cond, cond, sizeof(float) * kCond * B, kind, st));
+    F_CUDA(f, cudaMemcpyAsync(f->y, tres, sizeof(float) * B, kind, st));
+    F_CUDA(f, cudaMemcpyAsync(f->nh, nhits, sizeof(float) * B, kind, st));
+    F_CUDA(f, cudaMemcpyAsync(f->hy, has_time, sizeof(int) * B, kind, st));
+    if (f->use_graph) {
+        if (!f->gexec || f->g_B != B || f->g_update != update) {
+            if (f->gexec) cudaGraphExecDestroy(f->gexec);
+            f->gexec = nullptr;
+            F_CUDA(f, prepare_kernels(f));
+            F_CUDA(f, cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
+            const ntp_status rs = record_step(f, B, update != 0);
+            cudaGraph_t graph = nullptr;
+            const cudaError_t ec = cudaStreamEndCapture(st, &graph);
+            if (rs != NTP_OK || ec != cudaSuccess) {
+                if (graph) cudaGraphDestroy(graph);
+                if (rs != NTP_OK) return rs;
+                return ferr(f, ec, "ntp_flow_train_step: capture");
+            }
+            const cudaError_t ei = cudaGraphInstantiate(&f->gexec, graph, 0);
+            cudaGraphDestroy(graph);
+            if (ei != cudaSuccess) {
+                f->gexec = nullptr;
+                return ferr(f, ei, "ntp_flow_train_step: instantiate");
+            }
+            f->g_B = B;
+            f->g_update = update;
         }
-        pb.off[8] = static_cast<long long>(f->n_params);
-        const int grid = static_cast<int>(std::min<size_t>((f->n_params + 255) / 256, 152 * 8));
-        F_CUDA(f, cudaMemsetAsync(f->skip, 0, sizeof(int), st));
-        ntp::nonfinite_kernel<<<grid, 256, 0, st>>>(g, static_cast<long long>(f->n_params), f->skip);
-        ntp::adam_kernel<<<grid, 256, 0, st>>>(f->theta, f->m, f->v, g, pb, f->lr, f->b1, f->b2, f->eps, c1, c2,
-                                               f->skip);
-        F_CUDA(f, cudaGetLastError());
+        F_CUDA(f, cudaGraphLaunch(f->gexec, st));
+    } else {
+        F_OK(record_step(f, B, update != 0));
     }
     double hl = 0.0;
     int skipped = 0;
     F_CUDA(f, cudaMemcpyAsync(&hl, f->loss, sizeof(double), cudaMemcpyDeviceToHost, st));
     if (update) F_CUDA(f, cudaMemcpyAsync(&skipped, f->skip, sizeof(int), cudaMemcpyDeviceToHost, st));
     F_OK(check_gemm(f));
-    if (skipped) {
-        --f->step;  // Adam's bias correction counts the steps taken
-        ++f->skipped;
-        hl = std::numeric_limits<double>::quiet_NaN();
+    if (update) {
+        if (skipped) {
+            ++f->skipped;
+            hl = std::numeric_limits<double>::quiet_NaN();
+        } else {
+            ++f->step;
+        }
     }
     if (loss_out) *loss_out = hl;
     return NTP_OK;

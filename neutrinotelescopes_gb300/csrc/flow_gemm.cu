@@ -376,21 +376,29 @@ bool make_map(CUtensorMap* map, const void* base, int rows, int cols, int ld, in
                CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
 }
 
+// Sets the dynamic shared-memory limit of the BN variant once per device.
+template <int BN>
+cudaError_t configure_bn() {
+    static std::atomic<unsigned long long> configured{0};  // one bit per device
+    int dev = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e != cudaSuccess) return e;
+    const unsigned long long bit = 1ull << (dev & 63);
+    if (!(configured.load() & bit)) {
+        e = cudaFuncSetAttribute(gemm_bf16_kernel<BN>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 static_cast<int>(sizeof(Smem<BN>) + 1024));
+        if (e != cudaSuccess) return e;
+        configured.fetch_or(bit);
+    }
+    return cudaSuccess;
+}
+
 template <int BN>
 cudaError_t launch_bn(const CUtensorMap& ma, const CUtensorMap& mb, int M, int N, int splits, int k_tiles,
                       const GemmEpilogue& ep, int vec_ok, int* error, cudaStream_t st) {
     const size_t smem = sizeof(Smem<BN>) + 1024;
-    int dev = 0;
-    cudaError_t e = cudaGetDevice(&dev);
+    cudaError_t e = configure_bn<BN>();
     if (e != cudaSuccess) return e;
-    static std::atomic<unsigned long long> configured{0};  // one bit per device
-    const unsigned long long bit = 1ull << (dev & 63);
-    if (!(configured.load() & bit)) {
-        e = cudaFuncSetAttribute(gemm_bf16_kernel<BN>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                 static_cast<int>(smem));
-        if (e != cudaSuccess) return e;
-        configured.fetch_or(bit);
-    }
     const int per = (k_tiles + splits - 1) / splits;
     dim3 grid((M + kBM - 1) / kBM, (N + BN - 1) / BN, (k_tiles + per - 1) / per);
     gemm_bf16_kernel<BN><<<grid, kThreads, smem, st>>>(ma, mb, M, N, per, k_tiles, ep, vec_ok, error);
@@ -453,6 +461,15 @@ cudaError_t gemm_bf16_ep(const void* A, int lda, const void* B, int ldb, int M, 
     if (bn == 64) return launch_bn<64>(ma, mb, M, N, splits, k_tiles, ep, vec_ok, error, st);
     if (bn == 128) return launch_bn<128>(ma, mb, M, N, splits, k_tiles, ep, vec_ok, error, st);
     return launch_bn<256>(ma, mb, M, N, splits, k_tiles, ep, vec_ok, error, st);
+}
+
+cudaError_t gemm_prepare() {
+    cudaError_t e = configure_bn<64>();
+    if (e == cudaSuccess) e = configure_bn<128>();
+    if (e == cudaSuccess) e = configure_bn<256>();
+    if (e == cudaSuccess) (void)sm_count();
+    if (e == cudaSuccess && !encode_fn()) e = cudaErrorNotSupported;  // the driver's tensor-map encoder
+    return e;
 }
 
 cudaError_t gemm_bf16(const void* A, int lda, const void* B, int ldb, void* C, int ldc, int M, int N, int K,

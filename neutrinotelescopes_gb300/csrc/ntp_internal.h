@@ -148,6 +148,8 @@ struct GemmEpilogue {
 };
 cudaError_t gemm_bf16_ep(const void* A, int lda, const void* B, int ldb, int M, int N, int K, const GemmEpilogue& ep,
                          int splits, int* error, cudaStream_t st);
+// Sets the GEMM kernels' function attributes (before a stream capture).
+cudaError_t gemm_prepare();
 
 // C = A * B^T, BF16 operands (K-major), FP32 accumulation on the tensor cores
 // (flow_gemm.cu).  out_kind: 0 = FP32, 1 = BF16, 2 = FP32 atomic add.
