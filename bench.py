@@ -198,7 +198,8 @@ def flow_bench(train_steps: int = 300, n_tuples: int = 100_000_000) -> dict:
       table      -- the MC kernel generates a training table (8192 simulations,
                     distance 1-200 m log-uniform, direction isotropic, log10 E
                     2-6, 16 module orientations each) on the device;
-      training   -- train_step on rows of that table already in HBM;
+      training   -- Adam steps on rows of that table already in HBM, run
+                    back to back by one multi-step call;
                     samples/s and the conditioner GEMMs' tensor throughput
                     (algorithmic FLOPs: 3 x forward, forward = 2 x (5 x 256 +
                     2 x 256 x 256 + 256 x 188) per sample);
@@ -230,15 +231,20 @@ def flow_bench(train_steps: int = 300, n_tuples: int = 100_000_000) -> dict:
     torch.cuda.synchronize()
     nb = len(tab) // bs
 
-    def tstep(i):
-        s = (i % nb) * bs
-        return fl.train_step(cond[s:s + bs], tres[s:s + bs], nh[s:s + bs], has[s:s + bs])
+    def tsteps(first, n):
+        # consecutive batches of the shuffled table, one host synchronisation per pass
+        done = []
+        while len(done) < n:
+            b0 = (first + len(done)) % nb
+            k = min(n - len(done), nb - b0)
+            s = b0 * bs
+            done += fl.train_steps(cond[s:], tres[s:], nh[s:], has[s:], bs, k)
+        return done
 
-    for i in range(20):
-        tstep(i)
+    tsteps(0, 20)
     torch.cuda.synchronize()
     t0 = time.perf_counter()
-    losses = [tstep(20 + i) for i in range(train_steps)]
+    losses = tsteps(20, train_steps)
     torch.cuda.synchronize()
     dt = time.perf_counter() - t0
     fwd_flops = 2 * (5 * 256 + 2 * 256 * 256 + 256 * 188)

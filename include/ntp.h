@@ -441,6 +441,14 @@ ntp_status ntp_flow_get_params(ntp_flow* flow, float* host, uint64_t n, int32_t 
 ntp_status ntp_flow_train_step(ntp_flow* flow, const float* cond, const float* tres, const float* nhits,
                                const int32_t* has_time, int32_t B, int32_t on_device, int32_t update,
                                double* loss);
+/* n_steps training steps on consecutive batches of B rows (rows i*B ..
+   (i+1)*B - 1 form step i), one synchronisation for all of them; losses
+   (host, n_steps, may be NULL) receives each step's loss (NaN for a skipped
+   step).  The training step itself is captured once as a CUDA graph and
+   replayed (NTP_FLOW_GRAPH=0 in the environment runs it eagerly). */
+ntp_status ntp_flow_train_steps(ntp_flow* flow, const float* cond, const float* tres, const float* nhits,
+                                const int32_t* has_time, int32_t B, int32_t n_steps, int32_t on_device,
+                                int32_t update, double* losses);
 /* The conditioner's raw outputs for n conditions (host): params_out [n x n_outputs]. */
 ntp_status ntp_flow_forward(ntp_flow* flow, const float* cond, int32_t n, float* params_out);
 /* The loss and its gradient by the raw outputs, for given raw outputs

@@ -846,6 +846,8 @@ struct Block {  // one parameter block of the flat FP32 vector
 struct ntp_flow {
     int device = 0;
     cudaStream_t stream = nullptr;
+    cudaStream_t stream2 = nullptr;  // weight-gradient GEMMs, alongside the activation-gradient chain
+    cudaEvent_t ev[5] = {};
     int cap = 0;  // batch capacity (multiple of 128)
     int L = 1, K = 12, n_out = 0, n_pad = 0;
     float r0 = -20.0f, r1 = 1500.0f;
@@ -874,6 +876,10 @@ struct ntp_flow {
     bool use_graph = true;
     cudaGraphExec_t gexec = nullptr;
     int g_B = 0, g_update = -1;
+    // per-step losses and skip flags of a multi-step call (grown on demand)
+    double* loss_hist = nullptr;
+    int* skip_hist = nullptr;
+    int hist_cap = 0;
     // inference
     float* knots = nullptr;
     size_t knots_cap = 0;
@@ -913,8 +919,8 @@ cudaError_t dalloc(T** p, size_t n) {
 }
 
 ntp_status gemm(ntp_flow* f, const bf16* A, int lda, const bf16* B, int ldb, int M, int N, int K,
-                const ntp::GemmEpilogue& ep, int splits = 1) {
-    F_CUDA(f, ntp::gemm_bf16_ep(A, lda, B, ldb, M, N, K, ep, splits, f->gemm_err, f->stream));
+                const ntp::GemmEpilogue& ep, int splits = 1, cudaStream_t st = nullptr) {
+    F_CUDA(f, ntp::gemm_bf16_ep(A, lda, B, ldb, M, N, K, ep, splits, f->gemm_err, st ? st : f->stream));
     return NTP_OK;
 }
 
@@ -992,7 +998,7 @@ ntp_status launch_head(ntp_flow* f, const float* y, const float* nh, const int* 
 
 void free_all(ntp_flow* f) {
     void* ps[] = {f->theta, f->m, f->v, f->grad, f->x, f->xt, f->dp, f->dpt, f->P, f->cond, f->y, f->nh, f->hy,
-                  f->loss, f->gemm_err, f->skip, f->step_dev, f->lr_dev, f->knots};
+                  f->loss, f->gemm_err, f->skip, f->step_dev, f->lr_dev, f->knots, f->loss_hist, f->skip_hist};
     for (void* p : ps)
         if (p) cudaFree(p);
     for (int l = 0; l < 4; ++l) {
@@ -1020,12 +1026,17 @@ ntp_status record_step(ntp_flow* f, int B, bool update) {
     auto gw = [&](int l) { return g + f->blk[2 * l].off; };
     auto gb = [&](int l) { return g + f->blk[2 * l + 1].off; };
     F_OK(launch_head(f, f->y, f->nh, f->hy, B, nullptr, gb(3)));
-    // output layer: dW4 = dP^T H3
-    ntp::GemmEpilogue ew{};
+    // The weight gradients dW_l = dZ_l^T X_l run on stream2 beside the chain
+    // of activation gradients dZ_{l-1} = (dZ_l W_l) * mask on the main stream;
+    // events order each dW_l after its dZ_l and join the two before Adam.
+    cudaStream_t s2 = f->stream2;
+    F_CUDA(f, cudaEventRecord(f->ev[0], st));
+    F_CUDA(f, cudaStreamWaitEvent(s2, f->ev[0], 0));
+    ntp::GemmEpilogue ew{};  // output layer: dW4 = dP^T H3
     ew.out_kind = 2;
     ew.ldc = kHid;
     ew.c = gw(3);
-    F_OK(gemm(f, f->dpt, B, f->ht[2], B, f->n_pad, kHid, B, ew, 0));
+    F_OK(gemm(f, f->dpt, B, f->ht[2], B, f->n_pad, kHid, B, ew, 0, s2));
     const bf16* dnext = f->dp;
     int k_next = f->n_pad;
     for (int l = 2; l >= 0; --l) {
@@ -1041,16 +1052,20 @@ ntp_status record_step(ntp_flow* f, int B, bool update) {
         ed.ldm = kHid;
         ed.colsum = gb(l);
         F_OK(gemm(f, dnext, k_next, f->wt[l + 1], k_next, B, kHid, k_next, ed));
+        F_CUDA(f, cudaEventRecord(f->ev[3 - l], st));
+        F_CUDA(f, cudaStreamWaitEvent(s2, f->ev[3 - l], 0));
         // dW_l = dZ_l^T X_l with X_l = H_{l-1} or the packed input
         ntp::GemmEpilogue eg{};
         eg.out_kind = 2;
         eg.c = gw(l);
         eg.ldc = l == 0 ? kIn : kHid;
         const bf16* xt = l == 0 ? f->xt : f->ht[l - 1];
-        F_OK(gemm(f, f->dzt[l], B, xt, B, kHid, l == 0 ? kIn : kHid, B, eg, 0));
+        F_OK(gemm(f, f->dzt[l], B, xt, B, kHid, l == 0 ? kIn : kHid, B, eg, 0, s2));
         dnext = f->dz[l];
         k_next = kHid;
     }
+    F_CUDA(f, cudaEventRecord(f->ev[4], s2));
+    F_CUDA(f, cudaStreamWaitEvent(st, f->ev[4], 0));
     if (update) {
         ntp::ParamBlocks pb{};
         pb.n = 8;
@@ -1128,6 +1143,9 @@ ntp_status ntp_flow_create(int32_t device, const ntp_flow_config* cfg, ntp_flow*
     f->n_params = off;
     auto fail = [&](cudaError_t e) {
         if (f->stream) cudaStreamDestroy(f->stream);
+        if (f->stream2) cudaStreamDestroy(f->stream2);
+        for (cudaEvent_t ev : f->ev)
+            if (ev) cudaEventDestroy(ev);
         free_all(f);
         delete f;
         return e == cudaErrorMemoryAllocation ? NTP_ERR_NOMEM : NTP_ERR_CUDA;
@@ -1135,6 +1153,9 @@ ntp_status ntp_flow_create(int32_t device, const ntp_flow_config* cfg, ntp_flow*
     cudaError_t e;
     if ((e = cudaSetDevice(device)) != cudaSuccess) return fail(e);
     if ((e = cudaStreamCreateWithFlags(&f->stream, cudaStreamNonBlocking)) != cudaSuccess) return fail(e);
+    if ((e = cudaStreamCreateWithFlags(&f->stream2, cudaStreamNonBlocking)) != cudaSuccess) return fail(e);
+    for (cudaEvent_t& ev : f->ev)
+        if ((e = cudaEventCreateWithFlags(&ev, cudaEventDisableTiming)) != cudaSuccess) return fail(e);
     const size_t B = f->cap;
     if ((e = dalloc(&f->theta, off)) || (e = dalloc(&f->m, off)) || (e = dalloc(&f->v, off)) ||
         (e = dalloc(&f->grad, off)))
@@ -1184,7 +1205,11 @@ void ntp_flow_destroy(ntp_flow* f) {
     cudaSetDevice(f->device);
     if (f->stream) cudaStreamSynchronize(f->stream);
     if (f->gexec) cudaGraphExecDestroy(f->gexec);
+    if (f->stream2) cudaStreamSynchronize(f->stream2);
     free_all(f);
+    for (cudaEvent_t ev : f->ev)
+        if (ev) cudaEventDestroy(ev);
+    if (f->stream2) cudaStreamDestroy(f->stream2);
     if (f->stream) cudaStreamDestroy(f->stream);
     delete f;
 }
@@ -1241,60 +1266,87 @@ ntp_status ntp_flow_get_params(ntp_flow* f, float* host, uint64_t n, int32_t whi
 ntp_status ntp_flow_train_step(ntp_flow* f, const float* cond, const float* tres, const float* nhits,
                                const int32_t* has_time, int32_t B, int32_t on_device, int32_t update,
                                double* loss_out) {
-    if (!f || !cond || !tres || !nhits || !has_time) return NTP_ERR_INVALID;
+    return ntp_flow_train_steps(f, cond, tres, nhits, has_time, B, 1, on_device, update, loss_out);
+}
+
+ntp_status ntp_flow_train_steps(ntp_flow* f, const float* cond, const float* tres, const float* nhits,
+                                const int32_t* has_time, int32_t B, int32_t n_steps, int32_t on_device,
+                                int32_t update, double* losses) {
+    if (!f || !cond || !tres || !nhits || !has_time || n_steps < 1) return NTP_ERR_INVALID;
     if (B < 128 || B > f->cap || B % 128) {
         f->err = "ntp_flow_train_step: the batch must be a multiple of 128 up to the capacity";
         return NTP_ERR_INVALID;
     }
     F_CUDA(f, cudaSetDevice(f->device));
     cudaStream_t st = f->stream;
-    // the batch into the staging buffers the step reads
+    // per-step loss and skip flag, gathered on the device and read once
+    if (f->hist_cap < n_steps) {
+        if (f->loss_hist) cudaFree(f->loss_hist);
+        if (f->skip_hist) cudaFree(f->skip_hist);
+        f->loss_hist = nullptr;
+        f->skip_hist = nullptr;
+        f->hist_cap = 0;
+        F_CUDA(f, dalloc(&f->loss_hist, static_cast<size_t>(n_steps)));
+        F_CUDA(f, dalloc(&f->skip_hist, static_cast<size_t>(n_steps)));
+        f->hist_cap = n_steps;
+    }
+    double* d_loss = f->loss_hist;
+    int* d_skip = f->skip_hist;
+    F_CUDA(f, cudaMemsetAsync(d_skip, 0, sizeof(int) * n_steps, st));
     const cudaMemcpyKind kind = on_device ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice;
-    F_CUDA(f, cudaMemcpyAsync(f->cond, cond, sizeof(float) * kCond * B, kind, st));
-    F_CUDA(f, cudaMemcpyAsync(f->y, tres, sizeof(float) * B, kind, st));
-    F_CUDA(f, cudaMemcpyAsync(f->nh, nhits, sizeof(float) * B, kind, st));
-    F_CUDA(f, cudaMemcpyAsync(f->hy, has_time, sizeof(int) * B, kind, st));
-    if (f->use_graph) {
-        if (!f->gexec || f->g_B != B || f->g_update != update) {
-            if (f->gexec) cudaGraphExecDestroy(f->gexec);
-            f->gexec = nullptr;
-            F_CUDA(f, prepare_kernels(f));
-            F_CUDA(f, cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
-            const ntp_status rs = record_step(f, B, update != 0);
-            cudaGraph_t graph = nullptr;
-            const cudaError_t ec = cudaStreamEndCapture(st, &graph);
-            if (rs != NTP_OK || ec != cudaSuccess) {
-                if (graph) cudaGraphDestroy(graph);
-                if (rs != NTP_OK) return rs;
-                return ferr(f, ec, "ntp_flow_train_step: capture");
-            }
-            const cudaError_t ei = cudaGraphInstantiate(&f->gexec, graph, 0);
-            cudaGraphDestroy(graph);
-            if (ei != cudaSuccess) {
+    for (int i = 0; i < n_steps; ++i) {
+        const size_t o = static_cast<size_t>(i) * B;
+        // the batch into the staging buffers the step reads
+        F_CUDA(f, cudaMemcpyAsync(f->cond, cond + o * kCond, sizeof(float) * kCond * B, kind, st));
+        F_CUDA(f, cudaMemcpyAsync(f->y, tres + o, sizeof(float) * B, kind, st));
+        F_CUDA(f, cudaMemcpyAsync(f->nh, nhits + o, sizeof(float) * B, kind, st));
+        F_CUDA(f, cudaMemcpyAsync(f->hy, has_time + o, sizeof(int) * B, kind, st));
+        if (f->use_graph) {
+            if (!f->gexec || f->g_B != B || f->g_update != update) {
+                if (f->gexec) cudaGraphExecDestroy(f->gexec);
                 f->gexec = nullptr;
-                return ferr(f, ei, "ntp_flow_train_step: instantiate");
+                F_CUDA(f, prepare_kernels(f));
+                F_CUDA(f, cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
+                const ntp_status rs = record_step(f, B, update != 0);
+                cudaGraph_t graph = nullptr;
+                const cudaError_t ec = cudaStreamEndCapture(st, &graph);
+                if (rs != NTP_OK || ec != cudaSuccess) {
+                    if (graph) cudaGraphDestroy(graph);
+                    if (rs != NTP_OK) return rs;
+                    return ferr(f, ec, "ntp_flow_train_step: capture");
+                }
+                const cudaError_t ei = cudaGraphInstantiate(&f->gexec, graph, 0);
+                cudaGraphDestroy(graph);
+                if (ei != cudaSuccess) {
+                    f->gexec = nullptr;
+                    return ferr(f, ei, "ntp_flow_train_step: instantiate");
+                }
+                f->g_B = B;
+                f->g_update = update;
             }
-            f->g_B = B;
-            f->g_update = update;
-        }
-        F_CUDA(f, cudaGraphLaunch(f->gexec, st));
-    } else {
-        F_OK(record_step(f, B, update != 0));
-    }
-    double hl = 0.0;
-    int skipped = 0;
-    F_CUDA(f, cudaMemcpyAsync(&hl, f->loss, sizeof(double), cudaMemcpyDeviceToHost, st));
-    if (update) F_CUDA(f, cudaMemcpyAsync(&skipped, f->skip, sizeof(int), cudaMemcpyDeviceToHost, st));
-    F_OK(check_gemm(f));
-    if (update) {
-        if (skipped) {
-            ++f->skipped;
-            hl = std::numeric_limits<double>::quiet_NaN();
+            F_CUDA(f, cudaGraphLaunch(f->gexec, st));
         } else {
-            ++f->step;
+            F_OK(record_step(f, B, update != 0));
         }
+        F_CUDA(f, cudaMemcpyAsync(d_loss + i, f->loss, sizeof(double), cudaMemcpyDeviceToDevice, st));
+        if (update) F_CUDA(f, cudaMemcpyAsync(d_skip + i, f->skip, sizeof(int), cudaMemcpyDeviceToDevice, st));
     }
-    if (loss_out) *loss_out = hl;
+    std::vector<double> hl(n_steps);
+    std::vector<int> hs(n_steps);
+    F_CUDA(f, cudaMemcpyAsync(hl.data(), d_loss, sizeof(double) * n_steps, cudaMemcpyDeviceToHost, st));
+    F_CUDA(f, cudaMemcpyAsync(hs.data(), d_skip, sizeof(int) * n_steps, cudaMemcpyDeviceToHost, st));
+    F_OK(check_gemm(f));
+    for (int i = 0; i < n_steps; ++i) {
+        if (update) {
+            if (hs[i]) {
+                ++f->skipped;
+                hl[i] = std::numeric_limits<double>::quiet_NaN();
+            } else {
+                ++f->step;
+            }
+        }
+        if (losses) losses[i] = hl[i];
+    }
     return NTP_OK;
 }
 

@@ -229,11 +229,23 @@ class RQNormFlow:
             nh = table.nhits[perm].contiguous()
             has = table.has_time[perm].contiguous()
             torch.cuda.synchronize()
-            for s in range(0, n - bs + 1, bs):
-                losses.append(self.train_step(cond[s:s + bs], tres[s:s + bs], nh[s:s + bs], has[s:s + bs]))
-                if max_steps is not None and len(losses) >= max_steps:
-                    return losses
+            steps = n // bs
+            if max_steps is not None:
+                steps = min(steps, max_steps - len(losses))
+            if steps > 0:
+                losses.extend(self.train_steps(cond, tres, nh, has, bs, steps))
+            if max_steps is not None and len(losses) >= max_steps:
+                return losses
         return losses
+
+    def train_steps(self, cond, tres, nhits, has_time, batch: int, steps: int) -> list[float]:
+        """`steps` Adam steps on consecutive batches of `batch` rows of CUDA
+        tensors, one synchronisation for all; returns the losses."""
+        out = np.empty(steps, np.float64)
+        self._check(self.lib.ntp_flow_train_steps(self._h, cond.data_ptr(), tres.data_ptr(), nhits.data_ptr(),
+                                                  has_time.data_ptr(), int(batch), int(steps), 1, 1,
+                                                  out.ctypes.data))
+        return out.tolist()
 
     # --------------------------------------------------------------- inference
     def forward_params(self, cond) -> np.ndarray:

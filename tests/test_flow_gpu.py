@@ -187,6 +187,25 @@ def test_adam_steps_and_weight_copies():
         assert np.all(np.abs(P - ref) <= 2e-3 * (1 + np.abs(ref)))
 
 
+def test_multi_step_call_follows_single_steps():
+    """ntp_flow_train_steps over n consecutive batches gives the losses and
+    parameters of n single train_step calls (the split-K weight gradients add
+    in FP32 atomics, so equal up to rounding)."""
+    L, K, r0, r1 = 5, 12, -20.0, 1500.0
+    rng = np.random.default_rng(31)
+    B, n = 512, 6
+    cond, tres, nhits, has = batch(rng, B * n, r0, r1)
+    hp = RQNormFlowHParams(K=K, n_layers=L, range_min=r0, range_max=r1, batch_size=B, seed=4, lr=1e-3)
+    with RQNormFlow(hp) as a, RQNormFlow(hp) as b:
+        la = [a.train_step(cond[i * B:(i + 1) * B], tres[i * B:(i + 1) * B], nhits[i * B:(i + 1) * B],
+                           has[i * B:(i + 1) * B]) for i in range(n)]
+        dev = lambda x: torch.as_tensor(x, device="cuda")  # noqa: E731
+        lb = b.train_steps(dev(cond), dev(tres), dev(nhits), dev(has), B, n)
+        assert len(lb) == n and np.all(np.isfinite(lb))
+        np.testing.assert_allclose(lb, la, rtol=1e-4)
+        np.testing.assert_allclose(b.get_params(), a.get_params(), rtol=1e-3, atol=1e-5)
+
+
 @pytest.mark.parametrize("L,K,r0,r1", CASES)
 def test_evaluate_matches_oracle_on_the_same_parameters(L, K, r0, r1):
     rng = np.random.default_rng(40)
