@@ -468,6 +468,19 @@ ntp_status ntp_flow_evaluate(ntp_flow* flow, const float* cond, int32_t n_cond, 
    ntp_flow_evaluate (may be NULL).  Host, or device buffers with on_device. */
 ntp_status ntp_flow_evaluate_grid(ntp_flow* flow, const float* cond, int32_t n_cond, const float* times,
                                   int32_t n_times, float* logpdf, float* log_expec, int32_t on_device);
+/* The pooled arrival-time CDF of a mixture of conditions:
+   cdf[j] = sum_c w_c F(times[j] - offset[c] | cond[c]) / sum_c w_c, with F
+   the flow's CDF (the base normal's CDF of the inverse-transformed time: the
+   splines and the affine map are increasing bijections) and w_c = weight[c],
+   or the condition's expected count exp(log expectation) when weight is
+   NULL; offset may be NULL (0).  With the conditions of one event's PMTs and
+   their geometric times as offsets this is the event's predicted hit-time
+   CDF, the reference of a one-sample Kolmogorov-Smirnov test of Monte Carlo
+   hits.  No reference counterpart.  Host, or device buffers with on_device;
+   cdf in FP64. */
+ntp_status ntp_flow_mixture_cdf(ntp_flow* flow, const float* cond, int32_t n_cond, const float* weight,
+                                const float* offset, const float* times, uint64_t n_times, double* cdf,
+                                int32_t on_device);
 
 /* Sampling from the surrogate (the hits a PMT sees, as the MC would give
    them after resample_simulation): per condition c a count N_c ~

@@ -263,6 +263,7 @@ EXPORTED = (
     "ntp_flow_set_lr",
     "ntp_flow_train_step",
     "ntp_flow_train_steps",
+    "ntp_flow_mixture_cdf",
     "ntp_flow_forward",
     "ntp_flow_head",
     "ntp_flow_evaluate",
@@ -331,6 +332,7 @@ def _declare(lib: C.CDLL) -> None:
     lib.ntp_flow_set_lr.restype = C.c_int
     lib.ntp_flow_train_step.argtypes = [vp, vp, vp, vp, vp, i32, i32, i32, C.POINTER(C.c_double)]
     lib.ntp_flow_train_steps.argtypes = [vp, vp, vp, vp, vp, i32, i32, i32, i32, vp]
+    lib.ntp_flow_mixture_cdf.argtypes = [vp, vp, i32, vp, vp, vp, u64, vp, i32]
     lib.ntp_flow_forward.argtypes = [vp, vp, i32, vp]
     lib.ntp_flow_head.argtypes = [vp, vp, vp, vp, vp, i32, C.POINTER(C.c_double), vp]
     lib.ntp_flow_evaluate.argtypes = [vp, vp, i32, vp, vp, u64, vp, vp, i32]
@@ -338,7 +340,7 @@ def _declare(lib: C.CDLL) -> None:
     lib.ntp_flow_evaluate_grid.argtypes = [vp, vp, i32, vp, i32, vp, vp, i32]
     for name in ("ntp_flow_create", "ntp_flow_get_layout", "ntp_flow_set_params", "ntp_flow_get_params",
                  "ntp_flow_train_step", "ntp_flow_forward", "ntp_flow_head", "ntp_flow_evaluate",
-                 "ntp_flow_sample", "ntp_flow_evaluate_grid", "ntp_flow_train_steps"):
+                 "ntp_flow_sample", "ntp_flow_evaluate_grid", "ntp_flow_train_steps", "ntp_flow_mixture_cdf"):
         getattr(lib, name).restype = C.c_int
     lib.ntp_server_create.argtypes = [vp, C.POINTER(NtpServerConfig), C.POINTER(vp)]
     lib.ntp_server_destroy.argtypes = [vp]

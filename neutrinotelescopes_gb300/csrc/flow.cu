@@ -733,6 +733,76 @@ __global__ void logpdf_grid_kernel(const float* __restrict__ knots, int L, int n
     }
 }
 
+// sum of the mixture weights: w[c], or exp(log expectation) of the knot rows
+// when w is NULL; one block
+__global__ void mixture_total_kernel(const float* __restrict__ knots, int L, int K, int n_cond,
+                                     const float* __restrict__ w, double* __restrict__ total) {
+    __shared__ double part[32];
+    double acc = 0.0;
+    for (int c = threadIdx.x; c < n_cond; c += blockDim.x)
+        acc += w ? static_cast<double>(w[c])
+                 : exp(static_cast<double>(knots[static_cast<size_t>(c) * knot_row(L, K) + L * 3 * (K + 1) + 2]));
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
+    if ((threadIdx.x & 31) == 0) part[threadIdx.x >> 5] = acc;
+    __syncthreads();
+    if (threadIdx.x < 32) {
+        acc = threadIdx.x < (blockDim.x >> 5) ? part[threadIdx.x] : 0.0;
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
+        if (threadIdx.x == 0) *total = acc;
+    }
+}
+
+// The pooled CDF of a mixture of conditions at times t_j:
+//   F(t_j) = sum_c w_c Phi(u_c(t_j - off_c)) / sum_c w_c,
+// Phi of the base-normal residual being each condition's CDF (the splines
+// and the affine map are increasing bijections).  A block takes blockDim.x
+// consecutive times, one per thread, and walks the conditions in tiles whose
+// knot rows (and weights, offsets) are staged in shared memory.
+constexpr int kMixTile = 32;
+template <int K>
+__global__ void mixture_cdf_kernel(const float* __restrict__ knots, int L, int n_cond, const float* __restrict__ w,
+                                   const float* __restrict__ off, const float* __restrict__ t, unsigned long long n,
+                                   const double* __restrict__ total, double* __restrict__ out) {
+    extern __shared__ float s_tile[];
+    const int row = knot_row(L, K);
+    float* s_w = s_tile + kMixTile * row;
+    float* s_off = s_w + kMixTile;
+    const unsigned long long j = blockIdx.x * static_cast<unsigned long long>(blockDim.x) + threadIdx.x;
+    const float tj = j < n ? __ldg(t + j) : 0.0f;
+    double acc = 0.0;
+    for (int c0 = 0; c0 < n_cond; c0 += kMixTile) {
+        const int m = min(kMixTile, n_cond - c0);
+        __syncthreads();
+        for (int i = threadIdx.x; i < m * row; i += blockDim.x) s_tile[i] = knots[static_cast<size_t>(c0) * row + i];
+        for (int i = threadIdx.x; i < m; i += blockDim.x) {
+            const float le = knots[static_cast<size_t>(c0 + i) * row + L * 3 * (K + 1) + 2];
+            s_w[i] = w ? w[c0 + i] : expf(le);
+            s_off[i] = off ? off[c0 + i] : 0.0f;
+        }
+        __syncthreads();
+        if (j < n) {
+            for (int c = 0; c < m; ++c) {
+                const float* o = s_tile + c * row;
+                float cur = tj - s_off[c];
+                for (int li = L - 1; li >= 0; --li) {
+                    const float* xp = o + li * 3 * (K + 1);
+                    float x, ld;
+                    inv_spline_fast<K>(xp, xp + K + 1, xp + 2 * (K + 1), cur, x, ld);
+                    cur = x;
+                }
+                const float u = (cur - o[L * 3 * (K + 1)]) * __fdividef(1.0f, o[L * 3 * (K + 1) + 1]);
+                acc += static_cast<double>(s_w[c]) * static_cast<double>(normcdff(u));
+            }
+        }
+    }
+    if (j < n) {
+        const double tot = *total;
+        out[j] = tot > 0.0 ? acc / tot : 0.0;
+    }
+}
+
 // ------------------------------------------------------------ sampling
 // rqs_univariate (rq_spline_flow.jl:262-324) on constrained knots: the
 // forward spline, linear outside the range
@@ -1576,6 +1646,72 @@ ntp_status ntp_flow_evaluate_grid(ntp_flow* f, const float* cond, int32_t n_cond
     };
     const ntp_status s2 = run();
     if (stage) cudaFree(stage);
+    return s2;
+}
+
+ntp_status ntp_flow_mixture_cdf(ntp_flow* f, const float* cond, int32_t n_cond, const float* weight,
+                                const float* offset, const float* times, uint64_t n_times, double* cdf,
+                                int32_t on_device) {
+    if (!f || !cond || n_cond <= 0) return NTP_ERR_INVALID;
+    if (n_times > 0 && (!times || !cdf)) return NTP_ERR_INVALID;
+    F_OK(ntp_flow_evaluate(f, cond, n_cond, nullptr, nullptr, 0, nullptr, nullptr, on_device));
+    if (n_times == 0) return NTP_OK;
+    cudaStream_t st = f->stream;
+    // device copies of host inputs, the output and the weight total
+    const size_t nc = static_cast<size_t>(n_cond);
+    const size_t bytes = sizeof(double) * (1 + (on_device ? 0 : n_times)) +
+                         (on_device ? 0 : sizeof(float) * (n_times + (weight ? nc : 0) + (offset ? nc : 0)));
+    void* stage = nullptr;
+    F_CUDA(f, cudaMalloc(&stage, bytes));
+    double* d_total = static_cast<double*>(stage);
+    double* d_out = on_device ? cdf : d_total + 1;
+    float* fl = reinterpret_cast<float*>(on_device ? d_total + 1 : d_out + n_times);
+    const float* d_t = times;
+    const float* d_w = weight;
+    const float* d_off = offset;
+    auto run = [&]() -> ntp_status {
+        if (!on_device) {
+            F_CUDA(f, cudaMemcpyAsync(fl, times, sizeof(float) * n_times, cudaMemcpyHostToDevice, st));
+            d_t = fl;
+            float* nxt = fl + n_times;
+            if (weight) {
+                F_CUDA(f, cudaMemcpyAsync(nxt, weight, sizeof(float) * nc, cudaMemcpyHostToDevice, st));
+                d_w = nxt;
+                nxt += nc;
+            }
+            if (offset) {
+                F_CUDA(f, cudaMemcpyAsync(nxt, offset, sizeof(float) * nc, cudaMemcpyHostToDevice, st));
+                d_off = nxt;
+            }
+        }
+        const int row = ntp::knot_row(f->L, f->K);
+        const size_t smem = sizeof(float) * (ntp::kMixTile * (row + 2));
+        const unsigned long long blocks = (n_times + 255) / 256;
+        if (blocks > 0x7fffffffull) {
+            f->err = "ntp_flow_mixture_cdf: too many times";
+            return NTP_ERR_INVALID;
+        }
+        cudaError_t e = cudaSuccess;
+        with_bins(f->K, [&](auto kc) {
+            constexpr int K = decltype(kc)::value;
+            ntp::mixture_total_kernel<<<1, 1024, 0, st>>>(f->knots, f->L, K, n_cond, d_w, d_total);
+            e = cudaGetLastError();
+            if (e == cudaSuccess)
+                e = cudaFuncSetAttribute(ntp::mixture_cdf_kernel<K>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         static_cast<int>(smem));
+            if (e == cudaSuccess) {
+                ntp::mixture_cdf_kernel<K><<<static_cast<unsigned>(blocks), 256, smem, st>>>(
+                    f->knots, f->L, n_cond, d_w, d_off, d_t, n_times, d_total, d_out);
+                e = cudaGetLastError();
+            }
+        });
+        if (e != cudaSuccess) return ferr(f, e, "ntp_flow_mixture_cdf");
+        if (!on_device) F_CUDA(f, cudaMemcpyAsync(cdf, d_out, sizeof(double) * n_times, cudaMemcpyDeviceToHost, st));
+        F_CUDA(f, cudaStreamSynchronize(st));
+        return NTP_OK;
+    };
+    const ntp_status s2 = run();
+    cudaFree(stage);
     return s2;
 }
 

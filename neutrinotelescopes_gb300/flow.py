@@ -295,6 +295,33 @@ class RQNormFlow:
                                                    le.ctypes.data if le is not None else None, 0))
         return (out, le) if log_expec else out
 
+    def mixture_cdf(self, cond, times, offsets=None, weights=None):
+        """The pooled CDF sum_c w_c F(t - offset_c | cond_c) / sum_c w_c at
+        each time (w = the conditions' expected counts unless given): an
+        event's predicted hit-time distribution from its PMTs' conditions and
+        geometric times.  CUDA tensors in, a float64 CUDA tensor out; or
+        numpy in and out."""
+        dev = _is_device(cond)
+        n_cond = int(cond.shape[0])
+        if dev:
+            import torch
+            n = int(times.numel())
+            out = torch.empty(n, dtype=torch.float64, device=times.device)
+            ptr = (lambda a: a.data_ptr() if a is not None else None)
+            self._check(self.lib.ntp_flow_mixture_cdf(self._h, cond.data_ptr(), n_cond, ptr(weights), ptr(offsets),
+                                                      times.data_ptr(), n, out.data_ptr(), 1))
+            return out
+        cond = _f32(cond)
+        times = _f32(times)
+        w = None if weights is None else _f32(weights, n_cond)
+        o = None if offsets is None else _f32(offsets, n_cond)
+        out = np.empty(times.size, np.float64)
+        self._check(self.lib.ntp_flow_mixture_cdf(self._h, cond.ctypes.data, n_cond,
+                                                  w.ctypes.data if w is not None else None,
+                                                  o.ctypes.data if o is not None else None, times.ctypes.data,
+                                                  times.size, out.ctypes.data, 0))
+        return out
+
     def logpdf_grid(self, cond, times, *, log_expec: bool = False):
         """log p(times[j] | cond[c]) as an [n_cond x n_times] array (the
         reference's per-module evaluation on a time grid)."""

@@ -18,6 +18,7 @@ measures in ``compare``.
 from __future__ import annotations
 
 import ctypes as C
+import dataclasses
 import math
 from dataclasses import dataclass
 
@@ -44,10 +45,15 @@ class HybridSimulator:
 
     def __init__(self, setup: PhotonPropSetup, flow: RQNormFlow, *, d_range=(1.0, 200.0),
                  log10_energy_range=(2.0, 6.0), seed: int = 0, ks_check_every: int = 0,
-                 ks_threshold: float = 0.02):
+                 ks_threshold: float = 0.02, ks_min_hits: int = 20_000, ks_max_photons: float = 2e10):
         """ks_check_every > 0: every that many flow-served events one is also
-        simulated with plain MC and the two hit-time samples compared (KS,
-        pooled over the event); a KS above ks_threshold hands every later
+        simulated with plain MC (``ks_check``): the one-sample
+        Kolmogorov-Smirnov distance of the MC hit times from the flow's
+        predicted hit-time distribution of the event.  The MC run is
+        oversampled towards ks_min_hits hits (at most ks_max_photons photons)
+        so that its own noise stays below the threshold; a check with enough
+        hits for a decision (a perfect surrogate below the threshold at 95 %
+        confidence) and a distance above ks_threshold hands every later
         event to plain MC."""
         self.setup = setup
         self.flow = flow
@@ -56,8 +62,10 @@ class HybridSimulator:
         self.seed = int(seed)
         self.ks_check_every = int(ks_check_every)
         self.ks_threshold = float(ks_threshold)
+        self.ks_min_hits = int(ks_min_hits)
+        self.ks_max_photons = float(ks_max_photons)
         self.fallback = False
-        self.checks: list[tuple[int, float]] = []
+        self.checks: list[tuple[int, float, int]] = []   # (event id, KS distance, MC hits)
         self._served = 0
         self.lib, self.ctx = setup.context()
         self.n800 = float(np.float32(np.asarray(setup.medium.refractive_index(np.array([800.0])))[0]))
@@ -124,12 +132,50 @@ class HybridSimulator:
             elif self.ks_check_every > 0:
                 self._served += 1
                 if self._served % self.ks_check_every == 0:
-                    mc = self.mc_event(ids[i], srcs[i])
-                    ks = ks_statistic(mc.time, out[i].time.cpu().numpy())
-                    self.checks.append((ids[i], ks))
-                    if not (ks <= self.ks_threshold):
+                    ks, n_mc = self.ks_check(ids[i], srcs[i], float(le[i]))
+                    self.checks.append((ids[i], ks, n_mc))
+                    decisive = n_mc >= (1.36 / self.ks_threshold) ** 2
+                    if decisive and not (ks <= self.ks_threshold):
                         self.fallback = True
         return out
+
+    def ks_check(self, event_id: int, source, log10_energy: float) -> tuple[float, int]:
+        """One-sample KS distance of plain-MC hit times (modules in the
+        surrogate's domain only) from the flow's predicted hit-time CDF of
+        the event (``RQNormFlow.mixture_cdf`` over its PMTs, weighted by
+        their expected counts, offset by geometric and event time), and the
+        number of MC hits.  The MC run takes k times the source's photons, k
+        chosen from the flow's expected hits to reach ks_min_hits, and once
+        more from the hits that run gave when it fell short (at most
+        ks_max_photons photons)."""
+        import torch
+        cond, _, tgeo, tgt, _, _, _ = self.conditions([source], [log10_energy], [event_id])
+        if cond.shape[0] == 0:
+            return float("nan"), 0
+        idx = torch.zeros(1, dtype=torch.int32, device=cond.device)
+        _, le = self.flow.logpdf(cond, idx, torch.zeros(1, dtype=torch.float32, device=cond.device), log_expec=True)
+        expected = float(torch.exp(le.double()).sum().item())
+        k_max = max(1, int(self.ks_max_photons // max(int(source.photons), 1)))
+        k = min(max(1, math.ceil(self.ks_min_hits / max(expected, 1e-9))), k_max)
+        domain = np.unique(tgt.cpu().numpy())
+        for attempt in range(2):
+            truth = mc_truth(self.setup, dataclasses.replace(source, photons=int(source.photons) * k),
+                             seed=self.seed + 0x4B53 + int(event_id) + attempt)
+            keep = np.isin(truth["target"], domain)
+            n_got = int(keep.sum())
+            k_next = min(max(1, math.ceil(k * self.ks_min_hits / max(n_got, 1))), k_max)
+            if n_got >= self.ks_min_hits or k_next <= k:
+                break
+            k = k_next
+        t = np.sort(truth["time"][keep])
+        if t.size == 0:
+            return float("nan"), 0
+        off = tgeo + float(source.time)
+        F = self.flow.mixture_cdf(cond, torch.as_tensor(t.astype(np.float32), device=cond.device), off)
+        F = F.cpu().numpy()
+        n = t.size
+        i = np.arange(1, n + 1)
+        return float(max(np.max(i / n - F), np.max(F - (i - 1) / n))), int(n)
 
     def serve(self, arrivals, *, max_batch: int = 64) -> list[tuple[int, str, float]]:
         """Real-time replay: events (arrival time in s, event_id, source,
@@ -200,8 +246,11 @@ def ks_statistic(a: np.ndarray, b: np.ndarray) -> float:
 def compare(sim: HybridSimulator, source, log10_energy: float, event_id: int, *, seed: int = 0,
             min_hits: int = 100) -> dict:
     """Surrogate against plain MC for one event: per-module expected hits
-    (flow count head vs sum of MC weights) and arrival times (KS per module
-    with at least min_hits hits in both, and pooled over the event)."""
+    (flow count head vs sum of MC weights) and arrival times (two-sample KS
+    per module with at least min_hits hits in both, and pooled over the
+    event), plus the one-sample KS of an oversampled MC run against the
+    flow's predicted hit-time distribution (``HybridSimulator.ks_check``,
+    free of the flow sample's noise)."""
     import torch
     truth = mc_truth(sim.setup, source, seed=seed)
     cond, key, tgeo, tgt, pmt, first, close = sim.conditions([source], [log10_energy], [event_id])
@@ -227,9 +276,11 @@ def compare(sim: HybridSimulator, source, log10_energy: float, event_id: int, *,
         b = ft[fk == k]
         if a.size >= min_hits and b.size >= min_hits:
             ks_mod.append(ks_statistic(a, b))
+    ks_pred, n_pred = sim.ks_check(event_id, source, log10_energy)
     return {"modules": len(rel), "expected_rel_err": np.array(rel), "ks_modules": np.array(ks_mod),
             "ks_pooled": ks_statistic(truth["time"], ft), "mc_hits": int(truth["time"].size),
-            "flow_hits": int(ft.size), "method": ev.method}
+            "flow_hits": int(ft.size), "method": ev.method,
+            "ks_predicted": ks_pred, "ks_predicted_mc_hits": n_pred}
 
 
 def hybrid_events(n: int, setup: PhotonPropSetup, *, seed: int = 4, log10_energy=(2.0, 6.0),

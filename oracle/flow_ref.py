@@ -150,6 +150,20 @@ def flow_logpdf(y, raw, n_layers: int, r0: float, r1: float, K: int | None = Non
     return normal + ldsum
 
 
+def flow_cdf(y, raw, n_layers: int, r0: float, r1: float, K: int):
+    """P(T <= y) for raw outputs: the base normal's CDF of the standardised
+    inverse-transformed time (every layer and the affine map increase)."""
+    L = n_layers
+    NP = 3 * K + 1
+    cur = y
+    for li in range(L - 1, -1, -1):
+        xp, yp, d = constrain_spline_params(raw[:, li * NP:(li + 1) * NP], r0, r1)
+        cur, _ = inv_rqs_univariate(xp, yp, d, cur)
+    shift = raw[:, L * NP]
+    scale = torch.sigmoid(torch.clamp(raw[:, L * NP + 1], -SCALE_CLAMP, SCALE_CLAMP)) * 100.0
+    return 0.5 * torch.erfc(-((cur - shift) / scale) / math.sqrt(2.0))
+
+
 def head_loss(raw, tres, nhits, has_time, L: int, K: int, r0: float, r1: float):
     """Batch-mean loss of raw outputs [B x (L(3K+1)+3)] (log expectation last)."""
     NP = 3 * K + 1

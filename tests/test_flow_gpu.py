@@ -233,6 +233,35 @@ def test_evaluate_matches_oracle_on_the_same_parameters(L, K, r0, r1):
     assert ll == pytest.approx(want, rel=1e-4)
 
 
+@pytest.mark.parametrize("L,K,r0,r1", CASES)
+def test_mixture_cdf_matches_oracle(L, K, r0, r1):
+    """The pooled CDF of 70 conditions with offsets, weighted by their
+    expected counts and by given weights, against the oracle's CDFs (float64)
+    of the same raw parameters; monotone in time, 0 and 1 far out."""
+    rng = np.random.default_rng(41)
+    n_cond, n_t = 70, 3000
+    cond = rng.uniform(-1, 1, (n_cond, 5)).astype(np.float32)
+    off = rng.uniform(0.0, 400.0, n_cond).astype(np.float32)
+    t = np.sort(rng.uniform(r0 - 50.0, r1 + 500.0, n_t)).astype(np.float32)
+    w = rng.uniform(0.1, 3.0, n_cond).astype(np.float32)
+    with make(L, K, r0, r1) as fl:
+        P = fl.forward_params(cond)
+        F_le = fl.mixture_cdf(cond, t, off)
+        F_w = fl.mixture_cdf(cond, t, off, w)
+        dev = fl.mixture_cdf(torch.as_tensor(cond, device="cuda"), torch.as_tensor(t, device="cuda"),
+                             torch.as_tensor(off, device="cuda")).cpu().numpy()
+        ends = fl.mixture_cdf(cond, np.array([-1e6, 1e7], np.float32))
+    Pt = torch.as_tensor(np.repeat(P.astype(np.float64), n_t, axis=0))
+    y = torch.as_tensor((t[None, :].astype(np.float64) - off[:, None].astype(np.float64)).reshape(-1))
+    Fi = R.flow_cdf(y, Pt, L, r0, r1, K).numpy().reshape(n_cond, n_t)
+    lam = np.exp(P[:, -1].astype(np.float64))
+    np.testing.assert_allclose(F_le, (lam[:, None] * Fi).sum(0) / lam.sum(), atol=2e-4)
+    np.testing.assert_allclose(F_w, (w[:, None] * Fi).sum(0) / w.sum(), atol=2e-4)
+    np.testing.assert_array_equal(dev, F_le)
+    assert np.all(np.diff(F_le) >= -1e-6)
+    np.testing.assert_allclose(ends, [0.0, 1.0], atol=1e-6)
+
+
 def test_grid_evaluation_equals_tuples():
     L, K, r0, r1 = 5, 12, -20.0, 1500.0
     rng = np.random.default_rng(70)

@@ -123,3 +123,41 @@ def test_hybrid_domain_split():
     assert [o.method for o in out] == ["flow", "mc"]
     assert out[0].n_hits == int(out[0].time.numel())
     assert np.all(out[0].target.cpu().numpy() < 5) and np.all((out[0].pmt.cpu().numpy() >= 1))
+
+
+def test_sampled_hits_follow_the_predicted_cdf():
+    """The flow's sampled hit times of an event against its own predicted
+    hit-time CDF (mixture_cdf over the event's PMTs, weighted by their
+    expected counts, offset by the geometric times): one-sample KS at the
+    noise level of the sample (99 % bound 1.63 / sqrt(n))."""
+    setup = _setup()
+    ev = (5, _cascade((5.0, 3.0, 10.0), (0.0, 0.6, 0.8), e=300.0), 2.5)
+    with _flow(math.log(40.0)) as fl:
+        sim = HybridSimulator(setup, fl, seed=17)
+        out = sim.simulate([ev])[0]
+        cond, _, tgeo, _, _, _, _ = sim.conditions([ev[1]], [ev[2]], [ev[0]])
+        t = torch.sort(out.time.float())[0]
+        F = fl.mixture_cdf(cond, t.contiguous(), tgeo + float(ev[1].time)).cpu().numpy()
+    n = F.size
+    assert out.method == "flow" and n > 2000
+    i = np.arange(1, n + 1)
+    ks = max(np.max(i / n - F), np.max(F - (i - 1) / n))
+    assert ks < 1.63 / math.sqrt(n), (ks, n)
+
+
+def test_ks_check_hands_later_events_to_mc():
+    """A surrogate far from the MC (an untrained flow) fails its first
+    decisive check: the check's MC run is oversampled towards ks_min_hits
+    (here up to the photon cap, rescaled from the hits of a first run), and
+    every later event goes to plain MC."""
+    setup = _setup()
+    events = [(i, _cascade((5.0, 3.0, 10.0 + i), (0.0, 0.0, 1.0), e=200.0), 2.3) for i in range(3)]
+    with _flow(math.log(3.0)) as fl:
+        sim = HybridSimulator(setup, fl, ks_check_every=1, ks_threshold=0.1, ks_min_hits=100_000,
+                              ks_max_photons=2e9)
+        first = sim.simulate(events[:1])
+        assert first[0].method == "flow" and len(sim.checks) == 1
+        _, ks, n_mc = sim.checks[0]
+        assert n_mc >= (1.36 / 0.1) ** 2 and ks > 0.1 and sim.fallback
+        later = sim.simulate(events[1:])
+    assert [o.method for o in later] == ["mc", "mc"]
