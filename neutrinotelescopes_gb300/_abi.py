@@ -6,6 +6,7 @@ every call raises.  There is no CPU fallback.
 from __future__ import annotations
 
 import ctypes as C
+import os
 import threading
 from pathlib import Path
 
@@ -362,12 +363,14 @@ def _declare(lib: C.CDLL) -> None:
 
 
 def load_library(path: Path | str | None = None) -> C.CDLL:
-    """Loads libntp.so (building nothing); raises if it is absent."""
+    """Loads libntp.so (building nothing); raises if it is absent.  The
+    NTP_LIBRARY environment variable, when set, names the library to load
+    instead of the in-tree build."""
     global _lib
     with _lock:
         if _lib is not None and path is None:
             return _lib
-        p = Path(path) if path is not None else LIB_PATH
+        p = Path(path) if path is not None else Path(os.environ.get("NTP_LIBRARY") or LIB_PATH)
         if not p.exists():
             raise RuntimeError(
                 f"{p} is missing: build the CUDA library first "

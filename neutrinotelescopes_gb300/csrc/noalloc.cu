@@ -239,7 +239,7 @@ extern "C" ntp_status ntp_propagate_noalloc(const ntp_medium_desc* m, const ntp_
     p.max_steps = o.max_steps;
     p.hit_policy = o.hit_policy;
     p.exact_pole = (o.flags & NTP_FLAG_EXACT_POLE_ROTATION) ? 1 : 0;
-    p.key = make_uint2(static_cast<uint32_t>(seed), static_cast<uint32_t>(seed >> 32));
+    ntp::set_key(p, seed);
     p.hits = hits;
     p.capacity = capacity;
     p.counters = d_counters;

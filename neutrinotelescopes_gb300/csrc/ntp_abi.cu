@@ -618,7 +618,7 @@ ntp_status ntp_propagate(ntp_ctx* ctx, const ntp_source* sources, int32_t n_sour
     p.max_steps = o.max_steps;
     p.hit_policy = o.hit_policy;
     p.exact_pole = (o.flags & NTP_FLAG_EXACT_POLE_ROTATION) ? 1 : 0;
-    p.key = make_uint2(static_cast<uint32_t>(seed), static_cast<uint32_t>(seed >> 32));
+    ntp::set_key(p, seed);
     p.hits = d_hits;
     p.capacity = capacity;
     p.counters = ctx->d_counters;

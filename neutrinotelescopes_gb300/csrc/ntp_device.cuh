@@ -44,6 +44,20 @@ __device__ __forceinline__ uint4 philox4x32_10(uint4 c, uint2 k) {
     return c;
 }
 
+// The same generator with the round keys precomputed: rk[2r], rk[2r + 1] =
+// key + r (0x9E3779B9, 0xBB67AE85).  With rk in a kernel's parameters each
+// round's key is an operand of the XOR rather than two additions.
+__device__ __forceinline__ uint4 philox4x32_10_rk(uint4 c, const uint32_t (&rk)[20]) {
+#pragma unroll
+    for (int r = 0; r < 10; ++r) {
+        const unsigned long long p0 = static_cast<unsigned long long>(0xD2511F53u) * c.x;
+        const unsigned long long p1 = static_cast<unsigned long long>(0xCD9E8D57u) * c.z;
+        c = make_uint4(static_cast<uint32_t>(p1 >> 32) ^ c.y ^ rk[2 * r], static_cast<uint32_t>(p1),
+                       static_cast<uint32_t>(p0 >> 32) ^ c.w ^ rk[2 * r + 1], static_cast<uint32_t>(p0));
+    }
+    return c;
+}
+
 // Top 23 bits plus one half, times 2^-23: uniform on the open interval (0, 1),
 // exact in float; 1 - u01(w) is exact too.
 __device__ __forceinline__ float u01(uint32_t w) {

@@ -72,6 +72,10 @@ struct PropParams {
     int hit_policy;
     int exact_pole;
     uint2 key;
+    // Philox round keys: rk[2r], rk[2r + 1] = key + r (0x9E3779B9, 0xBB67AE85)
+    // for rounds r = 0..9, precomputed on the host so that each round reads
+    // them as kernel-parameter operands (set by set_key)
+    uint32_t rk[20];
 
     // Philox stream word per source (nullptr: the source index).  The serving
     // loop passes event ids, so an event draws the same photons whatever
@@ -91,6 +95,16 @@ struct PropParams {
     unsigned long long chunk;             // photons a warp claims at once
     int refill_min;                       // idle lanes a warp gathers before it initialises new photons
 };
+
+// The Philox key of a launch (low and high 32 bits of the seed) and its
+// round keys.
+inline void set_key(PropParams& p, uint64_t seed) {
+    p.key = make_uint2(static_cast<uint32_t>(seed), static_cast<uint32_t>(seed >> 32));
+    for (uint32_t r = 0; r < 10; ++r) {
+        p.rk[2 * r] = p.key.x + r * 0x9E3779B9u;
+        p.rk[2 * r + 1] = p.key.y + r * 0xBB67AE85u;
+    }
+}
 
 size_t prop_smem_bytes(const PropParams& p);
 cudaError_t launch_propagate(const PropParams& p, int grid, cudaStream_t stream);

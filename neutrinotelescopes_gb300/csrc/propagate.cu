@@ -46,12 +46,12 @@ __device__ __forceinline__ int source_of(const unsigned long long* prefix, int n
 
 // rand_gamma(shape, scale), utils.jl:267-294 (Marsaglia-Tsang, shape > 1),
 // the normal from Box-Muller on Philox words; at most kGammaAttempts tries.
-__device__ __forceinline__ float rand_gamma(float shape, float scale, uint4 ctr, uint2 key) {
+__device__ __forceinline__ float rand_gamma(float shape, float scale, uint4 ctr, const uint32_t (&rk)[20]) {
     const float d = shape - (1.0f / 3.0f);
     const float c = rsqrtf(9.0f * d);
     for (int k = 0; k < kGammaAttempts; ++k) {
         ctr.x = kDrawGamma0 + static_cast<uint32_t>(k);
-        const uint4 r = philox4x32_10(ctr, key);
+        const uint4 r = philox4x32_10_rk(ctr, rk);
         float s, cs;
         sincos_2pi(u01(r.y), &s, &cs);
         const float x = fast_sqrt(-2.0f * __logf(u01(r.x))) * cs;
@@ -222,7 +222,7 @@ __device__ __forceinline__ void init_photon(Photon& ph, const ntp_source* __rest
     ph.pk_lo = static_cast<uint32_t>(pk);
     ph.pk_hi = static_cast<uint32_t>(pk >> 32);
     const uint4 base = make_uint4(kDrawInitA, ph.pk_lo, ph.pk_hi, ph.src);
-    const uint4 A = philox4x32_10(base, p.key);
+    const uint4 A = philox4x32_10_rk(base, p.rk);
 
     const int kind = __ldg(&src->kind);
     ph.wl = sample_wavelength(spec, u01(A.x));
@@ -256,7 +256,7 @@ __device__ __forceinline__ void init_photon(Photon& ph, const ntp_source* __rest
     case NTP_SRC_EXTENDED_CHERENKOV: {  // :164-176
         const float b = __ldg(&src->long_b);
         const float long_pos =
-            rand_gamma(__ldg(&src->long_a), 1.0f / b, base, p.key) * __ldg(&src->long_lrad);
+            rand_gamma(__ldg(&src->long_a), 1.0f / b, base, p.rk) * __ldg(&src->long_lrad);
         ph.pos = V3{fmaf(long_pos, sdir.x, ph.pos.x), fmaf(long_pos, sdir.y, ph.pos.y),
                     fmaf(long_pos, sdir.z, ph.pos.z)};
         ph.time = fmaf(long_pos, kInvCVac, ph.time);
@@ -284,7 +284,7 @@ __device__ __forceinline__ void init_photon(Photon& ph, const ntp_source* __rest
         V3 d{cp * sin_c, sp * sin_c, cos_c};
         // track smearing, sample_cherenkov_track_direction utils.jl:249-260:
         // 1 - cos = (-log(1 - u I)/b)^(1/a), a = 0.39, b = 2.61
-        const uint4 B = philox4x32_10(make_uint4(kDrawInitB, ph.pk_lo, ph.pk_hi, ph.src), p.key);
+        const uint4 B = philox4x32_10_rk(make_uint4(kDrawInitB, ph.pk_lo, ph.pk_hi, ph.src), p.rk);
         const float I = 0.96729171f;  // 1 - exp(-2.61 * 2^0.39)
         const float base = -log1pf(-u01(B.x) * I) * (1.0f / 2.61f);
         const float omc = fminf(exp2f(__log2f(base) * (1.0f / 0.39f)), 2.0f);
@@ -383,8 +383,8 @@ __global__ void __launch_bounds__(kPropBlock, kMinBlocks) propagate_kernel(const
         bool hit = false;
         int hit_t = -1;
         if (active) {
-            const uint4 r = philox4x32_10(
-                make_uint4(kDrawStep0 + static_cast<uint32_t>(ph.step), ph.pk_lo, ph.pk_hi, ph.src), p.key);
+            const uint4 r = philox4x32_10_rk(
+                make_uint4(kDrawStep0 + static_cast<uint32_t>(ph.step), ph.pk_lo, ph.pk_hi, ph.src), p.rk);
             const float step = -__logf(u01(r.x)) * ph.sca_len;
 
             // check_intersection over the targets, photon_prop_cuda.jl:233-271, :460-468

@@ -349,7 +349,7 @@ ntp_status ntp_server_create(ntp_ctx* ctx, const ntp_server_config* cfg, ntp_ser
         s->world.columns = nullptr;
         s->world.cell_start = nullptr;
     }
-    s->world.key = make_uint2(static_cast<uint32_t>(cfg->seed), static_cast<uint32_t>(cfg->seed >> 32));
+    ntp::set_key(s->world, cfg->seed);
     s->world.refill_min = 8;
     s->n_max = cfg->max_events_per_batch;
     const size_t N = static_cast<size_t>(s->n_max);
