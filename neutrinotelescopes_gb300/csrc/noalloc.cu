@@ -235,7 +235,7 @@ extern "C" ntp_status ntp_propagate_noalloc(const ntp_medium_desc* m, const ntp_
     p.spec_p0 = p0;
     p.spec_p1 = p1;
     p.hg_g = m->hg_g;
-    p.rayleigh_fraction = m->rayleigh_fraction;
+    ntp::set_rayleigh(p, m->rayleigh_fraction);
     p.max_steps = o.max_steps;
     p.hit_policy = o.hit_policy;
     p.exact_pole = (o.flags & NTP_FLAG_EXACT_POLE_ROTATION) ? 1 : 0;

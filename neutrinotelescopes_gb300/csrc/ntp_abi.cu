@@ -170,7 +170,7 @@ bool fill_world_params(const ntp_ctx* ctx, PropParams& p) {
     p.spec_p0 = ctx->spec_p0;
     p.spec_p1 = ctx->spec_p1;
     p.hg_g = ctx->hg_g;
-    p.rayleigh_fraction = ctx->f_ray;
+    ntp::set_rayleigh(p, ctx->f_ray);
     return true;
 }
 

@@ -59,9 +59,12 @@ __device__ __forceinline__ uint4 philox4x32_10_rk(uint4 c, const uint32_t (&rk)[
 }
 
 // Top 23 bits plus one half, times 2^-23: uniform on the open interval (0, 1),
-// exact in float; 1 - u01(w) is exact too.
+// exact in float; 1 - u01(w) is exact too.  Formed from the bit pattern: the
+// float 1.m (m the top 23 bits) minus 1 - 2^-24 is exact (both lie within a
+// factor 2 of each other) and equals (m + 1/2) 2^-23, with no
+// integer-to-float conversion.
 __device__ __forceinline__ float u01(uint32_t w) {
-    return (static_cast<float>(w >> 9) + 0.5f) * (1.0f / 8388608.0f);
+    return __uint_as_float((w >> 9) | 0x3F800000u) - 0.999999940395355224609375f;
 }
 
 // 53 random bits from two Philox words: a double on the open interval (0, 1).
@@ -180,8 +183,21 @@ __device__ __forceinline__ float sample_wavelength(const SpectrumView& s, float 
 // below the 1e-4 per-photon agreement the propagation is held to.
 __device__ __forceinline__ float fast_rcp(float x) { return __fdividef(1.0f, x); }
 
-// sqrt(x) for x >= 0 from the reciprocal square root (exact 0 at 0)
-__device__ __forceinline__ float fast_sqrt(float x) { return x > 0.0f ? x * rsqrtf(x) : 0.0f; }
+// sqrt(max(x, 0)) by the approximate square-root instruction (relative error
+// within 2^-23 over the normal range; exact 0 at 0)
+__device__ __forceinline__ float fast_sqrt(float x) {
+    float r;
+    asm("sqrt.approx.f32 %0, %1;" : "=f"(r) : "f"(fmaxf(x, 0.0f)));
+    return r;
+}
+
+// 2^x by the approximate base-2 exponential instruction (relative error
+// about 2^-22; results below the normal range flush to 0)
+__device__ __forceinline__ float fast_exp2(float x) {
+    float r;
+    asm("ex2.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(x));
+    return r;
+}
 
 // (sin, cos)(2 pi u) for u in (0, 1): the hardware sine / cosine on the
 // argument moved to [-pi, pi), where their absolute error is below 2^-21.
@@ -209,7 +225,7 @@ __device__ __forceinline__ float hg_one_minus_cos(float g, float one_m_g, float 
 __device__ __forceinline__ float rayleigh_cos(float u) {
     const float q = fmaf(4.0f, u, -2.0f);
     const float x = fabsf(q) + fast_sqrt(fmaf(q, q, 1.0f));
-    const float A = exp2f(__log2f(x) * (1.0f / 3.0f));
+    const float A = fast_exp2(__log2f(x) * (1.0f / 3.0f));
     const float mu = A - fast_rcp(A);
     return copysignf(mu, q);
 }

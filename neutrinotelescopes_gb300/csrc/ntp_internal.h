@@ -2,6 +2,7 @@
 // kernels of libntp.so.  Not part of the public interface.
 #pragma once
 
+#include <cmath>
 #include <cstdint>
 #include <string>
 #include <vector>
@@ -68,6 +69,11 @@ struct PropParams {
 
     float hg_g;
     float rayleigh_fraction;
+    // the Rayleigh branch as an integer test on the Philox word w:
+    // u01(w) < rayleigh_fraction exactly when w <= rayleigh_wmax (and
+    // rayleigh_on); set by set_rayleigh
+    uint32_t rayleigh_wmax;
+    int rayleigh_on;
     int max_steps;
     int hit_policy;
     int exact_pole;
@@ -104,6 +110,18 @@ inline void set_key(PropParams& p, uint64_t seed) {
         p.rk[2 * r] = p.key.x + r * 0x9E3779B9u;
         p.rk[2 * r + 1] = p.key.y + r * 0xBB67AE85u;
     }
+}
+
+// The phase-function mixture: u01(w) = (m + 1/2) 2^-23 with m = w >> 9 is
+// below f for the first T = ceil(f 2^23 - 1/2) values of m (clamped to [0,
+// 2^23]), i.e. for w <= 512 T - 1.
+inline void set_rayleigh(PropParams& p, float f) {
+    p.rayleigh_fraction = f;
+    double t = std::ceil(static_cast<double>(f) * 8388608.0 - 0.5);
+    t = t < 0.0 ? 0.0 : (t > 8388608.0 ? 8388608.0 : t);
+    const uint64_t T = static_cast<uint64_t>(t);
+    p.rayleigh_on = T > 0 ? 1 : 0;
+    p.rayleigh_wmax = T > 0 ? static_cast<uint32_t>(T * 512u - 1u) : 0u;
 }
 
 size_t prop_smem_bytes(const PropParams& p);

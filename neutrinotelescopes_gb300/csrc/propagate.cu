@@ -26,7 +26,7 @@ namespace {
 
 struct Photon {
     V3 pos, dir, init_dir;
-    float time, wl, dist, sca_len, inv_vg;
+    float time, wl, dist, sca_len_ln2, inv_vg;  // sca_len_ln2: scattering length times ln 2
     uint32_t src;
     uint32_t pk_lo, pk_hi;  // photon index within its source
     int step;
@@ -294,7 +294,7 @@ __device__ __forceinline__ void init_photon(Photon& ph, const ntp_source* __rest
     }
     ph.init_dir = ph.dir;
     ph.dist = 0.0f;
-    ph.sca_len = med.z;
+    ph.sca_len_ln2 = med.z * 0.6931471805599453f;
     ph.inv_vg = fast_rcp(med.y);
     ph.step = 0;
 }
@@ -385,7 +385,8 @@ __global__ void __launch_bounds__(kPropBlock, kMinBlocks) propagate_kernel(const
         if (active) {
             const uint4 r = philox4x32_10_rk(
                 make_uint4(kDrawStep0 + static_cast<uint32_t>(ph.step), ph.pk_lo, ph.pk_hi, ph.src), p.rk);
-            const float step = -__logf(u01(r.x)) * ph.sca_len;
+            // -ln(u) lambda_sca as -log2(u) (lambda_sca ln 2)
+            const float step = -__log2f(u01(r.x)) * ph.sca_len_ln2;
 
             // check_intersection over the targets, photon_prop_cuda.jl:233-271, :460-468
             float hit_d = step;
@@ -424,9 +425,9 @@ __global__ void __launch_bounds__(kPropBlock, kMinBlocks) propagate_kernel(const
                 // computed and one selected, so lanes of a warp do not diverge.
                 const float eta = u01(r.y);
                 float omc = hg_one_minus_cos(g, one_m_g, one_m_g2, eta);
-                if (p.rayleigh_fraction > 0.0f) {
+                if (p.rayleigh_on) {
                     const float omr = 1.0f - rayleigh_cos(eta);
-                    omc = u01(r.w) < p.rayleigh_fraction ? omr : omc;
+                    omc = r.w <= p.rayleigh_wmax ? omr : omc;  // u01(r.w) < rayleigh_fraction
                 }
                 ph.dir = rot_from_ez(ph.dir, dir_from_omc(omc, u01(r.z)), p.exact_pole);
                 if (++ph.step >= p.max_steps) {
