@@ -191,6 +191,29 @@ __device__ __forceinline__ float fast_sqrt(float x) {
     return r;
 }
 
+// Approximate instructions with subnormal results and inputs flushed to 0,
+// for arguments known to be normal
+__device__ __forceinline__ float log2_ftz(float x) {
+    float r;
+    asm("lg2.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(x));
+    return r;
+}
+__device__ __forceinline__ float rcp_ftz(float x) {
+    float r;
+    asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(x));
+    return r;
+}
+__device__ __forceinline__ float sin_ftz(float x) {
+    float r;
+    asm("sin.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(x));
+    return r;
+}
+__device__ __forceinline__ float cos_ftz(float x) {
+    float r;
+    asm("cos.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(x));
+    return r;
+}
+
 // 2^x by the approximate base-2 exponential instruction (relative error
 // about 2^-22; results below the normal range flush to 0)
 __device__ __forceinline__ float fast_exp2(float x) {
@@ -203,8 +226,8 @@ __device__ __forceinline__ float fast_exp2(float x) {
 // argument moved to [-pi, pi), where their absolute error is below 2^-21.
 __device__ __forceinline__ void sincos_2pi(float u, float* s, float* c) {
     const float x = 6.283185307179586f * (u - 0.5f);
-    *s = -__sinf(x);
-    *c = -__cosf(x);
+    *s = -sin_ftz(x);
+    *c = -cos_ftz(x);
 }
 
 // One minus the Henyey-Greenstein cosine (cuda_hg_scattering_func,
@@ -213,7 +236,7 @@ __device__ __forceinline__ void sincos_2pi(float u, float* s, float* c) {
 // the second form keeps full relative precision for forward scatters.
 __device__ __forceinline__ float hg_one_minus_cos(float g, float one_m_g, float one_m_g2, float eta) {
     const float D = fmaf(g, fmaf(2.0f, eta, -1.0f), 1.0f);
-    const float invD = fast_rcp(D);
+    const float invD = rcp_ftz(D);
     const float t = one_m_g2 * invD;
     const float omc = one_m_g * (1.0f - eta) * (t + one_m_g) * invD;
     return fminf(fmaxf(omc, 0.0f), 2.0f);
@@ -225,8 +248,8 @@ __device__ __forceinline__ float hg_one_minus_cos(float g, float one_m_g, float 
 __device__ __forceinline__ float rayleigh_cos(float u) {
     const float q = fmaf(4.0f, u, -2.0f);
     const float x = fabsf(q) + fast_sqrt(fmaf(q, q, 1.0f));
-    const float A = fast_exp2(__log2f(x) * (1.0f / 3.0f));
-    const float mu = A - fast_rcp(A);
+    const float A = fast_exp2(log2_ftz(x) * (1.0f / 3.0f));
+    const float mu = A - rcp_ftz(A);
     return copysignf(mu, q);
 }
 

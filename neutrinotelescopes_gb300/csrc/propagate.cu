@@ -74,7 +74,7 @@ __device__ __forceinline__ bool sphere_hit(const float4 T, const V3 pos, const V
     const float pp = dx * dx + dy * dy + dz * dz;
     const float b = fmaf(a, a, T.w - pp);
     if (b >= 0.0f) {
-        d = -a - sqrtf(b);
+        d = -a - fast_sqrt(b);
         return d > 0.0f && d < step;
     }
     return false;
@@ -120,9 +120,9 @@ __device__ __forceinline__ void column_candidates(const Column& C, const int* __
             far = ex * ex + ey * ey > rc2;
         }
         if (far) return;
-        const float inv_dd = 1.0f / dd;
+        const float inv_dd = rcp_ftz(dd);  // dd > 1e-12
         const float ts = pd * inv_dd;
-        const float h = sqrtf(fmaxf(rc2 - cr * cr * inv_dd, 0.0f) * inv_dd);
+        const float h = fast_sqrt((rc2 - cr * cr * inv_dd) * inv_dd);
         t0 = fmaxf(ts - h, 0.0f);
         t1 = fminf(ts + h, step);
     } else if (px * px + py * py > rc2) {
@@ -133,7 +133,7 @@ __device__ __forceinline__ void column_candidates(const Column& C, const int* __
     if (zhi < C.z0 - C.r_cull || zlo > C.z_last + C.r_cull) return;
     int k0 = 0, k1 = C.count - 1;
     if (C.dz > 0.0f) {
-        const float inv = 1.0f / C.dz;
+        const float inv = rcp_ftz(C.dz);
         k0 = max(k0, static_cast<int>(floorf(fmaxf((zlo - C.z0) * inv, -1.0f))) - 1);
         k1 = min(k1, static_cast<int>(ceilf(fminf((zhi - C.z0) * inv, static_cast<float>(C.count)))) + 1);
     }
@@ -256,7 +256,7 @@ __device__ __forceinline__ void init_photon(Photon& ph, const ntp_source* __rest
     case NTP_SRC_EXTENDED_CHERENKOV: {  // :164-176
         const float b = __ldg(&src->long_b);
         const float long_pos =
-            rand_gamma(__ldg(&src->long_a), 1.0f / b, base, p.rk) * __ldg(&src->long_lrad);
+            rand_gamma(__ldg(&src->long_a), __frcp_rn(b), base, p.rk) * __ldg(&src->long_lrad);
         ph.pos = V3{fmaf(long_pos, sdir.x, ph.pos.x), fmaf(long_pos, sdir.y, ph.pos.y),
                     fmaf(long_pos, sdir.z, ph.pos.z)};
         ph.time = fmaf(long_pos, kInvCVac, ph.time);
@@ -287,7 +287,8 @@ __device__ __forceinline__ void init_photon(Photon& ph, const ntp_source* __rest
         const uint4 B = philox4x32_10_rk(make_uint4(kDrawInitB, ph.pk_lo, ph.pk_hi, ph.src), p.rk);
         const float I = 0.96729171f;  // 1 - exp(-2.61 * 2^0.39)
         const float base = -log1pf(-u01(B.x) * I) * (1.0f / 2.61f);
-        const float omc = fminf(exp2f(__log2f(base) * (1.0f / 0.39f)), 2.0f);
+        // base >= ~2e-8 (u01 >= 2^-24): base^(1/0.39) stays normal
+        const float omc = fminf(fast_exp2(log2_ftz(base) * (1.0f / 0.39f)), 2.0f);
         const V3 track = dir_from_omc(omc, u01(B.y));
         d = rot_from_ez(track, d, p.exact_pole);
         ph.dir = rot_from_ez(sdir, d, p.exact_pole);
@@ -386,7 +387,7 @@ __global__ void __launch_bounds__(kPropBlock, kMinBlocks) propagate_kernel(const
             const uint4 r = philox4x32_10_rk(
                 make_uint4(kDrawStep0 + static_cast<uint32_t>(ph.step), ph.pk_lo, ph.pk_hi, ph.src), p.rk);
             // -ln(u) lambda_sca as -log2(u) (lambda_sca ln 2)
-            const float step = -__log2f(u01(r.x)) * ph.sca_len_ln2;
+            const float step = -log2_ftz(u01(r.x)) * ph.sca_len_ln2;
 
             // check_intersection over the targets, photon_prop_cuda.jl:233-271, :460-468
             float hit_d = step;
