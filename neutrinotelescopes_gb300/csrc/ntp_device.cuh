@@ -108,6 +108,29 @@ __device__ __forceinline__ double poisson_draw(double lam, uint2 key, uint32_t l
     return floor(lam + 0.5);
 }
 
+// Approximate instructions with subnormal results and inputs flushed to 0,
+// for arguments known to be normal
+__device__ __forceinline__ float log2_ftz(float x) {
+    float r;
+    asm("lg2.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(x));
+    return r;
+}
+__device__ __forceinline__ float rcp_ftz(float x) {
+    float r;
+    asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(x));
+    return r;
+}
+__device__ __forceinline__ float sin_ftz(float x) {
+    float r;
+    asm("sin.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(x));
+    return r;
+}
+__device__ __forceinline__ float cos_ftz(float x) {
+    float r;
+    asm("cos.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(x));
+    return r;
+}
+
 struct V3 {
     float x, y, z;
 };
@@ -115,18 +138,21 @@ struct V3 {
 // rot_from_ez_fast, utils.jl:228-243: the rotation taking e_z to a, applied
 // to o.  At a = +-e_z the reference returns (o1, copysign(o2,a3),
 // copysign(o3,a3)); exact_pole switches to the true rotation there.
-// The reference tests |a3| == 1; here the pole is a1^2 + a2^2 == 0.  The two
-// agree for every exact +-e_z, but a scattered direction whose z component
-// rounds to 1.0f in single precision while x, y are not zero keeps its
-// transverse part here (the general formula stays bounded: a_i^2 fact <=
-// 1 - a3), as the same step in double precision does.
+// The reference tests |a3| == 1; here the pole is a1^2 + a2^2 below the
+// smallest normal float (a direction within 1e-19 of the axis, where the
+// two forms agree to that order).  The two agree for every exact +-e_z, but
+// a scattered direction whose z component rounds to 1.0f in single
+// precision while x, y are not tiny keeps its transverse part here (the
+// general formula stays bounded: a_i^2 fact <= 1 - a3), as the same step in
+// double precision does.
 __device__ __forceinline__ V3 rot_from_ez(V3 a, V3 o, bool exact_pole) {
     const float a1sq = a.x * a.x, a2sq = a.y * a.y;
-    if (a1sq + a2sq == 0.0f) {
+    const float t = a1sq + a2sq;
+    if (t < 1.17549435e-38f) {
         if (exact_pole) return V3{o.x, copysignf(1.0f, a.z) * o.y, copysignf(1.0f, a.z) * o.z};
         return V3{o.x, copysignf(o.y, a.z), copysignf(o.z, a.z)};
     }
-    const float fact = __fdividef(1.0f - a.z, a2sq + a1sq);
+    const float fact = (1.0f - a.z) * rcp_ftz(t);
     const float a1a2 = a.x * a.y;
     V3 r;
     r.x = fmaf(-a1sq, fact, 1.0f) * o.x - a1a2 * fact * o.y + a.x * o.z;
@@ -191,29 +217,6 @@ __device__ __forceinline__ float fast_sqrt(float x) {
     return r;
 }
 
-// Approximate instructions with subnormal results and inputs flushed to 0,
-// for arguments known to be normal
-__device__ __forceinline__ float log2_ftz(float x) {
-    float r;
-    asm("lg2.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(x));
-    return r;
-}
-__device__ __forceinline__ float rcp_ftz(float x) {
-    float r;
-    asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(x));
-    return r;
-}
-__device__ __forceinline__ float sin_ftz(float x) {
-    float r;
-    asm("sin.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(x));
-    return r;
-}
-__device__ __forceinline__ float cos_ftz(float x) {
-    float r;
-    asm("cos.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(x));
-    return r;
-}
-
 // 2^x by the approximate base-2 exponential instruction (relative error
 // about 2^-22; results below the normal range flush to 0)
 __device__ __forceinline__ float fast_exp2(float x) {
@@ -225,7 +228,7 @@ __device__ __forceinline__ float fast_exp2(float x) {
 // (sin, cos)(2 pi u) for u in (0, 1): the hardware sine / cosine on the
 // argument moved to [-pi, pi), where their absolute error is below 2^-21.
 __device__ __forceinline__ void sincos_2pi(float u, float* s, float* c) {
-    const float x = 6.283185307179586f * (u - 0.5f);
+    const float x = fmaf(u, 6.283185307179586f, -3.141592653589793f);
     *s = -sin_ftz(x);
     *c = -cos_ftz(x);
 }

@@ -353,33 +353,38 @@ __global__ void __launch_bounds__(kPropBlock, kMinBlocks) propagate_kernel(const
         // refill idle lanes in batches of at least refill_min (or when every
         // lane is idle), so the divergent initialisation runs for many lanes
         // at once instead of for one or two in almost every iteration
+        // (no lane idle, the common case, costs one vote and one branch)
         const unsigned idle = __ballot_sync(kFull, !active);
-        if (!exhausted && (idle == kFull || __popc(idle) >= p.refill_min)) {
-            unsigned long long avail = c_end - c_next;
-            if (avail == 0) {
-                unsigned long long base = 0;
-                if (lane == 0) base = atomicAdd(p.counters, p.chunk);
-                base = __shfl_sync(kFull, base, 0);
-                if (base >= p.total) {
-                    exhausted = true;
-                } else {
-                    c_next = base;
-                    c_end = min(base + p.chunk, p.total);
-                    avail = c_end - c_next;
+        if (idle) {
+            bool refilled = false;  // warp-uniform
+            if (!exhausted && (idle == kFull || __popc(idle) >= p.refill_min)) {
+                unsigned long long avail = c_end - c_next;
+                if (avail == 0) {
+                    unsigned long long base = 0;
+                    if (lane == 0) base = atomicAdd(p.counters, p.chunk);
+                    base = __shfl_sync(kFull, base, 0);
+                    if (base >= p.total) {
+                        exhausted = true;
+                    } else {
+                        c_next = base;
+                        c_end = min(base + p.chunk, p.total);
+                        avail = c_end - c_next;
+                    }
+                }
+                if (avail) {
+                    const unsigned long long take = min(static_cast<unsigned long long>(__popc(idle)), avail);
+                    const unsigned rank = __popc(idle & lt_mask);
+                    if (!active && rank < take) {
+                        const unsigned long long gid = c_next + rank;
+                        init_photon(ph, p.sources, p, spec, s_med, gid, source_of(p.prefix, p.n_src, gid));
+                        active = true;
+                    }
+                    c_next += take;
+                    refilled = true;
                 }
             }
-            if (avail) {
-                const unsigned long long take = min(static_cast<unsigned long long>(__popc(idle)), avail);
-                const unsigned rank = __popc(idle & lt_mask);
-                if (!active && rank < take) {
-                    const unsigned long long gid = c_next + rank;
-                    init_photon(ph, p.sources, p, spec, s_med, gid, source_of(p.prefix, p.n_src, gid));
-                    active = true;
-                }
-                c_next += take;
-            }
+            if (idle == kFull && !refilled) break;  // every lane idle and no photon left
         }
-        if (!__any_sync(kFull, active)) break;
 
         bool hit = false;
         int hit_t = -1;
