@@ -444,17 +444,23 @@ ntp_status ntp_flow_train_step(ntp_flow* flow, const float* cond, const float* t
 /* n_steps training steps on consecutive batches of B rows (rows i*B ..
    (i+1)*B - 1 form step i), one synchronisation for all of them; losses
    (host, n_steps, may be NULL) receives each step's loss (NaN for a skipped
-   step).  The training step itself is captured once as a CUDA graph and
-   replayed (NTP_FLOW_GRAPH=0 in the environment runs it eagerly). */
+   step).  count_weight (may be NULL = 1 for every row) multiplies each row's
+   Poisson count term: -(sum logpdf + sum c_i Poisson(n_i; exp(le_i))) / B;
+   with c = 1 / (rows of the PMT) every PMT's count enters once (the
+   reference's tables repeat it on each of the PMT's rows).  The training
+   step itself is captured once as a CUDA graph and replayed
+   (NTP_FLOW_GRAPH=0 in the environment runs it eagerly). */
 ntp_status ntp_flow_train_steps(ntp_flow* flow, const float* cond, const float* tres, const float* nhits,
-                                const int32_t* has_time, int32_t B, int32_t n_steps, int32_t on_device,
-                                int32_t update, double* losses);
+                                const int32_t* has_time, const float* count_weight, int32_t B, int32_t n_steps,
+                                int32_t on_device, int32_t update, double* losses);
 /* The conditioner's raw outputs for n conditions (host): params_out [n x n_outputs]. */
 ntp_status ntp_flow_forward(ntp_flow* flow, const float* cond, int32_t n, float* params_out);
 /* The loss and its gradient by the raw outputs, for given raw outputs
-   params [B x n_outputs] (host buffers; B <= batch_capacity). */
+   params [B x n_outputs] (host buffers; B <= batch_capacity; count_weight
+   as in ntp_flow_train_steps, may be NULL). */
 ntp_status ntp_flow_head(ntp_flow* flow, const float* params, const float* tres, const float* nhits,
-                         const int32_t* has_time, int32_t B, double* loss, float* grad_out);
+                         const int32_t* has_time, const float* count_weight, int32_t B, double* loss,
+                         float* grad_out);
 /* The model call (extended_cascade_model.jl:110-125): log p(t | cond) for
    n_tuples (condition index, time) pairs, and per condition the log
    expectation (log_expec may be NULL).  An index outside [0, n_cond) gives NaN. */

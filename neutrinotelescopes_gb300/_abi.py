@@ -332,10 +332,10 @@ def _declare(lib: C.CDLL) -> None:
     lib.ntp_flow_set_lr.argtypes = [vp, C.c_float]
     lib.ntp_flow_set_lr.restype = C.c_int
     lib.ntp_flow_train_step.argtypes = [vp, vp, vp, vp, vp, i32, i32, i32, C.POINTER(C.c_double)]
-    lib.ntp_flow_train_steps.argtypes = [vp, vp, vp, vp, vp, i32, i32, i32, i32, vp]
+    lib.ntp_flow_train_steps.argtypes = [vp, vp, vp, vp, vp, vp, i32, i32, i32, i32, vp]
     lib.ntp_flow_mixture_cdf.argtypes = [vp, vp, i32, vp, vp, vp, u64, vp, i32]
     lib.ntp_flow_forward.argtypes = [vp, vp, i32, vp]
-    lib.ntp_flow_head.argtypes = [vp, vp, vp, vp, vp, i32, C.POINTER(C.c_double), vp]
+    lib.ntp_flow_head.argtypes = [vp, vp, vp, vp, vp, vp, i32, C.POINTER(C.c_double), vp]
     lib.ntp_flow_evaluate.argtypes = [vp, vp, i32, vp, vp, u64, vp, vp, i32]
     lib.ntp_flow_sample.argtypes = [vp, vp, i32, vp, u64, vp, vp, vp, u64, C.POINTER(u64), i32]
     lib.ntp_flow_evaluate_grid.argtypes = [vp, vp, i32, vp, i32, vp, vp, i32]

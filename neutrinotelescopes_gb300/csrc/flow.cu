@@ -380,7 +380,7 @@ template <int K>
 __global__ void __launch_bounds__(32 * kMaxLayers) head_grad_kernel(
     const float* __restrict__ P, int ldp, int L, const float* __restrict__ y, const float* __restrict__ nhits,
     const int* __restrict__ has_y, int B, float r0, float r1, float clip, float count_w,
-    __nv_bfloat16* __restrict__ dp,
+    const float* __restrict__ count_w_rows, __nv_bfloat16* __restrict__ dp,
     __nv_bfloat16* __restrict__ dpt, float* __restrict__ gf, float* __restrict__ gbias, double* __restrict__ loss) {
     constexpr int NP = 3 * K + 1, NK = K + 1, KN = 3 * NK + 2 * K + NK;
     extern __shared__ float sm[];
@@ -429,7 +429,8 @@ __global__ void __launch_bounds__(32 * kMaxLayers) head_grad_kernel(
         const float le_raw = p[o_le], n = act ? nhits[b] : 0.0f;
         const float le = clamp_le(le_raw);
         const float lam = expf(le);
-        if (act) l -= count_w * (n * le - lam - lgammaf(n + 1.0f));
+        const float cw = act ? (count_w_rows ? count_w * count_w_rows[b] : count_w) : 0.0f;
+        if (act && cw != 0.0f) l -= cw * (n * le - lam - lgammaf(n + 1.0f));
         float a = 0.0f, g_shift = 0.0f, g_scale = 0.0f;
         if (timed) {
             float cur = y[b], ldsum = 0.0f;
@@ -455,7 +456,7 @@ __global__ void __launch_bounds__(32 * kMaxLayers) head_grad_kernel(
         s_s[lane * 4 + 0] = a;
         s_s[lane * 4 + 1] = g_shift;
         s_s[lane * 4 + 2] = g_scale;
-        s_s[lane * 4 + 3] = act && le_raw == le ? count_w * (lam - n) * inv_b : 0.0f;
+        s_s[lane * 4 + 3] = act && le_raw == le ? cw * (lam - n) * inv_b : 0.0f;
         l = warp_sum(l);
         if (lane == 0 && l != 0.0f) atomicAdd(loss, static_cast<double>(l) / B);
     }
@@ -936,6 +937,7 @@ struct ntp_flow {
     float* P = nullptr;
     float *cond = nullptr, *y = nullptr, *nh = nullptr;
     int* hy = nullptr;
+    float* cw = nullptr;  // per-row weights of the count term
     double* loss = nullptr;
     int* gemm_err = nullptr;
     int* skip = nullptr;     // set when a step's gradient is not finite
@@ -945,7 +947,7 @@ struct ntp_flow {
     // the training step captured as a CUDA graph (per batch size and update flag)
     bool use_graph = true;
     cudaGraphExec_t gexec = nullptr;
-    int g_B = 0, g_update = -1;
+    int g_B = 0, g_update = -1, g_rows_w = -1;
     // per-step losses and skip flags of a multi-step call (grown on demand)
     double* loss_hist = nullptr;
     int* skip_hist = nullptr;
@@ -1045,7 +1047,8 @@ ntp_status check_gemm(ntp_flow* f) {
 }
 
 // the head kernel on f->P for B samples (32 per block, one warp per layer)
-ntp_status launch_head(ntp_flow* f, const float* y, const float* nh, const int* hy, int B, float* gf, float* gbias) {
+ntp_status launch_head(ntp_flow* f, const float* y, const float* nh, const int* hy, const float* cwr, int B, float* gf,
+                       float* gbias) {
     const size_t smem = sizeof(float) * ntp::head_smem_floats(f->L, f->K, f->n_pad);
     cudaError_t e = cudaSuccess;
     with_bins(f->K, [&](auto kc) {
@@ -1057,7 +1060,7 @@ ntp_status launch_head(ntp_flow* f, const float* y, const float* nh, const int* 
                                      static_cast<int>(smem));
         if (e == cudaSuccess) {
             ntp::head_grad_kernel<K><<<(B + 31) / 32, 32 * f->L, smem, f->stream>>>(
-                f->P, f->n_pad, f->L, y, nh, hy, B, f->r0, f->r1, f->clip, f->count_w, f->dp, f->dpt, gf, gbias,
+                f->P, f->n_pad, f->L, y, nh, hy, B, f->r0, f->r1, f->clip, f->count_w, cwr, f->dp, f->dpt, gf, gbias,
                 f->loss);
             e = cudaGetLastError();
         }
@@ -1068,7 +1071,7 @@ ntp_status launch_head(ntp_flow* f, const float* y, const float* nh, const int* 
 
 void free_all(ntp_flow* f) {
     void* ps[] = {f->theta, f->m, f->v, f->grad, f->x, f->xt, f->dp, f->dpt, f->P, f->cond, f->y, f->nh, f->hy,
-                  f->loss, f->gemm_err, f->skip, f->step_dev, f->lr_dev, f->knots, f->loss_hist, f->skip_hist};
+                  f->loss, f->gemm_err, f->skip, f->step_dev, f->lr_dev, f->knots, f->loss_hist, f->skip_hist, f->cw};
     for (void* p : ps)
         if (p) cudaFree(p);
     for (int l = 0; l < 4; ++l) {
@@ -1085,7 +1088,7 @@ void free_all(ntp_flow* f) {
 
 // Every device operation of one training step on the staged batch (f->cond,
 // f->y, f->nh, f->hy): no host synchronisation, so it can be captured.
-ntp_status record_step(ntp_flow* f, int B, bool update) {
+ntp_status record_step(ntp_flow* f, int B, bool update, bool rows_w) {
     cudaStream_t st = f->stream;
     F_CUDA(f, cudaMemsetAsync(f->gemm_err, 0, sizeof(int), st));
     F_OK(pack(f, f->cond, B, B, 1));
@@ -1095,7 +1098,7 @@ ntp_status record_step(ntp_flow* f, int B, bool update) {
     float* g = f->grad;
     auto gw = [&](int l) { return g + f->blk[2 * l].off; };
     auto gb = [&](int l) { return g + f->blk[2 * l + 1].off; };
-    F_OK(launch_head(f, f->y, f->nh, f->hy, B, nullptr, gb(3)));
+    F_OK(launch_head(f, f->y, f->nh, f->hy, rows_w ? f->cw : nullptr, B, nullptr, gb(3)));
     // The weight gradients dW_l = dZ_l^T X_l run on stream2 beside the chain
     // of activation gradients dZ_{l-1} = (dZ_l W_l) * mask on the main stream;
     // events order each dW_l after its dZ_l and join the two before Adam.
@@ -1242,7 +1245,7 @@ ntp_status ntp_flow_create(int32_t device, const ntp_flow_config* cfg, ntp_flow*
     const size_t np = static_cast<size_t>(f->n_pad);
     if ((e = dalloc(&f->dp, B * np)) || (e = dalloc(&f->dpt, B * np)) || (e = dalloc(&f->P, B * np)) ||
         (e = dalloc(&f->cond, B * kCond)) || (e = dalloc(&f->y, B)) || (e = dalloc(&f->nh, B)) ||
-        (e = dalloc(&f->hy, B)) || (e = dalloc(&f->loss, 1)) || (e = dalloc(&f->gemm_err, 1)) ||
+        (e = dalloc(&f->hy, B)) || (e = dalloc(&f->cw, B)) || (e = dalloc(&f->loss, 1)) || (e = dalloc(&f->gemm_err, 1)) ||
         (e = dalloc(&f->skip, 1)) || (e = dalloc(&f->step_dev, 1)) || (e = dalloc(&f->lr_dev, 1)))
         return fail(e);
     // He-uniform weights (seeded); zero biases, zero padding input columns of
@@ -1336,12 +1339,12 @@ ntp_status ntp_flow_get_params(ntp_flow* f, float* host, uint64_t n, int32_t whi
 ntp_status ntp_flow_train_step(ntp_flow* f, const float* cond, const float* tres, const float* nhits,
                                const int32_t* has_time, int32_t B, int32_t on_device, int32_t update,
                                double* loss_out) {
-    return ntp_flow_train_steps(f, cond, tres, nhits, has_time, B, 1, on_device, update, loss_out);
+    return ntp_flow_train_steps(f, cond, tres, nhits, has_time, nullptr, B, 1, on_device, update, loss_out);
 }
 
 ntp_status ntp_flow_train_steps(ntp_flow* f, const float* cond, const float* tres, const float* nhits,
-                                const int32_t* has_time, int32_t B, int32_t n_steps, int32_t on_device,
-                                int32_t update, double* losses) {
+                                const int32_t* has_time, const float* count_weight, int32_t B, int32_t n_steps,
+                                int32_t on_device, int32_t update, double* losses) {
     if (!f || !cond || !tres || !nhits || !has_time || n_steps < 1) return NTP_ERR_INVALID;
     if (B < 128 || B > f->cap || B % 128) {
         f->err = "ntp_flow_train_step: the batch must be a multiple of 128 up to the capacity";
@@ -1362,6 +1365,7 @@ ntp_status ntp_flow_train_steps(ntp_flow* f, const float* cond, const float* tre
     }
     double* d_loss = f->loss_hist;
     int* d_skip = f->skip_hist;
+    const bool rows_w = count_weight != nullptr;
     F_CUDA(f, cudaMemsetAsync(d_skip, 0, sizeof(int) * n_steps, st));
     const cudaMemcpyKind kind = on_device ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice;
     for (int i = 0; i < n_steps; ++i) {
@@ -1371,13 +1375,14 @@ ntp_status ntp_flow_train_steps(ntp_flow* f, const float* cond, const float* tre
         F_CUDA(f, cudaMemcpyAsync(f->y, tres + o, sizeof(float) * B, kind, st));
         F_CUDA(f, cudaMemcpyAsync(f->nh, nhits + o, sizeof(float) * B, kind, st));
         F_CUDA(f, cudaMemcpyAsync(f->hy, has_time + o, sizeof(int) * B, kind, st));
+        if (rows_w) F_CUDA(f, cudaMemcpyAsync(f->cw, count_weight + o, sizeof(float) * B, kind, st));
         if (f->use_graph) {
-            if (!f->gexec || f->g_B != B || f->g_update != update) {
+            if (!f->gexec || f->g_B != B || f->g_update != update || f->g_rows_w != static_cast<int>(rows_w)) {
                 if (f->gexec) cudaGraphExecDestroy(f->gexec);
                 f->gexec = nullptr;
                 F_CUDA(f, prepare_kernels(f));
                 F_CUDA(f, cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
-                const ntp_status rs = record_step(f, B, update != 0);
+                const ntp_status rs = record_step(f, B, update != 0, rows_w);
                 cudaGraph_t graph = nullptr;
                 const cudaError_t ec = cudaStreamEndCapture(st, &graph);
                 if (rs != NTP_OK || ec != cudaSuccess) {
@@ -1393,10 +1398,11 @@ ntp_status ntp_flow_train_steps(ntp_flow* f, const float* cond, const float* tre
                 }
                 f->g_B = B;
                 f->g_update = update;
+                f->g_rows_w = static_cast<int>(rows_w);
             }
             F_CUDA(f, cudaGraphLaunch(f->gexec, st));
         } else {
-            F_OK(record_step(f, B, update != 0));
+            F_OK(record_step(f, B, update != 0, rows_w));
         }
         F_CUDA(f, cudaMemcpyAsync(d_loss + i, f->loss, sizeof(double), cudaMemcpyDeviceToDevice, st));
         if (update) F_CUDA(f, cudaMemcpyAsync(d_skip + i, f->skip, sizeof(int), cudaMemcpyDeviceToDevice, st));
@@ -1438,7 +1444,8 @@ ntp_status ntp_flow_forward(ntp_flow* f, const float* cond, int32_t n, float* pa
 }
 
 ntp_status ntp_flow_head(ntp_flow* f, const float* params, const float* tres, const float* nhits,
-                         const int32_t* has_time, int32_t B, double* loss_out, float* grad_out) {
+                         const int32_t* has_time, const float* count_weight, int32_t B, double* loss_out,
+                         float* grad_out) {
     if (!f || !params || !tres || !nhits || !has_time || B <= 0 || B > f->cap) return NTP_ERR_INVALID;
     F_CUDA(f, cudaSetDevice(f->device));
     cudaStream_t st = f->stream;
@@ -1450,8 +1457,10 @@ ntp_status ntp_flow_head(ntp_flow* f, const float* params, const float* tres, co
         F_CUDA(f, cudaMemcpyAsync(f->y, tres, sizeof(float) * B, cudaMemcpyHostToDevice, st));
         F_CUDA(f, cudaMemcpyAsync(f->nh, nhits, sizeof(float) * B, cudaMemcpyHostToDevice, st));
         F_CUDA(f, cudaMemcpyAsync(f->hy, has_time, sizeof(int) * B, cudaMemcpyHostToDevice, st));
+        if (count_weight)
+            F_CUDA(f, cudaMemcpyAsync(f->cw, count_weight, sizeof(float) * B, cudaMemcpyHostToDevice, st));
         F_CUDA(f, cudaMemsetAsync(f->loss, 0, sizeof(double), st));
-        F_OK(launch_head(f, f->y, f->nh, f->hy, B, gf, nullptr));
+        F_OK(launch_head(f, f->y, f->nh, f->hy, count_weight ? f->cw : nullptr, B, gf, nullptr));
         F_CUDA(f, cudaGetLastError());
         double hl = 0.0;
         F_CUDA(f, cudaMemcpyAsync(&hl, f->loss, sizeof(double), cudaMemcpyDeviceToHost, st));

@@ -207,20 +207,26 @@ class RQNormFlow:
         import torch
         t = table.tres[table.has_time.bool()]
         shift = float(torch.median(t).item()) if t.numel() else 0.0
-        log_n = float(torch.log1p(table.group_count.double()).mean().item())
+        log_n = float(torch.log1p(table.group_expec.double()).mean().item())
         self.init_output_bias(shift=shift, log_expec=log_n)
 
     def fit_table(self, table, *, epochs: int = 1, batch_size: int | None = None, seed: int = 0,
-                  max_steps: int | None = None) -> list[float]:
+                  max_steps: int | None = None, count_once: bool = False) -> list[float]:
         """Trains on a FlowTable held in device memory: the rows are shuffled
         on the device once per epoch and fed to the training step batch by
-        batch without leaving the GPU; returns the per-step losses."""
+        batch without leaving the GPU; returns the per-step losses.
+        count_once: every row's count term weighted by 1 / (rows of its PMT),
+        so that each PMT's count enters the loss once.  The reference's
+        tables repeat a PMT's count on each of its rows (False, the
+        default), which weights a PMT by its number of rows; for small
+        counts the rows grow with the count itself."""
         import torch
         n = len(table)
         bs = int(batch_size or self.hparams.batch_size)
         bs = max(128, min(bs, self.batch_capacity) // 128 * 128)
         gen = torch.Generator(device=table.tres.device)
         gen.manual_seed(int(seed))
+        cw_all = table.count_once_weights() if count_once else None
         losses: list[float] = []
         for _ in range(epochs):
             perm = torch.randperm(n, device=table.tres.device, generator=gen)
@@ -228,23 +234,28 @@ class RQNormFlow:
             tres = table.tres[perm].contiguous()
             nh = table.nhits[perm].contiguous()
             has = table.has_time[perm].contiguous()
+            cw = cw_all[perm].contiguous() if cw_all is not None else None
             torch.cuda.synchronize()
             steps = n // bs
             if max_steps is not None:
                 steps = min(steps, max_steps - len(losses))
             if steps > 0:
-                losses.extend(self.train_steps(cond, tres, nh, has, bs, steps))
+                losses.extend(self.train_steps(cond, tres, nh, has, bs, steps, count_weight=cw))
             if max_steps is not None and len(losses) >= max_steps:
                 return losses
         return losses
 
-    def train_steps(self, cond, tres, nhits, has_time, batch: int, steps: int) -> list[float]:
+    def train_steps(self, cond, tres, nhits, has_time, batch: int, steps: int, *, count_weight=None,
+                    update: bool = True) -> list[float]:
         """`steps` Adam steps on consecutive batches of `batch` rows of CUDA
-        tensors, one synchronisation for all; returns the losses."""
+        tensors, one synchronisation for all; returns the losses.
+        count_weight: per-row factors of the count term (None = 1); update
+        False computes loss and gradient only."""
         out = np.empty(steps, np.float64)
         self._check(self.lib.ntp_flow_train_steps(self._h, cond.data_ptr(), tres.data_ptr(), nhits.data_ptr(),
-                                                  has_time.data_ptr(), int(batch), int(steps), 1, 1,
-                                                  out.ctypes.data))
+                                                  has_time.data_ptr(),
+                                                  count_weight.data_ptr() if count_weight is not None else None,
+                                                  int(batch), int(steps), 1, int(bool(update)), out.ctypes.data))
         return out.tolist()
 
     # --------------------------------------------------------------- inference
@@ -256,16 +267,19 @@ class RQNormFlow:
         self._check(self.lib.ntp_flow_forward(self._h, cond.ctypes.data, cond.shape[0], out.ctypes.data))
         return out
 
-    def head(self, params, tres, nhits, has_time=None) -> tuple[float, np.ndarray]:
-        """Loss and its gradient by the raw outputs for given raw outputs."""
+    def head(self, params, tres, nhits, has_time=None, count_weight=None) -> tuple[float, np.ndarray]:
+        """Loss and its gradient by the raw outputs for given raw outputs
+        (count_weight: per-row factors of the count term, None = 1)."""
         params = _f32(params)
         B = params.shape[0]
         tres, nhits = _f32(tres, B), _f32(nhits, B)
         has_time = np.ones(B, np.int32) if has_time is None else np.ascontiguousarray(has_time, np.int32)
+        cw = None if count_weight is None else _f32(count_weight, B)
         grad = np.empty_like(params)
         loss = C.c_double()
         self._check(self.lib.ntp_flow_head(self._h, params.ctypes.data, tres.ctypes.data, nhits.ctypes.data,
-                                           has_time.ctypes.data, B, C.byref(loss), grad.ctypes.data))
+                                           has_time.ctypes.data, cw.ctypes.data if cw is not None else None, B,
+                                           C.byref(loss), grad.ctypes.data))
         return loss.value, grad
 
     def logpdf(self, cond, cond_index, times, *, log_expec: bool = False):

@@ -68,6 +68,16 @@ class FlowTable:
     def __len__(self) -> int:
         return int(self.tres.shape[0])
 
+    def count_once_weights(self):
+        """Per-row weights 1 / (rows of the row's group): with them each
+        group's count term enters a training loss once (float32, device)."""
+        import torch
+        if self.row_group is None:
+            raise ValueError("the table has no row_group")
+        rg = self.row_group.long()
+        n = torch.bincount(rg, minlength=int(self.group_cond.shape[0]))
+        return (1.0 / n[rg].to(torch.float32)).contiguous()
+
     def save(self, path) -> None:
         np.savez(path, **{k: getattr(self, k).cpu().numpy() for k in
                           ("cond", "tres", "nhits", "has_time", "group_cond", "group_expec", "group_count",

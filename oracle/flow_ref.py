@@ -164,12 +164,15 @@ def flow_cdf(y, raw, n_layers: int, r0: float, r1: float, K: int):
     return 0.5 * torch.erfc(-((cur - shift) / scale) / math.sqrt(2.0))
 
 
-def head_loss(raw, tres, nhits, has_time, L: int, K: int, r0: float, r1: float):
-    """Batch-mean loss of raw outputs [B x (L(3K+1)+3)] (log expectation last)."""
+def head_loss(raw, tres, nhits, has_time, L: int, K: int, r0: float, r1: float, count_weight=None):
+    """Batch-mean loss of raw outputs [B x (L(3K+1)+3)] (log expectation last);
+    count_weight multiplies each row's Poisson term (None = 1)."""
     NP = 3 * K + 1
     le = torch.clamp(raw[:, L * NP + 2], -LE_CLAMP, LE_CLAMP)
     n = nhits
     poiss = n * le - torch.exp(le) - torch.lgamma(n + 1.0)
+    if count_weight is not None:
+        poiss = poiss * count_weight
     lp = flow_logpdf(tres, raw, L, r0, r1, K)
     lp = torch.where(has_time, lp, torch.zeros_like(lp))
     return -(lp.sum() + poiss.sum()) / raw.shape[0]
@@ -213,7 +216,7 @@ def conditioner(layers, cond: torch.Tensor, bf16: bool = False) -> torch.Tensor:
 
 
 def full_loss(theta: np.ndarray, cond, tres, nhits, has_time, L: int, K: int, r0: float, r1: float,
-              n_pad: int, bf16: bool = False):
+              n_pad: int, bf16: bool = False, count_weight=None):
     """Loss and its gradient by the flat parameters (float64 numpy)."""
     layers = [(W.clone().requires_grad_(True), b.clone().requires_grad_(True)) for W, b in unpack(theta, n_pad)]
     c = torch.as_tensor(np.asarray(cond, np.float64))
@@ -221,7 +224,8 @@ def full_loss(theta: np.ndarray, cond, tres, nhits, has_time, L: int, K: int, r0
     n_out = L * (3 * K + 1) + 3
     loss = head_loss(raw[:, :n_out], torch.as_tensor(np.asarray(tres, np.float64)),
                      torch.as_tensor(np.asarray(nhits, np.float64)),
-                     torch.as_tensor(np.asarray(has_time, bool)), L, K, r0, r1)
+                     torch.as_tensor(np.asarray(has_time, bool)), L, K, r0, r1,
+                     None if count_weight is None else torch.as_tensor(np.asarray(count_weight, np.float64)))
     loss.backward()
     g = np.concatenate([np.concatenate([W.grad.numpy().ravel(), b.grad.numpy().ravel()]) for W, b in layers])
     return float(loss.item()), g

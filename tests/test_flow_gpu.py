@@ -76,6 +76,51 @@ def test_head_loss_and_gradient(L, K, r0, r1):
     assert np.linalg.norm(grad - g_ref) / np.linalg.norm(g_ref) < 2e-3
 
 
+def test_head_with_per_row_count_weights():
+    """Per-row factors of the Poisson term (0 on most rows, fractional on the
+    rest, as the expected-count tables give) against the oracle."""
+    L, K, r0, r1 = 5, 12, -20.0, 1500.0
+    rng = np.random.default_rng(15)
+    B = 1024
+    with make(L, K, r0, r1) as fl:
+        raw = (rng.standard_normal((B, fl.n_outputs)) * 0.8).astype(np.float32)
+        NP = 3 * K + 1
+        raw[:, L * NP] = rng.uniform(r0, r0 + 0.5 * (r1 - r0), B)
+        raw[:, L * NP + 2] = rng.standard_normal(B) * 2.0
+        _, tres, nhits, has = batch(rng, B, r0, r1)
+        nhits = (nhits * rng.uniform(0.5, 1.5, B)).astype(np.float32)  # expectations, not integers
+        cw = np.where(rng.uniform(size=B) < 0.3, rng.uniform(0.05, 1.0, B), 0.0).astype(np.float32)
+        loss, grad = fl.head(raw, tres, nhits, has, count_weight=cw)
+        loss1, _ = fl.head(raw, tres, nhits, has)
+    t = torch.as_tensor(raw.astype(np.float64)).requires_grad_(True)
+    ref = R.head_loss(t, torch.as_tensor(tres.astype(np.float64)), torch.as_tensor(nhits.astype(np.float64)),
+                      torch.as_tensor(has.astype(bool)), L, K, r0, r1, torch.as_tensor(cw.astype(np.float64)))
+    ref.backward()
+    g_ref = t.grad.numpy()
+    assert loss == pytest.approx(ref.item(), rel=1e-5)
+    assert loss != pytest.approx(loss1, rel=1e-3)
+    assert np.linalg.norm(grad - g_ref) / np.linalg.norm(g_ref) < 2e-3
+
+
+def test_full_gradient_with_count_weights():
+    L, K, r0, r1 = 5, 12, -20.0, 1500.0
+    rng = np.random.default_rng(25)
+    B = 1024
+    with make(L, K, r0, r1) as fl:
+        cond, tres, nhits, has = batch(rng, B, r0, r1)
+        cw = np.where(rng.uniform(size=B) < 0.2, rng.uniform(0.1, 1.0, B), 0.0).astype(np.float32)
+        dev = lambda x: torch.as_tensor(x, device="cuda")  # noqa: E731
+        loss = fl.train_steps(dev(cond), dev(tres), dev(nhits), dev(has), B, 1, count_weight=dev(cw),
+                              update=False)[0]
+        g = fl.gradient()
+        theta = fl.get_params()
+        n_pad = fl.n_outputs_padded
+    ref_loss, g_ref = R.full_loss(theta, cond, tres, nhits, has.astype(bool), L, K, r0, r1, n_pad, bf16=True,
+                                  count_weight=cw)
+    assert loss == pytest.approx(ref_loss, rel=1e-3)
+    assert np.linalg.norm(g - g_ref) <= 3e-2 * np.linalg.norm(g_ref)
+
+
 def test_head_gradient_clip():
     """With grad_clip = c every row of dL/dP has an L2 norm of at most c / B and
     points along the unclipped row; rows below the bound are unchanged."""

@@ -21,14 +21,15 @@ from neutrinotelescopes_gb300.tables import TableConfig, make_flow_table  # noqa
 pytestmark = pytest.mark.gpu
 
 
-def _train(tab, steps: int, lr0: float = 1e-3) -> RQNormFlow:
+def _train(tab, steps: int, lr0: float = 1e-3, count_once: bool = False) -> RQNormFlow:
     fl = RQNormFlow(RQNormFlowHParams(batch_size=8192, lr=lr0))
     fl.init_from_table(tab)
     per_epoch = len(tab) // 8192
     done, ep = 0, 0
     while done < steps:
         fl.set_lr(1e-5 + 0.5 * (lr0 - 1e-5) * (1 + math.cos(math.pi * done / steps)))
-        done += len(fl.fit_table(tab, epochs=1, seed=ep, max_steps=min(per_epoch, steps - done)))
+        done += len(fl.fit_table(tab, epochs=1, seed=ep, max_steps=min(per_epoch, steps - done),
+                                 count_once=count_once))
         ep += 1
     return fl
 
