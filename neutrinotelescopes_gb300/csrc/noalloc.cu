@@ -220,6 +220,7 @@ extern "C" ntp_status ntp_propagate_noalloc(const ntp_medium_desc* m, const ntp_
     p.target_ids = reinterpret_cast<const uint32_t*>(base + kOffIds);
     p.n_targets = n_targets;
     p.targets_in_smem = 1;
+    p.columns_in_smem = 0;
     p.columns = nullptr;
     p.members = nullptr;
     p.n_columns = 0;

@@ -147,7 +147,6 @@ bool fill_world_params(const ntp_ctx* ctx, PropParams& p) {
     p.targets = ctx->d_tgt;
     p.target_ids = ctx->d_tgt_id;
     p.n_targets = ctx->n_tgt;
-    p.targets_in_smem = ctx->n_tgt <= kMaxSmemTargets ? 1 : 0;
     p.columns = ctx->n_cols > 0 ? ctx->d_cols : nullptr;
     p.members = ctx->d_members;
     p.n_columns = ctx->n_cols;
@@ -171,6 +170,7 @@ bool fill_world_params(const ntp_ctx* ctx, PropParams& p) {
     p.spec_p1 = ctx->spec_p1;
     p.hg_g = ctx->hg_g;
     ntp::set_rayleigh(p, ctx->f_ray);
+    ntp::choose_staging(p);
     return true;
 }
 
@@ -614,6 +614,7 @@ ntp_status ntp_propagate(ntp_ctx* ctx, const ntp_source* sources, int32_t n_sour
     if (o.flags & NTP_FLAG_PLAIN_SCAN) {
         p.columns = nullptr;
         p.cell_start = nullptr;
+        ntp::choose_staging(p);
     }
     p.max_steps = o.max_steps;
     p.hit_policy = o.hit_policy;

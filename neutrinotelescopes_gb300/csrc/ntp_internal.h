@@ -16,6 +16,9 @@ namespace ntp {
 
 constexpr int kPropBlock = 256;      // threads per block of the propagation kernel
 constexpr int kMaxSmemTargets = 8192;  // targets staged in shared memory (20 B each)
+// with column culling, targets are staged only while the kernel's shared
+// memory stays within this budget (four blocks per SM, room left for L1)
+constexpr size_t kSmemStageBudget = 32 * 1024;
 constexpr int kMaxSmemColumns = 2048;  // columns staged in shared memory (32 B each)
 constexpr int kMaxSmemGridInts = 16384; // grid offsets + items staged in shared memory (4 B each)
 constexpr int kGridMinColumns = 9;      // below this many columns every column is tested
@@ -43,7 +46,8 @@ struct PropParams {
     const float4* targets;                // device, (x, y, z, r^2)
     const uint32_t* target_ids;           // device, module_id per target
     int n_targets;
-    int targets_in_smem;                  // stage targets in shared memory
+    int targets_in_smem;                  // stage targets (and ids, column members) in shared memory
+    int columns_in_smem;                  // stage the columns (and the cell grid) in shared memory
 
     const Column* columns;                // device; nullptr = scan every target
     const int* members;                   // device, target indices grouped by column
@@ -125,6 +129,18 @@ inline void set_rayleigh(PropParams& p, float f) {
 }
 
 size_t prop_smem_bytes(const PropParams& p);
+
+// What the propagation kernel stages in shared memory.  Without columns a
+// step tests every target: targets staged when they fit at all.  With
+// column culling a step reads the columns (and the cell grid) every time
+// and a target only when it is a candidate: columns staged, targets only
+// while the total stays within kSmemStageBudget (more would cost blocks per
+// SM; cached global loads serve the rare candidate tests).
+inline void choose_staging(PropParams& p) {
+    p.columns_in_smem = p.columns ? 1 : 0;
+    p.targets_in_smem = p.n_targets <= kMaxSmemTargets ? 1 : 0;
+    if (p.columns && p.targets_in_smem && prop_smem_bytes(p) > kSmemStageBudget) p.targets_in_smem = 0;
+}
 cudaError_t launch_propagate(const PropParams& p, int grid, cudaStream_t stream);
 cudaError_t propagate_occupancy(const PropParams& p, int* blocks_per_sm);
 // the kernel launch_propagate uses (for CUDA-graph kernel-node updates)

@@ -302,10 +302,13 @@ __device__ __forceinline__ void init_photon(Photon& ph, const ntp_source* __rest
 
 template <int kMinBlocks>
 __global__ void __launch_bounds__(kPropBlock, kMinBlocks) propagate_kernel(const PropParams p) {
-    // shared memory: medium knots | targets | module ids | columns | members | spectrum knots
+    // shared memory: medium knots | targets | columns | module ids | members |
+    // cell grid | spectrum knots (targets, ids and members when
+    // targets_in_smem; columns and the grid when columns_in_smem)
     extern __shared__ float4 smem[];
     const int nt_s = p.targets_in_smem ? p.n_targets : 0;
-    const int nc_s = p.targets_in_smem && p.columns ? p.n_columns : 0;
+    const int nc_s = p.columns_in_smem && p.columns ? p.n_columns : 0;
+    const int nm_s = nt_s && nc_s ? p.n_targets : 0;
     float4* s_med = smem;
     float4* s_tgt = s_med + p.n_medium;
     Column* s_col = reinterpret_cast<Column*>(s_tgt + nt_s);
@@ -313,7 +316,7 @@ __global__ void __launch_bounds__(kPropBlock, kMinBlocks) propagate_kernel(const
     int* s_mem = reinterpret_cast<int*>(s_tid + nt_s);
     const bool grid_s = nc_s && p.cell_start && (p.grid_nx * p.grid_ny + 1 + p.n_cell_items) <= kMaxSmemGridInts;
     const int ng_s = grid_s ? p.grid_nx * p.grid_ny + 1 : 0;
-    int* s_cstart = s_mem + (nc_s ? nt_s : 0);
+    int* s_cstart = s_mem + nm_s;
     int* s_citems = s_cstart + ng_s;
     float* s_spec = reinterpret_cast<float*>(s_citems + (grid_s ? p.n_cell_items : 0));
 
@@ -324,8 +327,7 @@ __global__ void __launch_bounds__(kPropBlock, kMinBlocks) propagate_kernel(const
         s_tid[i] = p.target_ids[i];
     }
     for (int i = threadIdx.x; i < nc_s; i += blockDim.x) s_col[i] = p.columns[i];
-    if (nc_s)
-        for (int i = threadIdx.x; i < nt_s; i += blockDim.x) s_mem[i] = p.members[i];
+    for (int i = threadIdx.x; i < nm_s; i += blockDim.x) s_mem[i] = p.members[i];
     if (grid_s) {
         for (int i = threadIdx.x; i < ng_s; i += blockDim.x) s_cstart[i] = p.cell_start[i];
         for (int i = threadIdx.x; i < p.n_cell_items; i += blockDim.x) s_citems[i] = p.cell_items[i];
@@ -333,10 +335,10 @@ __global__ void __launch_bounds__(kPropBlock, kMinBlocks) propagate_kernel(const
     __syncthreads();
     const int* cstart = grid_s ? s_cstart : p.cell_start;
     const int* citems = grid_s ? s_citems : p.cell_items;
-    const float4* tg = p.targets_in_smem ? s_tgt : p.targets;
-    const uint32_t* tid = p.targets_in_smem ? s_tid : p.target_ids;
+    const float4* tg = nt_s ? s_tgt : p.targets;
+    const uint32_t* tid = nt_s ? s_tid : p.target_ids;
     const Column* cols = p.columns ? (nc_s ? s_col : p.columns) : nullptr;
-    const int* mem = nc_s ? s_mem : p.members;
+    const int* mem = nm_s ? s_mem : p.members;
 
     SpectrumView spec{p.spec_kind, p.n_spec, s_spec, p.spec_p0, p.spec_p1};
     const float g = p.hg_g, one_m_g = 1.0f - g, one_m_g2 = fmaf(-g, g, 1.0f);
@@ -494,13 +496,13 @@ __global__ void __launch_bounds__(kPropBlock, kMinBlocks) propagate_kernel(const
 
 size_t prop_smem_bytes(const PropParams& p) {
     size_t b = sizeof(float4) * static_cast<size_t>(p.n_medium);
-    if (p.targets_in_smem) {
-        b += (sizeof(float4) + sizeof(uint32_t)) * static_cast<size_t>(p.n_targets);
-        if (p.columns) {
-            b += sizeof(Column) * static_cast<size_t>(p.n_columns) + sizeof(int) * static_cast<size_t>(p.n_targets);
-            const long long g = p.cell_start ? static_cast<long long>(p.grid_nx) * p.grid_ny + 1 + p.n_cell_items : 0;
-            if (p.cell_start && g <= kMaxSmemGridInts) b += sizeof(int) * static_cast<size_t>(g);
-        }
+    const bool nt = p.targets_in_smem != 0, nc = p.columns_in_smem && p.columns;
+    if (nt) b += (sizeof(float4) + sizeof(uint32_t)) * static_cast<size_t>(p.n_targets);
+    if (nc) {
+        b += sizeof(Column) * static_cast<size_t>(p.n_columns);
+        if (nt) b += sizeof(int) * static_cast<size_t>(p.n_targets);  // members
+        const long long g = p.cell_start ? static_cast<long long>(p.grid_nx) * p.grid_ny + 1 + p.n_cell_items : 0;
+        if (p.cell_start && g <= kMaxSmemGridInts) b += sizeof(int) * static_cast<size_t>(g);
     }
     b += sizeof(float) * static_cast<size_t>(p.n_spec);
     return b;
