@@ -468,7 +468,7 @@ cudaError_t gemm_prepare() {
     if (e == cudaSuccess) e = configure_bn<128>();
     if (e == cudaSuccess) e = configure_bn<256>();
     if (e == cudaSuccess) (void)sm_count();
-    if (e == cudaSuccess && !encode_fn()) e = cudaErrorNotSupported;  // the driver's tensor-map encoder
+    if (e == cudaSuccess && !encode_fn()) e = cudaErrorNotSupported;  // the CUDA driver API's tensor-map encoder
     return e;
 }
 

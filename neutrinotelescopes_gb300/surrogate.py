@@ -7,8 +7,8 @@ draws each PMT's hit count (Poisson of its expectation) and arrival-time
 residuals (``ntp_flow_sample``), and the geometric time turns them into hit
 times.  Events with a module closer than d_min, or energies outside the
 training range, go to plain MC (``propagate_photons`` + ``calc_total_weight``
-+ ``resample_simulation`` on the device), as the benchmark spec's hybrid mode
-asks.  Modules beyond d_max get no light from the surrogate (200 m is about
++ ``resample_simulation`` on the device): plain MC is the fallback outside
+the surrogate's training domain.  Modules beyond d_max get no light from the surrogate (200 m is about
 7 absorption lengths at 400 nm).
 
 ``mc_truth`` runs plain MC for one event and returns per-(module, PMT)

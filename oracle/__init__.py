@@ -1,8 +1,8 @@
 """Python access to the CPU oracle (oracle/libntp_oracle.so).
 
 TEST INFRASTRUCTURE ONLY: imported by tests/, by the smoke check and by the
-CPU-baseline leg of bench.py, always as the checker or the CPU reference
-timing, never as the product path.  Parity status and its limits are stated
+CPU-baseline leg of bench.py, always as the reference the GPU results are
+compared with or as the timed CPU reference, never as the product path.  Parity status and its limits are stated
 at the top of ntp_oracle.c.
 """
 from __future__ import annotations

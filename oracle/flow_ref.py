@@ -1,6 +1,6 @@
 """CPU oracle of the arrival-time flow in torch float64.
 
-TEST INFRASTRUCTURE ONLY: imported by tests/ as the checker of the flow's
+TEST INFRASTRUCTURE ONLY: imported by tests/ to verify the flow's
 CUDA kernels (forward, head gradient, full-network gradient, Adam), never by
 the product path.
 

@@ -1,6 +1,6 @@
 """CPU oracle of the flow's training-table generator (ntp_make_table).
 
-TEST INFRASTRUCTURE ONLY: imported by tests/ as the checker of the table
+TEST INFRASTRUCTURE ONLY: imported by tests/ to verify the table
 kernels, never by the product path.
 
 Restates, for hits already propagated and weighted: the PMT assignment of a
