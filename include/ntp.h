@@ -496,13 +496,21 @@ ntp_status ntp_flow_mixture_cdf(ntp_flow* flow, const float* cond, int32_t n_con
    and cond_key[c], so a condition's hits do not depend on the other
    conditions of the call.  Outputs grouped by condition in increasing c:
    hit_cond (the condition index) and hit_time; counts (may be NULL) per
-   condition.  *n_hits receives the total; above capacity nothing is written
-   and NTP_ERR_OVERFLOW returned.  n_cond <= 1048576.  All buffers on the
-   host, or on the device when on_device != 0.  No reference counterpart:
-   the reference only evaluates the density. */
+   condition.  *n_hits receives the total; above capacity no hit is written
+   (counts are) and NTP_ERR_OVERFLOW returned: the counts and offsets of
+   the call are kept, and ntp_flow_sample_resume draws its hits into larger
+   buffers without repeating the conditioner pass.  n_cond <= 1048576.  All
+   buffers on the host, or on the device when on_device != 0.  No reference
+   counterpart: the reference only evaluates the density. */
 ntp_status ntp_flow_sample(ntp_flow* flow, const float* cond, int32_t n_cond, const uint64_t* cond_key, uint64_t seed,
                            uint64_t* counts, int32_t* hit_cond, float* hit_time, uint64_t capacity, uint64_t* n_hits,
                            int32_t on_device);
+/* The hits of the last ntp_flow_sample call that returned NTP_ERR_OVERFLOW,
+   into buffers of at least its *n_hits entries (the same hits that call
+   would have written).  Any other call on the flow in between discards the
+   pending sample (NTP_ERR_NOT_READY). */
+ntp_status ntp_flow_sample_resume(ntp_flow* flow, int32_t* hit_cond, float* hit_time, uint64_t capacity,
+                                  uint64_t* n_hits, int32_t on_device);
 
 /* ------------------------------------------------------------------ serving
  * Continuous-batching event server (no reference counterpart; the reference

@@ -955,6 +955,13 @@ struct ntp_flow {
     // inference
     float* knots = nullptr;
     size_t knots_cap = 0;
+    // sampling scratch (keys, counts, offsets, scan sums; grown on demand) and
+    // the state of a sample that overflowed its buffers (resumable)
+    unsigned long long* samp = nullptr;
+    size_t samp_cap = 0;
+    int samp_n = 0;  // conditions of the pending sample, 0 = none
+    uint2 samp_key{};
+    unsigned long long samp_total = 0;
 };
 
 namespace {
@@ -1071,7 +1078,8 @@ ntp_status launch_head(ntp_flow* f, const float* y, const float* nh, const int* 
 
 void free_all(ntp_flow* f) {
     void* ps[] = {f->theta, f->m, f->v, f->grad, f->x, f->xt, f->dp, f->dpt, f->P, f->cond, f->y, f->nh, f->hy,
-                  f->loss, f->gemm_err, f->skip, f->step_dev, f->lr_dev, f->knots, f->loss_hist, f->skip_hist, f->cw};
+                  f->loss, f->gemm_err, f->skip, f->step_dev, f->lr_dev, f->knots, f->loss_hist, f->skip_hist, f->cw,
+                  f->samp};
     for (void* p : ps)
         if (p) cudaFree(p);
     for (int l = 0; l < 4; ++l) {
@@ -1482,6 +1490,7 @@ ntp_status ntp_flow_evaluate(ntp_flow* f, const float* cond, int32_t n_cond, con
     if (!f || !cond || n_cond <= 0) return NTP_ERR_INVALID;
     if (n_tuples > 0 && (!cond_index || !times || !logpdf)) return NTP_ERR_INVALID;
     F_CUDA(f, cudaSetDevice(f->device));
+    f->samp_n = 0;  // the knots are rewritten: no pending sample
     cudaStream_t st = f->stream;
     const int row = ntp::knot_row(f->L, f->K);
     const size_t need = static_cast<size_t>(n_cond) * row;
@@ -1543,6 +1552,43 @@ ntp_status ntp_flow_evaluate(ntp_flow* f, const float* cond, int32_t n_cond, con
 }
 
 
+namespace {
+
+// Draws the hits of the counts and offsets in f->samp (keys | counts |
+// offsets) for the knots in f->knots.
+ntp_status sample_draw(ntp_flow* f, int n_cond, uint2 key, unsigned long long total, int32_t* hit_cond,
+                       float* hit_time, int32_t on_device) {
+    cudaStream_t st = f->stream;
+    const size_t n = static_cast<size_t>(n_cond);
+    const unsigned long long* d_key = f->samp;
+    const unsigned long long* d_off = f->samp + 2 * n;
+    int32_t* d_hc = hit_cond;
+    float* d_ht = hit_time;
+    void* stage = nullptr;
+    if (!on_device) {
+        F_CUDA(f, cudaMalloc(&stage, 8 * total));
+        d_hc = static_cast<int32_t*>(stage);
+        d_ht = reinterpret_cast<float*>(static_cast<int32_t*>(stage) + total);
+    }
+    const int grid = static_cast<int>(std::min<unsigned long long>((total + 255) / 256, 152ull * 32));
+    cudaError_t e = cudaSuccess;
+    with_bins(f->K, [&](auto kc) {
+        ntp::sample_draw_kernel<decltype(kc)::value>
+            <<<grid, 256, 0, st>>>(f->knots, f->L, n_cond, d_key, key, d_off, total, d_hc, d_ht);
+        e = cudaGetLastError();
+    });
+    if (e == cudaSuccess && !on_device) {
+        e = cudaMemcpyAsync(hit_cond, d_hc, 4 * total, cudaMemcpyDeviceToHost, st);
+        if (e == cudaSuccess) e = cudaMemcpyAsync(hit_time, d_ht, 4 * total, cudaMemcpyDeviceToHost, st);
+    }
+    if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+    if (stage) cudaFree(stage);
+    if (e != cudaSuccess) return ferr(f, e, "ntp_flow_sample");
+    return NTP_OK;
+}
+
+}  // namespace
+
 ntp_status ntp_flow_sample(ntp_flow* f, const float* cond, int32_t n_cond, const uint64_t* cond_key, uint64_t seed,
                            uint64_t* counts, int32_t* hit_cond, float* hit_time, uint64_t capacity, uint64_t* n_hits,
                            int32_t on_device) {
@@ -1559,68 +1605,70 @@ ntp_status ntp_flow_sample(ntp_flow* f, const float* cond, int32_t n_cond, const
     const int nb = (n_cond + 1023) / 1024;
     // scratch: keys u64[n] | counts u64[n] | offsets u64[n] | block sums u64[nb + 1] x 2 | total
     const size_t n = static_cast<size_t>(n_cond);
-    unsigned long long* scratch = nullptr;
-    F_CUDA(f, dalloc(&scratch, 3 * n + 2 * (nb + 1) + 1));
-    auto run = [&]() -> ntp_status {
-        unsigned long long* d_key = scratch;
-        unsigned long long* d_cnt = scratch + n;
-        unsigned long long* d_off = scratch + 2 * n;
-        unsigned long long* d_bs = scratch + 3 * n;
-        unsigned long long* d_bo = d_bs + nb + 1;
-        unsigned long long* d_tot = d_bo + nb + 1;
-        F_CUDA(f, cudaMemcpyAsync(d_key, cond_key, 8 * n, on_device ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice,
+    const size_t need = 3 * n + 2 * (static_cast<size_t>(nb) + 1) + 1;
+    if (need > f->samp_cap) {
+        if (f->samp) cudaFree(f->samp);
+        f->samp = nullptr;
+        f->samp_cap = 0;
+        F_CUDA(f, dalloc(&f->samp, need));
+        f->samp_cap = need;
+    }
+    unsigned long long* d_key = f->samp;
+    unsigned long long* d_cnt = f->samp + n;
+    unsigned long long* d_off = f->samp + 2 * n;
+    unsigned long long* d_bs = f->samp + 3 * n;
+    unsigned long long* d_bo = d_bs + nb + 1;
+    unsigned long long* d_tot = d_bo + nb + 1;
+    F_CUDA(f, cudaMemcpyAsync(d_key, cond_key, 8 * n, on_device ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice,
+                              st));
+    const uint2 key = make_uint2(static_cast<uint32_t>(seed), static_cast<uint32_t>(seed >> 32));
+    ntp::sample_count_kernel<<<ntp::blocks_for(n_cond), 256, 0, st>>>(f->knots, f->L, f->K, n_cond, d_key, key,
+                                                                      d_cnt);
+    F_CUDA(f, cudaGetLastError());
+    ntp::scan_block_kernel<<<nb, 1024, 0, st>>>(d_cnt, n_cond, d_off, d_bs);
+    ntp::scan_block_kernel<<<1, 1024, 0, st>>>(d_bs, nb, d_bo, d_bs + nb);  // nb <= 1024
+    F_CUDA(f, cudaMemcpyAsync(d_bo + nb, d_bs + nb, 8, cudaMemcpyDeviceToDevice, st));
+    ntp::scan_add_kernel<<<nb, 1024, 0, st>>>(d_off, n_cond, d_bo, d_tot, nb);
+    F_CUDA(f, cudaGetLastError());
+    unsigned long long total = 0;
+    F_CUDA(f, cudaMemcpyAsync(&total, d_tot, 8, cudaMemcpyDeviceToHost, st));
+    if (counts)
+        F_CUDA(f, cudaMemcpyAsync(counts, d_cnt, 8 * n, on_device ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost,
                                   st));
-        const uint2 key = make_uint2(static_cast<uint32_t>(seed), static_cast<uint32_t>(seed >> 32));
-        ntp::sample_count_kernel<<<ntp::blocks_for(n_cond), 256, 0, st>>>(f->knots, f->L, f->K, n_cond, d_key, key,
-                                                                          d_cnt);
-        F_CUDA(f, cudaGetLastError());
-        ntp::scan_block_kernel<<<nb, 1024, 0, st>>>(d_cnt, n_cond, d_off, d_bs);
-        ntp::scan_block_kernel<<<1, 1024, 0, st>>>(d_bs, nb, d_bo, d_bs + nb);  // nb <= 1024
-        F_CUDA(f, cudaMemcpyAsync(d_bo + nb, d_bs + nb, 8, cudaMemcpyDeviceToDevice, st));
-        ntp::scan_add_kernel<<<nb, 1024, 0, st>>>(d_off, n_cond, d_bo, d_tot, nb);
-        F_CUDA(f, cudaGetLastError());
-        unsigned long long total = 0;
-        F_CUDA(f, cudaMemcpyAsync(&total, d_tot, 8, cudaMemcpyDeviceToHost, st));
-        if (counts)
-            F_CUDA(f, cudaMemcpyAsync(counts, d_cnt, 8 * n, on_device ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost,
-                                      st));
-        F_CUDA(f, cudaStreamSynchronize(st));
-        if (n_hits) *n_hits = total;
-        if (total > capacity) {
-            f->err = "ntp_flow_sample: capacity " + std::to_string(capacity) + " below " + std::to_string(total);
-            return NTP_ERR_OVERFLOW;
-        }
-        if (total == 0) return NTP_OK;
-        if (!hit_cond || !hit_time) return NTP_ERR_INVALID;
-        int32_t* d_hc = hit_cond;
-        float* d_ht = hit_time;
-        void* stage = nullptr;
-        if (!on_device) {
-            F_CUDA(f, cudaMalloc(&stage, 8 * total));
-            d_hc = static_cast<int32_t*>(stage);
-            d_ht = reinterpret_cast<float*>(static_cast<int32_t*>(stage) + total);
-        }
-        const int grid = static_cast<int>(std::min<unsigned long long>((total + 255) / 256, 152ull * 32));
-        cudaError_t e = cudaSuccess;
-        with_bins(f->K, [&](auto kc) {
-            ntp::sample_draw_kernel<decltype(kc)::value>
-                <<<grid, 256, 0, st>>>(f->knots, f->L, n_cond, d_key, key, d_off, total, d_hc, d_ht);
-            e = cudaGetLastError();
-        });
-        if (e == cudaSuccess && !on_device) {
-            e = cudaMemcpyAsync(hit_cond, d_hc, 4 * total, cudaMemcpyDeviceToHost, st);
-            if (e == cudaSuccess) e = cudaMemcpyAsync(hit_time, d_ht, 4 * total, cudaMemcpyDeviceToHost, st);
-        }
-        if (e == cudaSuccess) e = cudaStreamSynchronize(st);
-        if (stage) cudaFree(stage);
-        if (e != cudaSuccess) return ferr(f, e, "ntp_flow_sample");
-        return NTP_OK;
-    };
-    const ntp_status s2 = run();
-    cudaFree(scratch);
-    return s2;
+    F_CUDA(f, cudaStreamSynchronize(st));
+    if (n_hits) *n_hits = total;
+    if (total > capacity) {
+        f->samp_n = n_cond;  // resumable: knots, keys and offsets stay
+        f->samp_key = key;
+        f->samp_total = total;
+        f->err = "ntp_flow_sample: capacity " + std::to_string(capacity) + " below " + std::to_string(total);
+        return NTP_ERR_OVERFLOW;
+    }
+    if (total == 0) return NTP_OK;
+    if (!hit_cond || !hit_time) return NTP_ERR_INVALID;
+    return sample_draw(f, n_cond, key, total, hit_cond, hit_time, on_device);
 }
 
+ntp_status ntp_flow_sample_resume(ntp_flow* f, int32_t* hit_cond, float* hit_time, uint64_t capacity,
+                                  uint64_t* n_hits, int32_t on_device) {
+    if (n_hits) *n_hits = 0;
+    if (!f) return NTP_ERR_INVALID;
+    if (f->samp_n == 0) {
+        f->err = "ntp_flow_sample_resume: no pending sample";
+        return NTP_ERR_NOT_READY;
+    }
+    if (n_hits) *n_hits = f->samp_total;
+    if (f->samp_total > capacity) {
+        f->err = "ntp_flow_sample_resume: capacity " + std::to_string(capacity) + " below " +
+                 std::to_string(f->samp_total);
+        return NTP_ERR_OVERFLOW;
+    }
+    if (!hit_cond || !hit_time) return NTP_ERR_INVALID;
+    F_CUDA(f, cudaSetDevice(f->device));
+    const int n = f->samp_n;
+    f->samp_n = 0;
+    return sample_draw(f, n, f->samp_key, f->samp_total, hit_cond, hit_time, on_device);
+}
 
 ntp_status ntp_flow_evaluate_grid(ntp_flow* f, const float* cond, int32_t n_cond, const float* times, int32_t n_times,
                                   float* logpdf, float* log_expec, int32_t on_device) {

@@ -82,6 +82,7 @@ class RQNormFlow:
             raise _abi.NtpError(st, "ntp_flow_create failed (invalid configuration or CUDA error)")
         self._h = h
         self.batch_capacity = cap
+        self._hits_per_cond = 1.0  # sampled hits per condition of the last sample_hits call
         n_params, n_out, n_pad = C.c_uint64(), C.c_int32(), C.c_int32()
         self._check(self.lib.ntp_flow_get_layout(h, C.byref(n_params), C.byref(n_out), C.byref(n_pad)))
         self.n_params, self.n_outputs, self.n_outputs_padded = n_params.value, n_out.value, n_pad.value
@@ -381,37 +382,44 @@ class RQNormFlow:
                     np.concatenate([p[2] for p in parts]))
         dev = _is_device(cond)
         n_hits = C.c_uint64()
+        # first buffer: from the hits per condition of the previous call; on
+        # an overflow the pending sample is drawn into an exact-size buffer
+        # (ntp_flow_sample_resume: no second conditioner pass)
+        guess = int(capacity if capacity is not None else max(1 << 16, 1.25 * self._hits_per_cond * n + 4096))
         if dev:
             import torch
             cnt = torch.empty(n, dtype=torch.int64, device=cond.device)
-            cap = int(capacity if capacity is not None else 1 << 20)
-            while True:
-                hc = torch.empty(max(cap, 1), dtype=torch.int32, device=cond.device)
-                ht = torch.empty(max(cap, 1), dtype=torch.float32, device=cond.device)
-                torch.cuda.synchronize()
-                st = self.lib.ntp_flow_sample(self._h, cond.data_ptr(), n, keys.data_ptr(), int(seed) & (2 ** 64 - 1),
-                                              cnt.data_ptr(), hc.data_ptr(), ht.data_ptr(), cap, C.byref(n_hits), 1)
-                if st == _abi.NTP_ERR_OVERFLOW and capacity is None:
-                    cap = int(n_hits.value)
-                    continue
-                self._check(st)
+            hc = torch.empty(max(guess, 1), dtype=torch.int32, device=cond.device)
+            ht = torch.empty(max(guess, 1), dtype=torch.float32, device=cond.device)
+            torch.cuda.synchronize()
+            st = self.lib.ntp_flow_sample(self._h, cond.data_ptr(), n, keys.data_ptr(), int(seed) & (2 ** 64 - 1),
+                                          cnt.data_ptr(), hc.data_ptr(), ht.data_ptr(), guess, C.byref(n_hits), 1)
+            if st == _abi.NTP_ERR_OVERFLOW and capacity is None:
                 m = int(n_hits.value)
-                return cnt, hc[:m], ht[:m]
+                hc = torch.empty(m, dtype=torch.int32, device=cond.device)
+                ht = torch.empty(m, dtype=torch.float32, device=cond.device)
+                torch.cuda.synchronize()
+                st = self.lib.ntp_flow_sample_resume(self._h, hc.data_ptr(), ht.data_ptr(), m, C.byref(n_hits), 1)
+            self._check(st)
+            m = int(n_hits.value)
+            self._hits_per_cond = m / max(n, 1)
+            return cnt, hc[:m], ht[:m]
         cond = _f32(cond)
         keys = np.ascontiguousarray(keys, np.uint64)
         cnt = np.empty(n, np.uint64)
-        cap = int(capacity if capacity is not None else 1 << 20)
-        while True:
-            hc = np.empty(max(cap, 1), np.int32)
-            ht = np.empty(max(cap, 1), np.float32)
-            st = self.lib.ntp_flow_sample(self._h, cond.ctypes.data, n, keys.ctypes.data, int(seed) & (2 ** 64 - 1),
-                                          cnt.ctypes.data, hc.ctypes.data, ht.ctypes.data, cap, C.byref(n_hits), 0)
-            if st == _abi.NTP_ERR_OVERFLOW and capacity is None:
-                cap = int(n_hits.value)
-                continue
-            self._check(st)
+        hc = np.empty(max(guess, 1), np.int32)
+        ht = np.empty(max(guess, 1), np.float32)
+        st = self.lib.ntp_flow_sample(self._h, cond.ctypes.data, n, keys.ctypes.data, int(seed) & (2 ** 64 - 1),
+                                      cnt.ctypes.data, hc.ctypes.data, ht.ctypes.data, guess, C.byref(n_hits), 0)
+        if st == _abi.NTP_ERR_OVERFLOW and capacity is None:
             m = int(n_hits.value)
-            return cnt, hc[:m], ht[:m]
+            hc = np.empty(max(m, 1), np.int32)
+            ht = np.empty(max(m, 1), np.float32)
+            st = self.lib.ntp_flow_sample_resume(self._h, hc.ctypes.data, ht.ctypes.data, m, C.byref(n_hits), 0)
+        self._check(st)
+        m = int(n_hits.value)
+        self._hits_per_cond = m / max(n, 1)
+        return cnt, hc[:m], ht[:m]
 
     def __call__(self, x, cond, pred_log_expec: bool = False):
         """The reference's model call (extended_cascade_model.jl:110-125):

@@ -114,18 +114,24 @@ class HybridSimulator:
         if cond.shape[0] and in_domain.any():
             cnt, hc, ht = self.flow.sample_hits(cond, key, seed=self.seed)
             hc64 = hc.long()
-            times = ht + tgeo[hc64]
-            ev_time = torch.as_tensor(np.array([s.time for s in srcs], np.float32), device=times.device)
+            dev = hc.device
+            # per hit, once for the batch: target, PMT and time (residual +
+            # geometric time + the event's time); each event then takes views
+            rows_per_event = torch.as_tensor(np.diff(first.astype(np.int64)), device=dev)
+            ev_of_row = torch.repeat_interleave(torch.arange(len(events), device=dev), rows_per_event,
+                                                output_size=int(first[-1]))
+            ev_time = torch.as_tensor(np.array([s.time for s in srcs], np.float32), device=dev)
+            times = ht + tgeo[hc64] + ev_time[ev_of_row[hc64]]
+            tgt_h, pmt_h = tgt[hc64], pmt[hc64]
             # hits are grouped by condition, conditions by event
-            bounds = torch.searchsorted(hc.contiguous(), torch.as_tensor(first.astype(np.int64), device=hc.device,
+            bounds = torch.searchsorted(hc.contiguous(), torch.as_tensor(first.astype(np.int64), device=dev,
                                                                          dtype=torch.int32))
             b = bounds.cpu().numpy()
             for i in range(len(events)):
                 if not in_domain[i]:
                     continue
                 sl = slice(int(b[i]), int(b[i + 1]))
-                out[i] = EventHits(ids[i], "flow", int(b[i + 1] - b[i]), tgt[hc64[sl]], pmt[hc64[sl]],
-                                   times[sl] + ev_time[i])
+                out[i] = EventHits(ids[i], "flow", int(b[i + 1] - b[i]), tgt_h[sl], pmt_h[sl], times[sl])
         for i in range(len(events)):
             if out[i] is None:
                 out[i] = self.mc_event(ids[i], srcs[i])

@@ -161,3 +161,37 @@ def test_ks_check_hands_later_events_to_mc():
         assert n_mc >= (1.36 / 0.1) ** 2 and ks > 0.1 and sim.fallback
         later = sim.simulate(events[1:])
     assert [o.method for o in later] == ["mc", "mc"]
+
+
+def test_sample_resume_after_overflow():
+    """A sample whose hits overflow the buffer is drawn by
+    ntp_flow_sample_resume into a larger one: the same counts and hits as one
+    call with room enough; a resume without a pending sample is refused."""
+    import ctypes as C
+
+    from neutrinotelescopes_gb300 import _abi
+    rng = np.random.default_rng(8)
+    n = 3000
+    cond = torch.as_tensor(rng.uniform(-1, 1, (n, 5)).astype(np.float32), device="cuda")
+    keys = torch.as_tensor(rng.integers(0, 2 ** 62, n), dtype=torch.int64, device="cuda")
+    with _flow(math.log(4.0)) as fl:
+        cnt, hc, ht = fl.sample_hits(cond, keys, seed=5, capacity=1 << 20)
+        total = int(hc.numel())
+        assert total > 1000
+        lib, h = fl.lib, fl._h
+        n_hits = C.c_uint64()
+        cnt2 = torch.empty(n, dtype=torch.int64, device="cuda")
+        small = torch.empty(16, dtype=torch.int32, device="cuda"), torch.empty(16, dtype=torch.float32, device="cuda")
+        torch.cuda.synchronize()
+        st = lib.ntp_flow_sample(h, cond.data_ptr(), n, keys.data_ptr(), 5, cnt2.data_ptr(), small[0].data_ptr(),
+                                 small[1].data_ptr(), 16, C.byref(n_hits), 1)
+        assert st == _abi.NTP_ERR_OVERFLOW and n_hits.value == total
+        assert torch.equal(cnt2, cnt)
+        hc2 = torch.empty(total, dtype=torch.int32, device="cuda")
+        ht2 = torch.empty(total, dtype=torch.float32, device="cuda")
+        st = lib.ntp_flow_sample_resume(h, hc2.data_ptr(), ht2.data_ptr(), total, C.byref(n_hits), 1)
+        assert st == _abi.NTP_OK and n_hits.value == total
+        assert torch.equal(hc2, hc) and torch.equal(ht2, ht)
+        # consumed: a second resume has nothing pending
+        st = lib.ntp_flow_sample_resume(h, hc2.data_ptr(), ht2.data_ptr(), total, C.byref(n_hits), 1)
+        assert st == _abi.NTP_ERR_NOT_READY
