@@ -301,12 +301,13 @@ def flow_bench(train_steps: int = 300, n_tuples: int = 100_000_000) -> dict:
     return out
 
 
-def hybrid_bench(n_events: int = 10_000, batch: int = 256, train_steps: int = 12_000) -> dict:
+def hybrid_bench(n_events: int = 10_000, batch: int = 256, train_steps: int = 48_000) -> dict:
     """Hybrid serving workload: 10 x 10 strings x 80 POM modules x 16 PMTs
     (50 m, 15 m spacing), n_events cascades with E log-uniform 1e2-1e6 GeV,
     vertex uniform in the detector's bounding box, isotropic direction.  The
-    flow (trained here on an MC table of 4096 simulations, each PMT's count
-    entering the loss once) supplies every
+    flow (trained here on an MC table of 8192 simulations, half of them
+    drawn 8-80 m from the module near the Cherenkov angle, each PMT's count
+    weighted by the hits simulated for it) supplies every
     PMT within 1-200 m of the vertex; events with a module closer than 1 m go
     to plain MC.  Reported: events/s and per-event latency of the saturated
     stream (batches of `batch` events), plain MC's events/s on the same
@@ -325,7 +326,12 @@ def hybrid_bench(n_events: int = 10_000, batch: int = 256, train_steps: int = 12
 
     out = {"workload": f"{n_events} cascades 1e2-1e6 GeV, 10 x 10 strings x 80 modules x 16 PMTs (50 m, 15 m), "
                        "simple water; flow for PMTs 1-200 m from the vertex, MC for events with a module < 1 m"}
-    tab = make_flow_table(TableConfig(n_sims=4096, n_orientations=16, target_hits=300, max_photons=10_000_000, seed=1))
+    tcfg = TableConfig(n_sims=8192, n_orientations=16, target_hits=1000, max_photons=100_000_000, seed=2,
+                       focus_fraction=0.5)
+    t0 = time.perf_counter()
+    tab = make_flow_table(tcfg)
+    torch.cuda.synchronize()
+    t_table = time.perf_counter() - t0
     fl = RQNormFlow(RQNormFlowHParams(batch_size=8192), batch_capacity=65536)
     fl.init_from_table(tab)
     per = len(tab) // 8192
@@ -333,9 +339,12 @@ def hybrid_bench(n_events: int = 10_000, batch: int = 256, train_steps: int = 12
     t0 = time.perf_counter()
     while done < train_steps:
         fl.set_lr(1e-5 + 0.5 * (1e-3 - 1e-5) * (1 + _m.cos(_m.pi * done / train_steps)))
-        done += len(fl.fit_table(tab, epochs=1, seed=ep, max_steps=min(per, train_steps - done), count_once=True))
+        done += len(fl.fit_table(tab, epochs=1, seed=ep, max_steps=min(per, train_steps - done),
+                                 count_mode="information"))
         ep += 1
-    out["training"] = {"table_rows": len(tab), "steps": done, "seconds": time.perf_counter() - t0}
+    out["training"] = {"table_simulations": tcfg.n_sims, "table_photons": int(tab.n_photons),
+                       "table_rows": len(tab), "table_seconds": t_table, "steps": done,
+                       "count_mode": "information", "seconds": time.perf_counter() - t0}
     del tab
     torch.cuda.empty_cache()
     setup = workloads.hybrid_setup()

@@ -212,28 +212,41 @@ class RQNormFlow:
         self.init_output_bias(shift=shift, log_expec=log_n)
 
     def fit_table(self, table, *, epochs: int = 1, batch_size: int | None = None, seed: int = 0,
-                  max_steps: int | None = None, count_once: bool = False) -> list[float]:
+                  max_steps: int | None = None, count_once: bool = False,
+                  count_mode: str | None = None) -> list[float]:
         """Trains on a FlowTable held in device memory: the rows are shuffled
         on the device once per epoch and fed to the training step batch by
         batch without leaving the GPU; returns the per-step losses.
-        count_once: every row's count term weighted by 1 / (rows of its PMT),
-        so that each PMT's count enters the loss once.  The reference's
-        tables repeat a PMT's count on each of its rows (False, the
-        default), which weights a PMT by its number of rows; for small
-        counts the rows grow with the count itself."""
+
+        count_mode selects the count term:
+          "rows" (the default): the reference's tables, every row carries
+            its PMT's drawn count, which weights a PMT by its number of
+            rows; for small counts the rows grow with the count itself.
+          "once" (or count_once=True): every row's count term weighted by
+            1 / (rows of its PMT), so that each PMT's count enters once.
+          "information": each PMT once, weighted by the hits simulated for
+            it, with its MC expectation as the target
+            (FlowTable.information_weights)."""
         import torch
+        mode = count_mode or ("once" if count_once else "rows")
+        if mode not in ("rows", "once", "information"):
+            raise ValueError(f"unknown count_mode {mode!r}")
         n = len(table)
         bs = int(batch_size or self.hparams.batch_size)
         bs = max(128, min(bs, self.batch_capacity) // 128 * 128)
         gen = torch.Generator(device=table.tres.device)
         gen.manual_seed(int(seed))
-        cw_all = table.count_once_weights() if count_once else None
+        cw_all, nh_all = None, table.nhits
+        if mode == "once":
+            cw_all = table.count_once_weights()
+        elif mode == "information":
+            cw_all, nh_all = table.information_weights()
         losses: list[float] = []
         for _ in range(epochs):
             perm = torch.randperm(n, device=table.tres.device, generator=gen)
             cond = table.cond[perm].contiguous()
             tres = table.tres[perm].contiguous()
-            nh = table.nhits[perm].contiguous()
+            nh = nh_all[perm].contiguous()
             has = table.has_time[perm].contiguous()
             cw = cw_all[perm].contiguous() if cw_all is not None else None
             torch.cuda.synchronize()

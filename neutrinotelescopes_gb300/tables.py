@@ -46,6 +46,17 @@ class TableConfig:
     downsample: float = 1.0
     module_radius: float = 0.21
     seed: int = 7
+    # a fraction of the simulations drawn from a narrower region instead
+    # (distance log-uniform over focus_distance, cos theta of the source
+    # direction uniform over focus_cos_theta): the light of an event comes
+    # mostly from modules 10-60 m away near the Cherenkov angle (the source
+    # direction's cos theta about -0.74 relative to the module -> source
+    # axis), where a uniform table holds few simulations.  The flow is
+    # conditional on the features, so where its data lie moves its accuracy
+    # but does not bias it.
+    focus_fraction: float = 0.0
+    focus_distance: tuple = (8.0, 80.0)
+    focus_cos_theta: tuple = (-0.95, -0.5)
 
 
 @dataclass
@@ -64,6 +75,7 @@ class FlowTable:
     n_hits: int = 0
     meta: dict = field(default_factory=dict)
     row_group: object = None   # group index of every row
+    sim_scale: object = None   # per simulation: emitted / simulated photons (the weight scale of its hits)
 
     def __len__(self) -> int:
         return int(self.tres.shape[0])
@@ -78,10 +90,45 @@ class FlowTable:
         n = torch.bincount(rg, minlength=int(self.group_cond.shape[0]))
         return (1.0 / n[rg].to(torch.float32)).contiguous()
 
+    def information_weights(self):
+        """Per-row count weights and count targets of the information-weighted
+        count loss: (weight, target) float32 tensors on the table's device.
+
+        A group's MC expectation is its simulation's weighted hits times the
+        simulation's scale s (emitted / simulated photons), so its variance
+        is about s times the expectation: the group's information on log
+        lambda is the expectation / s, its simulated (weighted) hits.  The
+        Poisson term c (N log lambda - lambda) with c = 1 / s and N = the
+        expectation has exactly that curvature at its minimum, so each group
+        pulls on the fit in proportion to the hits simulated for it, instead
+        of in proportion to lambda, which spans about ten decades over the
+        table (the reference's per-row Poisson term, dominated by the
+        brightest PMTs).  Each group enters once (its c is split over its
+        rows); the c are scaled to a mean of 1 over the groups, so the count
+        term's total weight equals count_once's.  The target is the
+        expectation itself rather than a Poisson draw of it, which would add
+        noise on top of the simulation's own."""
+        import torch
+        if self.row_group is None or self.sim_scale is None:
+            raise ValueError("the table needs row_group and sim_scale")
+        G = int(self.group_cond.shape[0])
+        S = int(self.sim_scale.shape[0])
+        if S == 0 or G % S:
+            raise ValueError(f"{G} groups do not split into {S} simulations")
+        dev = self.row_group.device
+        c_sim = 1.0 / torch.as_tensor(self.sim_scale, dtype=torch.float64, device=dev)
+        c = c_sim.repeat_interleave(G // S)
+        c = c / c.mean()
+        rg = self.row_group.long()
+        rows = torch.bincount(rg, minlength=G).to(torch.float64)
+        w = (c[rg] / rows[rg]).to(torch.float32).contiguous()
+        target = self.group_expec.to(dev)[rg].to(torch.float32).contiguous()
+        return w, target
+
     def save(self, path) -> None:
         np.savez(path, **{k: getattr(self, k).cpu().numpy() for k in
                           ("cond", "tres", "nhits", "has_time", "group_cond", "group_expec", "group_count",
-                           "row_group") if getattr(self, k) is not None},
+                           "row_group", "sim_scale") if getattr(self, k) is not None},
                  n_photons=self.n_photons, n_hits=self.n_hits,
                  meta=np.array([repr(sorted(self.meta.items()))]))
 
@@ -90,8 +137,8 @@ class FlowTable:
         import torch
         z = np.load(path)
         t = {k: torch.as_tensor(z[k]).to(device) for k in
-             ("cond", "tres", "nhits", "has_time", "group_cond", "group_expec", "group_count", "row_group")
-             if k in z.files}
+             ("cond", "tres", "nhits", "has_time", "group_cond", "group_expec", "group_count", "row_group",
+              "sim_scale") if k in z.files}
         return cls(**t, n_photons=int(z["n_photons"]), n_hits=int(z["n_hits"]))
 
 
@@ -117,6 +164,11 @@ def draw_simulations(cfg: TableConfig, rng: np.random.Generator):
     ct = rng.uniform(-1.0, 1.0, S)
     phi = rng.uniform(0.0, 2 * np.pi, S)
     le = rng.uniform(cfg.log10_energy[0], cfg.log10_energy[1], S)
+    if cfg.focus_fraction > 0:
+        f = rng.uniform(0.0, 1.0, S) < cfg.focus_fraction
+        nf = int(f.sum())
+        d[f] = np.exp(rng.uniform(np.log(cfg.focus_distance[0]), np.log(cfg.focus_distance[1]), nf))
+        ct[f] = rng.uniform(cfg.focus_cos_theta[0], cfg.focus_cos_theta[1], nf)
     st = np.sqrt(1.0 - ct * ct)
     dirs = np.stack([st * np.cos(phi), st * np.sin(phi), ct], -1)
     e = 10.0 ** le
@@ -211,7 +263,8 @@ def make_flow_table(cfg: TableConfig | None = None, medium=None, spectrum=None, 
         break
     m = int(n_rows.value)
     meta = dict(n_sims=cfg.n_sims, n_orientations=R, seed=cfg.seed, photons_per_gev=cfg.photons_per_gev)
-    table = FlowTable(cond[:m], tres[:m], nh[:m], has[:m], gcond, gexp, gcnt, n_phot, n, meta, rg[:m])
+    table = FlowTable(cond[:m], tres[:m], nh[:m], has[:m], gcond, gexp, gcnt, n_phot, n, meta, rg[:m],
+                      torch.as_tensor(scale, device=dev))
     table.sims = sims
     table.hits = hits[: n * 64]
     table.weights = w[:n]

@@ -20,3 +20,28 @@ def test_count_once_weights():
     np.testing.assert_allclose(np.bincount(rg.numpy(), weights=w), [1.0, 0.0, 1.0, 1.0])
     with pytest.raises(ValueError):
         FlowTable(t.cond, t.tres, t.nhits, t.has_time, t.group_cond, t.group_expec, t.group_count).count_once_weights()
+
+
+def test_information_weights():
+    # 2 simulations x 2 groups; simulation 0 oversampled 4x (scale 0.25), simulation 1 scale 4
+    rg = torch.tensor([0, 0, 1, 2, 3, 3, 3], dtype=torch.int32)
+    n = rg.numel()
+    gexp = torch.tensor([8.0, 2.0, 40.0, 0.0], dtype=torch.float64)
+    t = FlowTable(torch.zeros((n, 5)), torch.zeros(n), torch.zeros(n), torch.ones(n, dtype=torch.int32),
+                  torch.zeros((4, 5)), gexp, torch.zeros(4, dtype=torch.int64), row_group=rg,
+                  sim_scale=torch.tensor([0.25, 4.0], dtype=torch.float64))
+    w, target = t.information_weights()
+    c = np.array([4.0, 4.0, 0.25, 0.25])
+    c /= c.mean()
+    rows = np.bincount(rg.numpy(), minlength=4)
+    np.testing.assert_allclose(w.numpy(), c[rg.numpy()] / rows[rg.numpy()], rtol=1e-6)
+    # every group's weights sum to its c; the c average to one over the groups
+    np.testing.assert_allclose(np.bincount(rg.numpy(), weights=w.numpy()), c, rtol=1e-6)
+    np.testing.assert_allclose(target.numpy(), gexp.numpy()[rg.numpy()])
+    # the count term's curvature at its minimum (c times the expectation) is the
+    # simulated weighted hits, expectation / scale, up to the common factor
+    info = np.bincount(rg.numpy(), weights=(w * target).numpy())
+    np.testing.assert_allclose(info / info[0], (gexp.numpy() / np.array([0.25, 0.25, 4, 4])) / 32.0, rtol=1e-6)
+    with pytest.raises(ValueError):
+        FlowTable(t.cond, t.tres, t.nhits, t.has_time, t.group_cond, t.group_expec, t.group_count,
+                  row_group=rg).information_weights()
