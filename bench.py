@@ -389,7 +389,8 @@ def hybrid_bench(n_events: int = 10_000, batch: int = 256, train_steps: int = 48
                                        "log10_energy": float(events[worst][2])}}
     # the KS check of the hybrid mode: every 25th flow event also through
     # (oversampled) MC, one-sample KS against the flow's predicted hit-time
-    # distribution; plain MC from the first decisive check above 0.02 on
+    # distribution; plain MC from the first check whose distance, less the
+    # MC sample's own 95 % noise bound, is above 0.02
     chk = HybridSimulator(setup, fl, seed=workloads.SEED_BASE + 6, ks_check_every=25, ks_threshold=0.02)
     chk_events = [e for e in events if e[2] <= 4.0][:100]
     t1 = time.perf_counter()
@@ -397,8 +398,10 @@ def hybrid_bench(n_events: int = 10_000, batch: int = 256, train_steps: int = 48
     for s0 in range(0, len(chk_events), 25):
         res_chk += chk.simulate(chk_events[s0:s0 + 25])
     out["ks_check"] = {"threshold": 0.02, "every": 25, "events": len(chk_events),
+                       "confidence": chk.ks_confidence,
                        "checks": [{"event": int(a), "ks": float(b), "mc_hits": int(c),
-                                   "decisive": bool(c >= (1.36 / 0.02) ** 2)} for a, b, c in chk.checks],
+                                   "mc_noise_bound": chk.ks_noise_bound(c), "fails": chk.ks_fails(b, c)}
+                                  for a, b, c in chk.checks],
                        "fell_back_to_mc": chk.fallback,
                        "events_mc": int(sum(r.method == "mc" for r in res_chk)),
                        "seconds": time.perf_counter() - t1}
@@ -430,13 +433,13 @@ def hybrid_bench(n_events: int = 10_000, batch: int = 256, train_steps: int = 48
     out["speedup_vs_plain_mc"] = out["saturated"]["events_per_s"] / out["plain_mc"]["events_per_s"]
     # error against MC on sample events
     errs, ksm, ksp, kspred = [], [], [], []
-    for e in [e for e in events if 3.0 <= e[2] <= 4.0][:6]:
-        c = compare(sim, e[1], e[2], e[0], seed=e[0])
+    for e in [e for e in events if 3.0 <= e[2] <= 4.0][:10]:
+        c = compare(sim, e[1], e[2], e[0], seed=e[0], oversample=8)
         if c.get("modules"):
             errs.extend(list(c["expected_rel_err"]))
             ksm.extend(list(c["ks_modules"]))
             ksp.append(c["ks_pooled"])
-            kspred.append((c["ks_predicted"], c["ks_predicted_mc_hits"]))
+            kspred.append((c["ks_predicted"], c["ks_predicted_mc_hits"], c["ks_predicted_bound"]))
     errs, ksm = np.abs(np.array(errs)), np.array(ksm)
     out["error_vs_mc"] = {"ks_threshold_of_the_mc_fallback": 0.02,
                           "events": len(ksp), "modules_expected_ge_100": int(errs.size),
@@ -444,11 +447,14 @@ def hybrid_bench(n_events: int = 10_000, batch: int = 256, train_steps: int = 48
                           "expected_hits_rel_err_p90": float(np.quantile(errs, 0.9)) if errs.size else None,
                           "ks_per_module_median": float(np.median(ksm)) if ksm.size else None,
                           "ks_pooled_median": float(np.median(ksp)) if ksp else None,
-                          "ks_predicted": [{"ks": float(a), "mc_hits": int(b)} for a, b in kspred],
-                          "ks_predicted_median": float(np.median([a for a, _ in kspred])) if kspred else None,
-                          "note": "ks_pooled: flow sample vs MC sample of the event (both ~1e3 hits, noise "
-                                  "~0.03); ks_predicted: oversampled MC hits vs the flow's predicted "
-                                  "hit-time CDF (noise ~0.87/sqrt(mc_hits))"}
+                          "ks_predicted": [{"ks": float(a), "mc_hits": int(b), "mc_noise_bound": float(d)}
+                                           for a, b, d in kspred],
+                          "ks_predicted_median": float(np.median([a for a, _, _ in kspred])) if kspred else None,
+                          "note": "expected hits: MC of 8x the event's photons (sum of weights / 8), modules "
+                                  "with >= 100 expected hits; ks_pooled: flow sample vs MC sample of the event "
+                                  "(~1e3 flow hits, noise ~0.03); ks_predicted: oversampled MC hits vs the "
+                                  "flow's predicted hit-time CDF (MC noise ~0.87/sqrt(mc_hits), 95 % bound "
+                                  "mc_noise_bound)"}
     setup.close()
     fl.close()
     return out

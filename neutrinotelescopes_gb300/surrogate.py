@@ -30,6 +30,18 @@ from .photon_prop import (PhotonPropSetup, _check, calc_total_weight, make_hits_
                           propagate_photons, resample_simulation)
 
 
+def ks_noise_bound(n: int, confidence: float) -> float:
+    """eps(n) with P(sup |F_n - F| > eps) <= 1 - confidence for the
+    empirical CDF F_n of n samples of F: the Dvoretzky-Kiefer-Wolfowitz
+    inequality with Massart's constant, eps = sqrt(ln(2 / (1 - confidence))
+    / (2 n)); 0 for confidence 0, infinite without samples."""
+    if confidence <= 0.0:
+        return 0.0
+    if n <= 0:
+        return math.inf
+    return math.sqrt(math.log(2.0 / (1.0 - confidence)) / (2.0 * n))
+
+
 @dataclass
 class EventHits:
     event_id: int
@@ -45,16 +57,24 @@ class HybridSimulator:
 
     def __init__(self, setup: PhotonPropSetup, flow: RQNormFlow, *, d_range=(1.0, 200.0),
                  log10_energy_range=(2.0, 6.0), seed: int = 0, ks_check_every: int = 0,
-                 ks_threshold: float = 0.02, ks_min_hits: int = 20_000, ks_max_photons: float = 2e10):
+                 ks_threshold: float = 0.02, ks_min_hits: int = 40_000, ks_max_photons: float = 2e10,
+                 ks_confidence: float = 0.95):
         """ks_check_every > 0: every that many flow-served events one is also
         simulated with plain MC (``ks_check``): the one-sample
-        Kolmogorov-Smirnov distance of the MC hit times from the flow's
+        Kolmogorov-Smirnov distance D of the MC hit times from the flow's
         predicted hit-time distribution of the event.  The MC run is
         oversampled towards ks_min_hits hits (at most ks_max_photons photons)
-        so that its own noise stays below the threshold; a check with enough
-        hits for a decision (a perfect surrogate below the threshold at 95 %
-        confidence) and a distance above ks_threshold hands every later
-        event to plain MC."""
+        so that its own noise stays small next to the threshold.
+
+        D measures the surrogate's distance from the MC's true hit-time
+        distribution plus the MC sample's own deviation from it, which the
+        Dvoretzky-Kiefer-Wolfowitz inequality bounds by
+        eps(n) = sqrt(ln(2 / (1 - ks_confidence)) / (2 n)) with probability
+        ks_confidence (0.0068 at 40 000 hits and 95 %).  A check fails when
+        D - eps(n) > ks_threshold, i.e. when the surrogate's own distance is
+        above the threshold at that confidence, and hands every later event
+        to plain MC.  ks_confidence = 0 compares D itself with the
+        threshold."""
         self.setup = setup
         self.flow = flow
         self.d_range = (float(d_range[0]), float(d_range[1]))
@@ -64,6 +84,7 @@ class HybridSimulator:
         self.ks_threshold = float(ks_threshold)
         self.ks_min_hits = int(ks_min_hits)
         self.ks_max_photons = float(ks_max_photons)
+        self.ks_confidence = float(ks_confidence)
         self.fallback = False
         self.checks: list[tuple[int, float, int]] = []   # (event id, KS distance, MC hits)
         self._served = 0
@@ -140,10 +161,19 @@ class HybridSimulator:
                 if self._served % self.ks_check_every == 0:
                     ks, n_mc = self.ks_check(ids[i], srcs[i], float(le[i]))
                     self.checks.append((ids[i], ks, n_mc))
-                    decisive = n_mc >= (1.36 / self.ks_threshold) ** 2
-                    if decisive and not (ks <= self.ks_threshold):
+                    if self.ks_fails(ks, n_mc):
                         self.fallback = True
         return out
+
+    def ks_noise_bound(self, n_mc: int) -> float:
+        """ks_noise_bound(n_mc, ks_confidence)."""
+        return ks_noise_bound(n_mc, self.ks_confidence)
+
+    def ks_fails(self, ks: float, n_mc: int) -> bool:
+        """True when a check of distance ks from n_mc MC hits shows the
+        surrogate above ks_threshold (a NaN distance, an event without
+        MC hits, decides nothing)."""
+        return bool(ks - self.ks_noise_bound(n_mc) > self.ks_threshold)
 
     def ks_check(self, event_id: int, source, log10_energy: float) -> tuple[float, int]:
         """One-sample KS distance of plain-MC hit times (modules in the
@@ -250,15 +280,18 @@ def ks_statistic(a: np.ndarray, b: np.ndarray) -> float:
 
 
 def compare(sim: HybridSimulator, source, log10_energy: float, event_id: int, *, seed: int = 0,
-            min_hits: int = 100) -> dict:
+            min_hits: int = 100, oversample: int = 1) -> dict:
     """Surrogate against plain MC for one event: per-module expected hits
-    (flow count head vs sum of MC weights) and arrival times (two-sample KS
-    per module with at least min_hits hits in both, and pooled over the
+    (flow count head vs sum of MC weights, from an MC run of `oversample`
+    times the event's photons divided by it) and arrival times (two-sample
+    KS per module with at least min_hits hits in both, and pooled over the
     event), plus the one-sample KS of an oversampled MC run against the
     flow's predicted hit-time distribution (``HybridSimulator.ks_check``,
     free of the flow sample's noise)."""
     import torch
-    truth = mc_truth(sim.setup, source, seed=seed)
+    k = max(1, int(oversample))
+    truth = mc_truth(sim.setup, dataclasses.replace(source, photons=int(source.photons) * k), seed=seed)
+    truth["expected"] = truth["expected"] / k
     cond, key, tgeo, tgt, pmt, first, close = sim.conditions([source], [log10_energy], [event_id])
     if cond.shape[0] == 0:
         return {"modules": 0}
@@ -286,7 +319,8 @@ def compare(sim: HybridSimulator, source, log10_energy: float, event_id: int, *,
     return {"modules": len(rel), "expected_rel_err": np.array(rel), "ks_modules": np.array(ks_mod),
             "ks_pooled": ks_statistic(truth["time"], ft), "mc_hits": int(truth["time"].size),
             "flow_hits": int(ft.size), "method": ev.method,
-            "ks_predicted": ks_pred, "ks_predicted_mc_hits": n_pred}
+            "ks_predicted": ks_pred, "ks_predicted_mc_hits": n_pred,
+            "ks_predicted_bound": sim.ks_noise_bound(n_pred)}
 
 
 def hybrid_events(n: int, setup: PhotonPropSetup, *, seed: int = 4, log10_energy=(2.0, 6.0),

@@ -1,0 +1,33 @@
+"""The noise bound of the hybrid mode's KS check (surrogate.ks_noise_bound):
+the Dvoretzky-Kiefer-Wolfowitz bound on the KS distance of an empirical CDF
+from its own distribution, and how often samples of a perfect surrogate
+exceed it."""
+import math
+
+import numpy as np
+
+from neutrinotelescopes_gb300.surrogate import ks_noise_bound
+
+
+def test_bound_values():
+    assert math.isclose(ks_noise_bound(40_000, 0.95), math.sqrt(math.log(40.0) / 80_000), rel_tol=1e-12)
+    assert abs(ks_noise_bound(40_000, 0.95) - 0.00679) < 1e-5
+    assert ks_noise_bound(40_000, 0.0) == 0.0
+    assert ks_noise_bound(0, 0.95) == math.inf
+    assert ks_noise_bound(10_000, 0.99) > ks_noise_bound(10_000, 0.95) > ks_noise_bound(40_000, 0.95)
+
+
+def test_perfect_samples_exceed_the_bound_rarely():
+    """n uniform samples against the uniform CDF: the KS distance exceeds
+    eps(n) in at most 5 % of the trials at 95 % confidence (the bound is
+    conservative: about 4 % here)."""
+    rng = np.random.default_rng(3)
+    n, trials = 2000, 1000
+    eps = ks_noise_bound(n, 0.95)
+    i = np.arange(1, n + 1)
+    over = 0
+    for _ in range(trials):
+        u = np.sort(rng.uniform(size=n))
+        d = max(np.max(i / n - u), np.max(u - (i - 1) / n))
+        over += d > eps
+    assert over / trials <= 0.05 + 3 * math.sqrt(0.05 * 0.95 / trials)

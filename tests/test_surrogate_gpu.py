@@ -147,18 +147,19 @@ def test_sampled_hits_follow_the_predicted_cdf():
 
 def test_ks_check_hands_later_events_to_mc():
     """A surrogate far from the MC (an untrained flow) fails its first
-    decisive check: the check's MC run is oversampled towards ks_min_hits
-    (here up to the photon cap, rescaled from the hits of a first run), and
-    every later event goes to plain MC."""
+    check: the check's MC run is oversampled towards ks_min_hits (here up
+    to the photon cap, rescaled from the hits of a first run), its distance
+    less the MC sample's 95 % noise bound is above the threshold, and every
+    later event goes to plain MC."""
     setup = _setup()
     events = [(i, _cascade((5.0, 3.0, 10.0 + i), (0.0, 0.0, 1.0), e=200.0), 2.3) for i in range(3)]
     with _flow(math.log(3.0)) as fl:
         sim = HybridSimulator(setup, fl, ks_check_every=1, ks_threshold=0.1, ks_min_hits=100_000,
-                              ks_max_photons=2e9)
+                              ks_max_photons=1e10)
         first = sim.simulate(events[:1])
         assert first[0].method == "flow" and len(sim.checks) == 1
         _, ks, n_mc = sim.checks[0]
-        assert n_mc >= (1.36 / 0.1) ** 2 and ks > 0.1 and sim.fallback
+        assert n_mc >= (1.36 / 0.1) ** 2 and ks - sim.ks_noise_bound(n_mc) > 0.1 and sim.fallback
         later = sim.simulate(events[1:])
     assert [o.method for o in later] == ["mc", "mc"]
 
