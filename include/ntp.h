@@ -447,7 +447,11 @@ ntp_status ntp_flow_train_step(ntp_flow* flow, const float* cond, const float* t
    step).  count_weight (may be NULL = 1 for every row) multiplies each row's
    Poisson count term: -(sum logpdf + sum c_i Poisson(n_i; exp(le_i))) / B;
    with c = 1 / (rows of the PMT) every PMT's count enters once (the
-   reference's tables repeat it on each of the PMT's rows).  The training
+   reference's tables repeat it on each of the PMT's rows); with c = the
+   PMT's simulated photons per emitted photon over its rows and nhits = its
+   MC expectation, every PMT pulls in proportion to the hits simulated for
+   it (the information-weighted count term).  nhits need not be an
+   integer.  The training
    step itself is captured once as a CUDA graph and replayed
    (NTP_FLOW_GRAPH=0 in the environment runs it eagerly). */
 ntp_status ntp_flow_train_steps(ntp_flow* flow, const float* cond, const float* tres, const float* nhits,
