@@ -433,7 +433,7 @@ def hybrid_bench(n_events: int = 10_000, batch: int = 256, train_steps: int = 48
     out["speedup_vs_plain_mc"] = out["saturated"]["events_per_s"] / out["plain_mc"]["events_per_s"]
     # error against MC on sample events
     errs, ksm, ksp, kspred = [], [], [], []
-    for e in [e for e in events if 3.0 <= e[2] <= 4.0][:10]:
+    for e in [e for e in events if 3.0 <= e[2] <= 4.0][:14]:
         c = compare(sim, e[1], e[2], e[0], seed=e[0], oversample=8)
         if c.get("modules"):
             errs.extend(list(c["expected_rel_err"]))

@@ -45,3 +45,23 @@ def test_information_weights():
     with pytest.raises(ValueError):
         FlowTable(t.cond, t.tres, t.nhits, t.has_time, t.group_cond, t.group_expec, t.group_count,
                   row_group=rg).information_weights()
+
+
+def test_focus_draws():
+    """TableConfig.focus_fraction: that fraction of the simulations (about)
+    drawn over focus_distance and focus_cos_theta; energies, azimuths and
+    the other simulations as without it (the same generator stream)."""
+    from neutrinotelescopes_gb300.tables import TableConfig, draw_simulations
+    cfg = TableConfig(n_sims=4000, seed=3)
+    a = draw_simulations(cfg, np.random.default_rng(3))
+    b = draw_simulations(TableConfig(n_sims=4000, seed=3, focus_fraction=0.5), np.random.default_rng(3))
+    moved = a["distance"] != b["distance"]
+    assert abs(moved.mean() - 0.5) < 0.04
+    assert np.all((b["distance"][moved] >= 8.0) & (b["distance"][moved] <= 80.0))
+    assert np.all((b["cos_theta"][moved] >= -0.95) & (b["cos_theta"][moved] <= -0.5))
+    np.testing.assert_array_equal(a["cos_theta"][~moved], b["cos_theta"][~moved])
+    np.testing.assert_array_equal(a["log10_energy"], b["log10_energy"])
+    np.testing.assert_array_equal(a["phi"], b["phi"])
+    # photons per simulation follow the distance: the focus simulations reach
+    # the hit target up to the cap
+    assert np.all(b["n_simulated"] >= cfg.min_photons) and np.all(b["n_simulated"] <= cfg.max_photons)
