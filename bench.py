@@ -76,7 +76,8 @@ def parse():
     ap.add_argument("--flow", type=int, default=1, help="1: include the flow surrogate measurement")
     ap.add_argument("--legs", default="propagation,serving,flow,hybrid",
                     help="comma list of the measurements to run: propagation (the headline line), serving, flow, "
-                         "hybrid")
+                         "hybrid; compat (the bench cascades in the reference's own water, not in the default "
+                         "list) runs when propagation is not among them")
     ap.add_argument("--small", action="store_true",
                     help="profiling case: one cascade at 1% of its photons, 64 MB hit buffer, 256 MB L2 flush")
     return ap.parse_args()
@@ -299,6 +300,68 @@ def flow_bench(train_steps: int = 300, n_tuples: int = 100_000_000) -> dict:
     del tab, cond, tres, nh, has, c, idx, tt, lp, lpg
     torch.cuda.empty_cache()
     return out
+
+
+def compat_bench(steps: int = 3, photon_scale: float = 0.25) -> dict:
+    """The bench workload's cascades (at photon_scale of their photons) on
+    the same 20-module string in the reference's own water: Cascadia Basin
+    optics (Quan-Fry dispersion with the reference's coefficients, Kopper
+    scattering, STRAW absorption as a per-hit weight, pure Henyey-Greenstein
+    with g = 0.99) and its Frank-Tamm spectrum on 300-800 nm as a 30-knot
+    texture table.  Device photons/s (CUDA events, L2 flushed between
+    steps)."""
+    import numpy as np
+    import torch
+
+    from neutrinotelescopes_gb300 import _abi, workloads
+    from neutrinotelescopes_gb300.detection import string_of_modules
+    from neutrinotelescopes_gb300.medium import make_cascadia_medium_properties
+    from neutrinotelescopes_gb300.photon_prop import PhotonPropSetup, pack_sources
+    from neutrinotelescopes_gb300.spectrum import CherenkovSpectrum
+
+    medium = make_cascadia_medium_properties(0.99)
+    srcs = workloads.cascade_sources(N_CASCADES, np.random.default_rng(WORKLOAD_SEED), photon_scale=photon_scale)
+    setup = PhotonPropSetup(srcs, string_of_modules(20, 15.0, pmt_area=workloads.PMT_AREA), medium,
+                            CherenkovSpectrum((300.0, 800.0), 30, medium))
+    lib, ctx = setup.context()
+    psrc = pack_sources(setup.sources)
+    photons = sum(int(s.photons) for s in setup.sources)
+    cap = 1 << 24
+    hits = torch.empty((cap, 64), dtype=torch.uint8, device="cuda")
+    flush = torch.empty(512 << 20, dtype=torch.uint8, device="cuda")
+    stream = torch.cuda.current_stream()
+    opts = setup.prop_opts(stream=stream.cuda_stream)
+    nh, ns = C.c_uint64(), C.c_uint64()
+    stats = _abi.NtpRunStats()
+
+    def run(seed: int) -> None:
+        st = lib.ntp_propagate(ctx, psrc, len(setup.sources), seed, C.byref(opts), hits.data_ptr(), cap, 1,
+                               C.byref(nh), C.byref(ns))
+        if st != _abi.NTP_OK:
+            raise _abi.NtpError(st, lib.ntp_last_error(ctx).decode())
+
+    run(20_000)
+    torch.cuda.synchronize()
+    ms, photon_steps, n_hits = [], 0, 0
+    for i in range(steps):
+        flush.zero_()
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        a.record(stream)
+        run(20_001 + i)
+        b.record(stream)
+        torch.cuda.synchronize()
+        ms.append(a.elapsed_time(b))
+        lib.ntp_get_run_stats(ctx, C.byref(stats))
+        photon_steps += int(stats.photon_steps)
+        n_hits += int(stats.hits)
+    setup.close()
+    t = sum(ms) / 1e3
+    return {"workload": f"{N_CASCADES} EM cascades 1e3-1e5 GeV at {photon_scale} of their photons, 20 POM "
+                        "modules; Cascadia Basin water (reference optics, HG g = 0.99), Frank-Tamm spectrum "
+                        "300-800 nm (30-knot texture table)",
+            "photons_per_step": photons, "steps": steps, "photons_per_s": photons * steps / t,
+            "photon_steps_per_photon": photon_steps / (photons * steps), "hits_per_step": n_hits / steps,
+            "ms_per_step": 1e3 * t / steps}
 
 
 def hybrid_bench(n_events: int = 10_000, batch: int = 256, train_steps: int = 48_000) -> dict:
@@ -576,6 +639,8 @@ def main():
             out["flow"] = flow_bench()
         if "hybrid" in legs and rank == 0:
             out["hybrid"] = hybrid_bench()
+        if "compat" in legs and rank == 0:
+            out["compat_medium"] = compat_bench()
         if rank == 0:
             print(json.dumps(out))
         return
