@@ -35,7 +35,9 @@ def ks_noise_bound(n: int, confidence: float) -> float:
     empirical CDF F_n of n samples of F: the Dvoretzky-Kiefer-Wolfowitz
     inequality with Massart's constant, eps = sqrt(ln(2 / (1 - confidence))
     / (2 n)); 0 for confidence 0, infinite without samples."""
-    if confidence <= 0.0:
+    if not 0.0 <= confidence < 1.0:
+        raise ValueError(f"confidence must be in [0, 1), got {confidence}")
+    if confidence == 0.0:
         return 0.0
     if n <= 0:
         return math.inf
@@ -85,6 +87,8 @@ class HybridSimulator:
         self.ks_min_hits = int(ks_min_hits)
         self.ks_max_photons = float(ks_max_photons)
         self.ks_confidence = float(ks_confidence)
+        if not 0.0 <= self.ks_confidence < 1.0:
+            raise ValueError(f"ks_confidence must be in [0, 1), got {ks_confidence}")
         self.fallback = False
         self.checks: list[tuple[int, float, int]] = []   # (event id, KS distance, MC hits)
         self._served = 0

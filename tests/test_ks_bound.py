@@ -5,6 +5,7 @@ exceed it."""
 import math
 
 import numpy as np
+import pytest
 
 from neutrinotelescopes_gb300.surrogate import ks_noise_bound
 
@@ -15,6 +16,9 @@ def test_bound_values():
     assert ks_noise_bound(40_000, 0.0) == 0.0
     assert ks_noise_bound(0, 0.95) == math.inf
     assert ks_noise_bound(10_000, 0.99) > ks_noise_bound(10_000, 0.95) > ks_noise_bound(40_000, 0.95)
+    for bad in (1.0, 1.5, -0.1):
+        with pytest.raises(ValueError):
+            ks_noise_bound(1000, bad)
 
 
 def test_perfect_samples_exceed_the_bound_rarely():
