@@ -44,6 +44,10 @@ def test_record_layouts():
     assert _abi.HIT_DTYPE.fields["photon_index"][1] == 56
     assert _abi.NtpSource.photons.offset == 32
     assert _abi.NtpMediumDesc.hg_g.offset == 64
+    # ntp_flow_config: 3 int32, 8 floats (t_min .. count_weight), then the u64 seed
+    assert _abi.NtpFlowConfig.count_weight.offset == 40
+    assert _abi.NtpFlowConfig.seed.offset == 48
+    assert C.sizeof(_abi.NtpFlowConfig) == 56
 
 
 def test_missing_library_fails_loudly(tmp_path):
