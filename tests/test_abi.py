@@ -64,3 +64,42 @@ def test_create_without_gpu_reports_error():
     st = lib.ntp_create(0, C.byref(ctx))
     assert st != _abi.NTP_OK and not ctx.value
     assert lib.ntp_last_error(None)
+
+
+# (C struct in include/ntp.h, ctypes mirror) pairs checked field by field
+_RECORDS = [("ntp_source", "NtpSource"), ("ntp_target", "NtpTarget"), ("ntp_medium_desc", "NtpMediumDesc"),
+            ("ntp_spectrum_desc", "NtpSpectrumDesc"), ("ntp_prop_opts", "NtpPropOpts"),
+            ("ntp_run_stats", "NtpRunStats"), ("ntp_summary_spec", "NtpSummarySpec"),
+            ("ntp_table_spec", "NtpTableSpec"), ("ntp_flow_config", "NtpFlowConfig"),
+            ("ntp_server_config", "NtpServerConfig"), ("ntp_event_result", "NtpEventResult"),
+            ("ntp_server_stats", "NtpServerStats")]
+
+
+def test_ctypes_records_match_the_header(tmp_path):
+    """Every ctypes record has the size and field offsets that a C compiler
+    gives the header's struct (compiled with gcc here)."""
+    import shutil
+    import subprocess
+    if shutil.which("gcc") is None:
+        pytest.skip("no gcc")
+    lines = ['#include <stdio.h>', '#include <stddef.h>', '#include "ntp.h"', "int main(void) {"]
+    expect = {}
+    for cname, pyname in _RECORDS:
+        cls = getattr(_abi, pyname)
+        lines.append(f'printf("{cname} size %zu\\n", sizeof({cname}));')
+        expect[f"{cname} size"] = C.sizeof(cls)
+        for fname, _ in cls._fields_:
+            lines.append(f'printf("{cname} {fname} %zu\\n", offsetof({cname}, {fname}));')
+            expect[f"{cname} {fname}"] = getattr(cls, fname).offset
+    lines.append("return 0; }")
+    src = tmp_path / "layout.c"
+    src.write_text("\n".join(lines))
+    exe = tmp_path / "layout"
+    r = subprocess.run(["gcc", "-std=c11", "-I", str(ROOT / "include"), str(src), "-o", str(exe)],
+                       capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
+    got = {}
+    for line in subprocess.run([str(exe)], capture_output=True, text=True, check=True).stdout.splitlines():
+        key, val = line.rsplit(" ", 1)
+        got[key] = int(val)
+    assert got == expect
