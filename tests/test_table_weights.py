@@ -65,3 +65,24 @@ def test_focus_draws():
     # photons per simulation follow the distance: the focus simulations reach
     # the hit target up to the cap
     assert np.all(b["n_simulated"] >= cfg.min_photons) and np.all(b["n_simulated"] <= cfg.max_photons)
+
+
+def test_save_load_keeps_what_training_needs(tmp_path):
+    """FlowTable.save / load round trip (CPU tensors): rows, groups, row groups
+    and the simulations' weight scales, so a loaded table trains with any
+    count_mode."""
+    rg = torch.tensor([0, 0, 1, 2, 3, 3, 3], dtype=torch.int32)
+    n = rg.numel()
+    t = FlowTable(torch.arange(n * 5, dtype=torch.float32).reshape(n, 5), torch.linspace(-5, 50, n),
+                  torch.arange(n, dtype=torch.float32), torch.ones(n, dtype=torch.int32),
+                  torch.zeros((4, 5)), torch.tensor([8.0, 2.0, 40.0, 0.0], dtype=torch.float64),
+                  torch.tensor([7, 1, 45, 0]), n_photons=123, n_hits=45, row_group=rg,
+                  sim_scale=torch.tensor([0.25, 4.0], dtype=torch.float64))
+    t.save(tmp_path / "t.npz")
+    u = FlowTable.load(tmp_path / "t.npz", device="cpu")
+    for k in ("cond", "tres", "nhits", "has_time", "group_cond", "group_expec", "group_count", "row_group",
+              "sim_scale"):
+        assert torch.equal(getattr(u, k), getattr(t, k)), k
+    assert (u.n_photons, u.n_hits) == (123, 45)
+    for a, b in zip(u.information_weights(), t.information_weights()):
+        assert torch.equal(a, b)
