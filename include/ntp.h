@@ -175,7 +175,8 @@ ntp_status ntp_create(int device, ntp_ctx** out);
 void ntp_destroy(ntp_ctx* ctx);
 
 /* Text of the last error on this context ("" if none).  With ctx == NULL,
-   the last error of a failed ntp_create. */
+   the last error of a context-free call (ntp_create, ntp_propagate_noalloc)
+   on the calling thread; each such call clears it first. */
 const char* ntp_last_error(const ntp_ctx* ctx);
 
 /* Medium of PhotonPropSetup (photon_prop_cuda.jl:34-39): copies the tables to
@@ -220,7 +221,12 @@ ntp_status ntp_propagate(ntp_ctx* ctx, const ntp_source* sources, int32_t n_sour
    array inside the library, so the call allocates nothing.  Limits: at most
    1024 sources, 4096 targets, NTP_MAX_MEDIUM_KNOTS medium knots and
    NTP_MAX_SPECTRUM_KNOTS spectrum knots; more is rejected with
-   NTP_ERR_INVALID.  The scratch is shared by all calls on a device: calls
+   NTP_ERR_INVALID, as are tables that ntp_set_medium / ntp_set_spectrum
+   reject and a hit buffer on another device than the current one.  Every
+   target is tested at every step (no column culling or grid walk): the same
+   hits as ntp_propagate, at a cost that grows with the number of targets
+   (a few per cent on a 20-module string, many times ntp_propagate's time on
+   thousands of modules).  The scratch is shared by all calls on a device: calls
    that overlap on the GPU race and must be serialised by the caller.  The
    first call on a device looks up the scratch address on that device (the
    current device); make that first call before any stream capture.  Uses
@@ -395,6 +401,19 @@ ntp_status ntp_event_conditions(ntp_ctx* ctx, const ntp_source* events, const fl
 ntp_status ntp_gemm_bf16(const void* A, int32_t lda, const void* B, int32_t ldb, void* C, int32_t ldc, int32_t M,
                          int32_t N, int32_t K, const float* bias, int32_t relu, int32_t out_kind, int32_t splits,
                          void* stream);
+
+/* Failure detection of the tensor-core GEMM (no reference counterpart; the
+ * reference's only device check, the @cuassert of photon_prop_cuda.jl:484,
+ * kills the context).  Every mbarrier wait of the GEMM pipeline gives up after
+ * wait_limit_ns of the GPU's global timer (0 = the default, 2 s), sets an
+ * error word, lets its copies in flight land, frees its tensor memory and
+ * returns; ntp_gemm_bf16 (and the flow calls built on it) then return
+ * NTP_ERR_TIMEOUT and the context stays usable.  withhold_first_copy != 0
+ * makes the following GEMM launches leave out the first pipeline stage's
+ * copies, so that the first wait has nothing to complete and runs out: this
+ * is how the timeout path is tested (outputs are undefined while it is set).
+ * Process-wide; applies to launches made after the call. */
+ntp_status ntp_gemm_set_wait_limit(uint64_t wait_limit_ns, int32_t withhold_first_copy);
 
 /* --------------------------------------------------------- arrival-time flow
  * The per-module arrival-time surrogate: RQNormFlow with a log-expectation

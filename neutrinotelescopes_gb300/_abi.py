@@ -255,6 +255,7 @@ EXPORTED = (
     "ntp_make_table",
     "ntp_event_conditions",
     "ntp_gemm_bf16",
+    "ntp_gemm_set_wait_limit",
     "ntp_flow_create",
     "ntp_flow_destroy",
     "ntp_flow_last_error",
@@ -314,6 +315,8 @@ def _declare(lib: C.CDLL) -> None:
     lib.ntp_resample.restype = C.c_int
     lib.ntp_gemm_bf16.argtypes = [vp, i32, vp, i32, vp, i32, i32, i32, i32, vp, i32, i32, i32, vp]
     lib.ntp_gemm_bf16.restype = C.c_int
+    lib.ntp_gemm_set_wait_limit.argtypes = [u64, i32]
+    lib.ntp_gemm_set_wait_limit.restype = C.c_int
     lib.ntp_make_table.argtypes = [vp, vp, u64, vp, C.POINTER(NtpSource), C.POINTER(C.c_float),
                                    C.POINTER(C.c_double), C.POINTER(C.c_double), C.POINTER(NtpTableSpec), vp, vp, vp,
                                    vp, vp, u64, C.POINTER(u64), vp, vp, vp, vp, vp]

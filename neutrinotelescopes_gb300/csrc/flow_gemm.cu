@@ -40,7 +40,11 @@ constexpr int kBM = 128;   // rows of a tile (UMMA M)
 constexpr int kBK = 64;    // K slice per stage: 64 bf16 = 128 bytes = one swizzle row
 constexpr int kUK = 16;    // K of one tcgen05.mma for 16-bit inputs
 constexpr int kThreads = 128;
-constexpr unsigned long long kWaitLimitNs = 2000000000ull;  // a wait gives up after 2 s
+constexpr unsigned long long kWaitLimitNs = 2000000000ull;  // by default a wait gives up after 2 s
+
+// failure-detection controls (ntp_gemm_set_wait_limit), read at each launch
+std::atomic<unsigned long long> g_wait_limit_ns{kWaitLimitNs};
+std::atomic<int> g_withhold_first{0};
 
 __device__ __forceinline__ uint32_t smem_u32(const void* p) {
     return static_cast<uint32_t>(__cvta_generic_to_shared(p));
@@ -61,8 +65,8 @@ __device__ __forceinline__ unsigned long long global_ns() {
     return t;
 }
 
-// Bounded wait for the phase with the given parity; false after kWaitLimitNs.
-__device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity) {
+// Bounded wait for the phase with the given parity; false after limit_ns.
+__device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity, unsigned long long limit_ns) {
     const uint32_t a = smem_u32(bar);
     const unsigned long long t0 = global_ns();
     for (unsigned i = 0;; ++i) {
@@ -73,7 +77,7 @@ __device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity) {
             : "r"(a), "r"(parity)
             : "memory");
         if (done) return true;
-        if ((i & 255u) == 255u && global_ns() - t0 > kWaitLimitNs) return false;
+        if ((i & 255u) == 255u && global_ns() - t0 > limit_ns) return false;
     }
 }
 
@@ -152,7 +156,7 @@ template <int BN>
 __global__ void __launch_bounds__(kThreads, 1)
     gemm_bf16_kernel(const __grid_constant__ CUtensorMap map_a, const __grid_constant__ CUtensorMap map_b, int M,
                      int N, int k_tiles_per_split, int k_tiles_total, const GemmEpilogue ep, int vec_ok,
-                     int* __restrict__ error) {
+                     int* __restrict__ error, unsigned long long wait_ns, int withhold_first) {
     extern __shared__ unsigned char smem_raw[];
     Smem<BN>* s = reinterpret_cast<Smem<BN>*>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
     constexpr int kStages = Smem<BN>::kStages;
@@ -188,6 +192,10 @@ __global__ void __launch_bounds__(kThreads, 1)
         const int nk = kt1 - kt0;
         int issued[kStages] = {}, landed[kStages] = {};  // TMA pairs per stage
         for (int i = 0; i < kStages && i < nk; ++i) {
+            // failure-detection test: the first stage's copies are not issued,
+            // so its barrier is a flag that nothing completes and the first
+            // wait runs out (nothing else is skipped; outputs are undefined)
+            if (i == 0 && withhold_first) continue;
             mbar_expect_tx(&s->full[i], kStageBytes);
             tma_load_2d(s->a[i], &map_a, &s->full[i], (kt0 + i) * kBK, m0);
             tma_load_2d(s->b[i], &map_b, &s->full[i], (kt0 + i) * kBK, n0);
@@ -195,7 +203,7 @@ __global__ void __launch_bounds__(kThreads, 1)
         }
         for (int i = 0; i < nk && ok; ++i) {
             const int st = i % kStages;
-            ok = mbar_wait(&s->full[st], (i / kStages) & 1);
+            ok = mbar_wait(&s->full[st], (i / kStages) & 1, wait_ns);
             if (!ok) break;
             ++landed[st];
             asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
@@ -210,7 +218,7 @@ __global__ void __launch_bounds__(kThreads, 1)
             const int prev = i - 1;
             if (prev >= 0 && prev + kStages < nk) {
                 const int ps = prev % kStages;
-                ok = mbar_wait(&s->empty[ps], (prev / kStages) & 1);
+                ok = mbar_wait(&s->empty[ps], (prev / kStages) & 1, wait_ns);
                 if (!ok) break;
                 mbar_expect_tx(&s->full[ps], kStageBytes);
                 tma_load_2d(s->a[ps], &map_a, &s->full[ps], (kt0 + prev + kStages) * kBK, m0);
@@ -223,13 +231,13 @@ __global__ void __launch_bounds__(kThreads, 1)
             atomicExch(error, 1);
             // let copies still in flight land before the CTA's shared memory goes away
             for (int st = 0; st < kStages; ++st)
-                while (landed[st] < issued[st] && mbar_wait(&s->full[st], landed[st] & 1)) ++landed[st];
+                while (landed[st] < issued[st] && mbar_wait(&s->full[st], landed[st] & 1, wait_ns)) ++landed[st];
         }
     }
     __syncwarp();
     // the accumulator is complete when `done` flips (a thread that timed out
     // above still committed, so this wait ends once its MMAs drain)
-    const bool have = (kt1 > kt0) && mbar_wait(&s->done, 0);
+    const bool have = (kt1 > kt0) && mbar_wait(&s->done, 0, wait_ns);
     if (kt1 > kt0 && !have && lane == 0) atomicExch(error, 2);
     asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
 
@@ -401,7 +409,8 @@ cudaError_t launch_bn(const CUtensorMap& ma, const CUtensorMap& mb, int M, int N
     if (e != cudaSuccess) return e;
     const int per = (k_tiles + splits - 1) / splits;
     dim3 grid((M + kBM - 1) / kBM, (N + BN - 1) / BN, (k_tiles + per - 1) / per);
-    gemm_bf16_kernel<BN><<<grid, kThreads, smem, st>>>(ma, mb, M, N, per, k_tiles, ep, vec_ok, error);
+    gemm_bf16_kernel<BN><<<grid, kThreads, smem, st>>>(ma, mb, M, N, per, k_tiles, ep, vec_ok, error,
+                                                        g_wait_limit_ns.load(), g_withhold_first.load());
     return cudaGetLastError();
 }
 
@@ -503,4 +512,10 @@ extern "C" ntp_status ntp_gemm_bf16(const void* A, int32_t lda, const void* B, i
         cudaStreamSynchronize(st) != cudaSuccess)
         return NTP_ERR_CUDA;
     return h ? NTP_ERR_TIMEOUT : NTP_OK;
+}
+
+extern "C" ntp_status ntp_gemm_set_wait_limit(uint64_t wait_limit_ns, int32_t withhold_first_copy) {
+    ntp::g_wait_limit_ns.store(wait_limit_ns ? wait_limit_ns : ntp::kWaitLimitNs);
+    ntp::g_withhold_first.store(withhold_first_copy ? 1 : 0);
+    return NTP_OK;
 }

@@ -85,11 +85,7 @@ struct ntp_ctx {
     size_t scratch_bytes = 0;
 };
 
-const char* ntp_noalloc_last_error();
-
 namespace {
-
-std::string g_create_error;
 
 #define NTP_CUDA(ctx, call)                                                                   \
     do {                                                                                      \
@@ -198,24 +194,70 @@ ntp::HitTargetTable hit_table(const ntp_ctx* ctx) {
 
 }  // namespace
 
+namespace ntp {
+
+const char* check_medium(const ntp_medium_desc* m, bool need_absorption) {
+    if (!m) return "medium is NULL";
+    if (m->n_knots < 2 || m->n_knots > NTP_MAX_MEDIUM_KNOTS) return "n_knots must be in [2, NTP_MAX_MEDIUM_KNOTS]";
+    if (!m->ref_index || !m->group_velocity || !m->scattering_length) return "a medium table is NULL";
+    if (!(m->wl_max > m->wl_min) || !finite(m->wl_min) || !finite(m->wl_max)) return "need wl_max > wl_min";
+    if (!finite(m->hg_g) || !(m->hg_g > -1.0f && m->hg_g < 1.0f)) return "hg_g must lie in (-1, 1)";
+    if (!(m->rayleigh_fraction >= 0.0f && m->rayleigh_fraction <= 1.0f)) return "rayleigh_fraction must lie in [0, 1]";
+    for (int i = 0; i < m->n_knots; ++i) {
+        const float n = m->ref_index[i], vg = m->group_velocity[i], ls = m->scattering_length[i];
+        if (!(n > 1.0f) || !(vg > 0.0f) || !(ls > 0.0f) || !finite(n) || !finite(vg) || !finite(ls))
+            return "need n > 1, group velocity > 0, scattering length > 0 (finite) at every knot";
+    }
+    if (!need_absorption) return nullptr;
+    if (m->n_abs_knots < 2 || m->n_abs_knots > NTP_MAX_ABS_KNOTS || !m->abs_wavelength || !m->abs_length)
+        return "absorption table needs 2..NTP_MAX_ABS_KNOTS knots";
+    for (int i = 0; i < m->n_abs_knots; ++i) {
+        if (i && !(m->abs_wavelength[i] > m->abs_wavelength[i - 1])) return "absorption wavelengths must ascend";
+        if (!(m->abs_length[i] > 0.0f)) return "absorption length must be > 0";
+    }
+    return nullptr;
+}
+
+const char* check_spectrum(const ntp_spectrum_desc* s) {
+    if (!s) return "spectrum is NULL";
+    switch (s->kind) {
+    case NTP_SPEC_MONOCHROMATIC:
+        return s->wavelength > 0.0f && finite(s->wavelength) ? nullptr : "wavelength must be > 0";
+    case NTP_SPEC_TABLE_LINEAR:
+    case NTP_SPEC_TABLE_TEXTURE:
+        if (s->n_knots < 2 || s->n_knots > NTP_MAX_SPECTRUM_KNOTS || !s->icdf_knots)
+            return "table needs 2..NTP_MAX_SPECTRUM_KNOTS knots";
+        for (int i = 0; i < s->n_knots; ++i)
+            if (!(s->icdf_knots[i] > 0.0f) || !finite(s->icdf_knots[i])) return "knots must be finite wavelengths > 0";
+        return nullptr;
+    case NTP_SPEC_INV_SQUARE:
+        return s->wl_min > 0.0f && s->wl_max > s->wl_min && finite(s->wl_max) ? nullptr : "need 0 < wl_min < wl_max";
+    default:
+        return "unknown kind";
+    }
+}
+
+}  // namespace ntp
+
 extern "C" {
 
 int ntp_abi_version(void) { return NTP_ABI_VERSION; }
 
 ntp_status ntp_create(int device, ntp_ctx** out) {
+    ntp::set_free_error("");
     if (!out) return NTP_ERR_INVALID;
     *out = nullptr;
     int n = 0;
     cudaError_t e = cudaGetDeviceCount(&n);
     if (e != cudaSuccess || device < 0 || device >= n) {
-        g_create_error = e != cudaSuccess ? std::string("cudaGetDeviceCount: ") + cudaGetErrorString(e)
-                                          : "device index out of range";
+        ntp::set_free_error(e != cudaSuccess ? (std::string("cudaGetDeviceCount: ") + cudaGetErrorString(e)).c_str()
+                                             : "device index out of range");
         return e != cudaSuccess ? NTP_ERR_CUDA : NTP_ERR_INVALID;
     }
     ntp_ctx* ctx = new ntp_ctx();
     ctx->device = device;
     auto fail = [&](cudaError_t err, const char* what) {
-        g_create_error = std::string(what) + ": " + cudaGetErrorString(err);
+        ntp::set_free_error((std::string(what) + ": " + cudaGetErrorString(err)).c_str());
         ntp_destroy(ctx);
         return NTP_ERR_CUDA;
     };
@@ -270,37 +312,15 @@ void ntp_destroy(ntp_ctx* ctx) {
 
 const char* ntp_last_error(const ntp_ctx* ctx) {
     if (ctx) return ctx->err.c_str();
-    const char* na = ntp_noalloc_last_error();  // set when the last ntp_propagate_noalloc on this thread failed
-    return na[0] ? na : g_create_error.c_str();
+    return ntp::free_error();
 }
 
 ntp_status ntp_set_medium(ntp_ctx* ctx, const ntp_medium_desc* m) {
     if (!ctx) return NTP_ERR_INVALID;
-    if (!m) return invalid(ctx, "ntp_set_medium: medium is NULL");
-    if (m->n_knots < 2 || m->n_knots > NTP_MAX_MEDIUM_KNOTS)
-        return invalid(ctx, "ntp_set_medium: n_knots must be in [2, NTP_MAX_MEDIUM_KNOTS]");
-    if (!m->ref_index || !m->group_velocity || !m->scattering_length)
-        return invalid(ctx, "ntp_set_medium: a medium table is NULL");
-    if (!(m->wl_max > m->wl_min) || !finite(m->wl_min) || !finite(m->wl_max))
-        return invalid(ctx, "ntp_set_medium: need wl_max > wl_min");
-    if (m->n_abs_knots < 2 || m->n_abs_knots > NTP_MAX_ABS_KNOTS || !m->abs_wavelength || !m->abs_length)
-        return invalid(ctx, "ntp_set_medium: absorption table needs 2..NTP_MAX_ABS_KNOTS knots");
-    if (!finite(m->hg_g) || !(m->hg_g > -1.0f && m->hg_g < 1.0f))
-        return invalid(ctx, "ntp_set_medium: hg_g must lie in (-1, 1)");
-    if (!(m->rayleigh_fraction >= 0.0f && m->rayleigh_fraction <= 1.0f))
-        return invalid(ctx, "ntp_set_medium: rayleigh_fraction must lie in [0, 1]");
+    if (const char* why = ntp::check_medium(m, true)) return invalid(ctx, std::string("ntp_set_medium: ") + why);
     std::vector<float4> tab(m->n_knots);
-    for (int i = 0; i < m->n_knots; ++i) {
-        const float n = m->ref_index[i], vg = m->group_velocity[i], ls = m->scattering_length[i];
-        if (!(n > 1.0f) || !(vg > 0.0f) || !(ls > 0.0f) || !finite(n) || !finite(vg) || !finite(ls))
-            return invalid(ctx, "ntp_set_medium: need n > 1, group velocity > 0, scattering length > 0");
-        tab[i] = make_float4(n, vg, ls, 0.0f);
-    }
-    for (int i = 0; i < m->n_abs_knots; ++i) {
-        if (i && !(m->abs_wavelength[i] > m->abs_wavelength[i - 1]))
-            return invalid(ctx, "ntp_set_medium: absorption wavelengths must ascend");
-        if (!(m->abs_length[i] > 0.0f)) return invalid(ctx, "ntp_set_medium: absorption length must be > 0");
-    }
+    for (int i = 0; i < m->n_knots; ++i)
+        tab[i] = make_float4(m->ref_index[i], m->group_velocity[i], m->scattering_length[i], 0.0f);
     cudaSetDevice(ctx->device);
     NTP_CUDA(ctx, dupload(ctx->d_med, tab.data(), tab.size(), ctx->stream));
     NTP_CUDA(ctx, dupload(ctx->d_abs_wl, m->abs_wavelength, m->n_abs_knots, ctx->stream));
@@ -317,11 +337,10 @@ ntp_status ntp_set_medium(ntp_ctx* ctx, const ntp_medium_desc* m) {
 
 ntp_status ntp_set_spectrum(ntp_ctx* ctx, const ntp_spectrum_desc* s) {
     if (!ctx) return NTP_ERR_INVALID;
-    if (!s) return invalid(ctx, "ntp_set_spectrum: spectrum is NULL");
+    if (const char* why = ntp::check_spectrum(s)) return invalid(ctx, std::string("ntp_set_spectrum: ") + why);
     cudaSetDevice(ctx->device);
     switch (s->kind) {
     case NTP_SPEC_MONOCHROMATIC:
-        if (!(s->wavelength > 0.0f)) return invalid(ctx, "ntp_set_spectrum: wavelength must be > 0");
         dfree(ctx->d_spec);
         ctx->n_spec = 0;
         ctx->spec_p0 = s->wavelength;
@@ -329,24 +348,15 @@ ntp_status ntp_set_spectrum(ntp_ctx* ctx, const ntp_spectrum_desc* s) {
         break;
     case NTP_SPEC_TABLE_LINEAR:
     case NTP_SPEC_TABLE_TEXTURE:
-        if (s->n_knots < 2 || s->n_knots > NTP_MAX_SPECTRUM_KNOTS || !s->icdf_knots)
-            return invalid(ctx, "ntp_set_spectrum: table needs 2..NTP_MAX_SPECTRUM_KNOTS knots");
-        for (int i = 0; i < s->n_knots; ++i)
-            if (!(s->icdf_knots[i] > 0.0f) || !finite(s->icdf_knots[i]))
-                return invalid(ctx, "ntp_set_spectrum: knots must be finite wavelengths > 0");
         NTP_CUDA(ctx, dupload(ctx->d_spec, s->icdf_knots, s->n_knots, ctx->stream));
         ctx->n_spec = s->n_knots;
         break;
-    case NTP_SPEC_INV_SQUARE:
-        if (!(s->wl_min > 0.0f) || !(s->wl_max > s->wl_min))
-            return invalid(ctx, "ntp_set_spectrum: need 0 < wl_min < wl_max");
+    default:  // NTP_SPEC_INV_SQUARE
         dfree(ctx->d_spec);
         ctx->n_spec = 0;
         ctx->spec_p0 = 1.0f / s->wl_min;
         ctx->spec_p1 = 1.0f / s->wl_min - 1.0f / s->wl_max;
         break;
-    default:
-        return invalid(ctx, "ntp_set_spectrum: unknown kind");
     }
     ctx->spec_kind = s->kind;
     ctx->have_spec = true;

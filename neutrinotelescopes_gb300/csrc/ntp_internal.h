@@ -146,6 +146,18 @@ cudaError_t propagate_occupancy(const PropParams& p, int* blocks_per_sm);
 // the kernel launch_propagate uses (for CUDA-graph kernel-node updates)
 const void* propagate_kernel_fn();
 
+// Checks shared by ntp_set_medium / ntp_set_spectrum and the context-free
+// ntp_propagate_noalloc: nullptr when the descriptor is valid, else the
+// reason.  need_absorption: also check the absorption table (unused by the
+// propagation kernel itself).
+const char* check_medium(const ntp_medium_desc* m, bool need_absorption);
+const char* check_spectrum(const ntp_spectrum_desc* s);
+
+// The error slot of context-free calls (ntp_create, ntp_propagate_noalloc),
+// one per host thread; ntp_last_error(NULL) returns it.
+void set_free_error(const char* msg);
+const char* free_error();
+
 // Medium / spectrum / target part of the kernel parameters from a context
 // whose tables are set (ntp_abi.cu); returns false if a table is missing.
 bool fill_world_params(const ntp_ctx* ctx, PropParams& p);

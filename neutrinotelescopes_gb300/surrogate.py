@@ -175,9 +175,12 @@ class HybridSimulator:
 
     def ks_fails(self, ks: float, n_mc: int) -> bool:
         """True when a check of distance ks from n_mc MC hits shows the
-        surrogate above ks_threshold (a NaN distance, an event without
-        MC hits, decides nothing)."""
-        return bool(ks - self.ks_noise_bound(n_mc) > self.ks_threshold)
+        surrogate above ks_threshold.  An event without MC hits (n_mc == 0)
+        decides nothing; with MC hits, a distance that is not finite (a
+        diverged or degenerate flow CDF) is a failure."""
+        if n_mc <= 0:
+            return False
+        return bool(not math.isfinite(ks) or ks - self.ks_noise_bound(n_mc) > self.ks_threshold)
 
     def ks_check(self, event_id: int, source, log10_energy: float) -> tuple[float, int]:
         """One-sample KS distance of plain-MC hit times (modules in the
@@ -212,10 +215,7 @@ class HybridSimulator:
             return float("nan"), 0
         off = tgeo + float(source.time)
         F = self.flow.mixture_cdf(cond, torch.as_tensor(t.astype(np.float32), device=cond.device), off)
-        F = F.cpu().numpy()
-        n = t.size
-        i = np.arange(1, n + 1)
-        return float(max(np.max(i / n - F), np.max(F - (i - 1) / n))), int(n)
+        return ks_distance(F.cpu().numpy()), int(t.size)
 
     def serve(self, arrivals, *, max_batch: int = 64) -> list[tuple[int, str, float]]:
         """Real-time replay: events (arrival time in s, event_id, source,
@@ -246,6 +246,18 @@ class HybridSimulator:
         """Plain MC for one event: propagation, weights and resampling."""
         r = mc_truth(self.setup, source, seed=self.seed + event_id)
         return EventHits(event_id, "mc", len(r["time"]), r["target"], r["pmt"], r["time"])
+
+
+def ks_distance(cdf_at_sorted: np.ndarray) -> float:
+    """One-sample KS distance sup |F_n - F| from the model CDF evaluated at
+    the sorted sample; NaN when any CDF value is not finite (a diverged or
+    degenerate model), so that the check cannot pass on it."""
+    F = np.asarray(cdf_at_sorted, dtype=np.float64)
+    n = F.size
+    if n == 0 or not np.all(np.isfinite(F)):
+        return float("nan")
+    i = np.arange(1, n + 1)
+    return float(max(np.max(i / n - F), np.max(F - (i - 1) / n)))
 
 
 def mc_truth(setup: PhotonPropSetup, source, *, seed: int = 0) -> dict:

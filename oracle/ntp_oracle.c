@@ -60,6 +60,70 @@ void ntpo_philox4x32_10(const uint32_t ctr[4], const uint32_t key[2], uint32_t o
    plus one half, times 2^-23.  Exactly representable in float and double. */
 double ntpo_u01_f64(uint32_t w) { return ((double)(w >> 9) + 0.5) * (1.0 / 8388608.0); }
 
+/* Candidate lookup for large detectors (the statistical checks on a string
+   grid), used only when asked for.  Target centres are bucketed on a 2-D
+   (x, y) grid.  A step segment that enters a sphere passes within one radius
+   of its centre, so the centre lies in the segment's bounding box widened by
+   that radius; the cells this box overlaps therefore hold every target the
+   literal scan of photon_prop_cuda.jl:460-468 can report.  Those candidates
+   go through the same check_intersection and the lowest list index (first
+   in list order) or the smallest distance (nearest) wins, which is what the
+   scan returns: the lookup only skips targets that cannot be hit.  The
+   widening adds 5 cm to the largest radius to cover float rounding of the
+   segment end points. */
+typedef struct {
+    int nx, ny;
+    double x0, y0, inv_h;
+    double margin;
+    int* start; /* nx * ny + 1 offsets into items */
+    int* items; /* target indices, ascending within a cell */
+} ntpo_bins;
+
+static int ntpo_clampi(long long v, int hi) { return v < 0 ? 0 : (v > hi ? hi : (int)v); }
+
+static void ntpo_bins_build(ntpo_bins* b, const ntp_target* tg, int n_tg) {
+    double xmin = 1e300, xmax = -1e300, ymin = 1e300, ymax = -1e300, rmax = 0.0;
+    for (int t = 0; t < n_tg; ++t) {
+        double x = tg[t].position[0], y = tg[t].position[1];
+        if (x < xmin) xmin = x;
+        if (x > xmax) xmax = x;
+        if (y < ymin) ymin = y;
+        if (y > ymax) ymax = y;
+        if (tg[t].radius > rmax) rmax = tg[t].radius;
+    }
+    double extent = (xmax - xmin) > (ymax - ymin) ? (xmax - xmin) : (ymax - ymin);
+    double cells = n_tg / 16.0 > 1.0 ? n_tg / 16.0 : 1.0;
+    double h = extent / sqrt(cells);
+    if (h < 4.0 * rmax) h = 4.0 * rmax;
+    if (h < 1.0) h = 1.0;
+    b->x0 = xmin;
+    b->y0 = ymin;
+    b->inv_h = 1.0 / h;
+    b->nx = (int)((xmax - xmin) / h) + 1;
+    b->ny = (int)((ymax - ymin) / h) + 1;
+    b->margin = rmax + 0.05;
+    int nc = b->nx * b->ny;
+    b->start = (int*)calloc((size_t)nc + 1, sizeof(int));
+    b->items = (int*)malloc(sizeof(int) * (size_t)(n_tg ? n_tg : 1));
+    int* cell = (int*)malloc(sizeof(int) * (size_t)(n_tg ? n_tg : 1));
+    for (int t = 0; t < n_tg; ++t) {
+        int ix = ntpo_clampi((long long)floor((tg[t].position[0] - b->x0) * b->inv_h), b->nx - 1);
+        int iy = ntpo_clampi((long long)floor((tg[t].position[1] - b->y0) * b->inv_h), b->ny - 1);
+        cell[t] = iy * b->nx + ix;
+        b->start[cell[t] + 1]++;
+    }
+    for (int c = 0; c < nc; ++c) b->start[c + 1] += b->start[c];
+    int* fill = (int*)calloc((size_t)nc, sizeof(int));
+    for (int t = 0; t < n_tg; ++t) b->items[b->start[cell[t]] + fill[cell[t]]++] = t;
+    free(fill);
+    free(cell);
+}
+
+static void ntpo_bins_free(ntpo_bins* b) {
+    free(b->start);
+    free(b->items);
+}
+
 /* ------------------------------------------------------------------------
  * The step law, in double and in float. */
 #define REAL double
@@ -97,7 +161,7 @@ uint64_t ntpo_propagate_f64(const ntp_source* src, int n_src, const ntp_medium_d
     for (uint64_t gid = gid_begin; gid < gid_end && gid < prefix[n_src]; ++gid) {
         int s = ntpo_source_of(prefix, n_src, gid);
         ntp_hit h;
-        if (propagate_one_f64(&src[s], (uint32_t)s, gid - prefix[s], m, sp, tg, n_tg, seed, o, &h)) {
+        if (propagate_one_f64(&src[s], (uint32_t)s, gid - prefix[s], m, sp, tg, n_tg, seed, o, NULL, &h)) {
             if (n < cap) out[n] = h;
             ++n;
         }
@@ -106,17 +170,18 @@ uint64_t ntpo_propagate_f64(const ntp_source* src, int n_src, const ntp_medium_d
     return n;
 }
 
-/* Single-precision mirror over all photons with OpenMP threads; used as the
-   timed CPU baseline.  Returns the hit count; hits are written (unordered)
-   up to cap.  *photons_done receives the number of photons stepped. */
-uint64_t ntpo_propagate_f32(const ntp_source* src, int n_src, const ntp_medium_desc* m,
-                            const ntp_spectrum_desc* sp, const ntp_target* tg, int n_tg,
-                            uint64_t seed, const ntp_prop_opts* o, uint64_t gid_begin,
-                            uint64_t gid_end, ntp_hit* out, uint64_t cap, int n_threads) {
+static uint64_t ntpo_f32_run(const ntp_source* src, int n_src, const ntp_medium_desc* m,
+                             const ntp_spectrum_desc* sp, const ntp_target* tg, int n_tg, uint64_t seed,
+                             const ntp_prop_opts* o, uint64_t gid_begin, uint64_t gid_end, ntp_hit* out,
+                             uint64_t cap, int n_threads, int binned) {
     uint64_t* prefix = (uint64_t*)malloc(sizeof(uint64_t) * (size_t)(n_src + 1));
     prefix[0] = 0;
     for (int i = 0; i < n_src; ++i) prefix[i + 1] = prefix[i] + src[i].photons;
     if (gid_end > prefix[n_src]) gid_end = prefix[n_src];
+    ntpo_bins bins;
+    if (n_tg == 0) binned = 0;
+    if (binned) ntpo_bins_build(&bins, tg, n_tg);
+    const ntpo_bins* bp = binned ? &bins : NULL;
     uint64_t n = 0;
     long long b = (long long)gid_begin, e = (long long)gid_end;
 #pragma omp parallel for schedule(dynamic, 4096) num_threads(n_threads > 0 ? n_threads : 1)
@@ -124,15 +189,36 @@ uint64_t ntpo_propagate_f32(const ntp_source* src, int n_src, const ntp_medium_d
         int s = ntpo_source_of(prefix, n_src, (uint64_t)gid);
         ntp_hit h;
         if (propagate_one_f32(&src[s], (uint32_t)s, (uint64_t)gid - prefix[s], m, sp, tg, n_tg,
-                              seed, o, &h)) {
+                              seed, o, bp, &h)) {
             uint64_t slot;
 #pragma omp atomic capture
             slot = n++;
             if (slot < cap) out[slot] = h;
         }
     }
+    if (binned) ntpo_bins_free(&bins);
     free(prefix);
     return n;
+}
+
+/* Single-precision mirror over photons [gid_begin, gid_end) with OpenMP
+   threads; used as the timed CPU baseline.  Returns the hit count; hits are
+   written (unordered) up to cap. */
+uint64_t ntpo_propagate_f32(const ntp_source* src, int n_src, const ntp_medium_desc* m,
+                            const ntp_spectrum_desc* sp, const ntp_target* tg, int n_tg,
+                            uint64_t seed, const ntp_prop_opts* o, uint64_t gid_begin,
+                            uint64_t gid_end, ntp_hit* out, uint64_t cap, int n_threads) {
+    return ntpo_f32_run(src, n_src, m, sp, tg, n_tg, seed, o, gid_begin, gid_end, out, cap, n_threads, 0);
+}
+
+/* The same with the bucket-grid candidate lookup (ntpo_bins) in place of the
+   scan over every target: the same hits, for detectors of thousands of
+   modules. */
+uint64_t ntpo_propagate_f32_binned(const ntp_source* src, int n_src, const ntp_medium_desc* m,
+                                   const ntp_spectrum_desc* sp, const ntp_target* tg, int n_tg,
+                                   uint64_t seed, const ntp_prop_opts* o, uint64_t gid_begin,
+                                   uint64_t gid_end, ntp_hit* out, uint64_t cap, int n_threads) {
+    return ntpo_f32_run(src, n_src, m, sp, tg, n_tg, seed, o, gid_begin, gid_end, out, cap, n_threads, 1);
 }
 
 /* ------------------------------------------------------------------------

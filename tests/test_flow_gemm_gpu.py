@@ -57,3 +57,30 @@ def test_gemm_rejects_bad_shapes():
     lib = _abi.load_library()
     assert lib.ntp_gemm_bf16(A.data_ptr(), 60, A.data_ptr(), 60, C.data_ptr(), 128, 128, 128, 60, None, 0, 0, 1,
                              None) == _abi.NTP_ERR_INVALID
+
+
+def test_gemm_wait_runs_out_and_the_context_stays_usable():
+    """The failure-detection path: with the first pipeline stage's copies
+    withheld, the first mbarrier wait has nothing to complete; it gives up
+    after the 1 ms limit and the call returns NTP_ERR_TIMEOUT.  The next GEMM
+    on the same context, with the default limit, is correct."""
+    import time
+
+    import torch
+    lib = _abi.load_library()
+    M, N, K = 128, 64, 256
+    A = torch.randn(M, K, device="cuda").to(torch.bfloat16)
+    B = torch.randn(N, K, device="cuda").to(torch.bfloat16)
+    C = torch.zeros(M, N, device="cuda")
+    assert lib.ntp_gemm_set_wait_limit(1_000_000, 1) == _abi.NTP_OK
+    try:
+        t0 = time.perf_counter()
+        st = lib.ntp_gemm_bf16(A.data_ptr(), K, B.data_ptr(), K, C.data_ptr(), N, M, N, K, None, 0, 0, 1, None)
+        elapsed = time.perf_counter() - t0
+    finally:
+        assert lib.ntp_gemm_set_wait_limit(0, 0) == _abi.NTP_OK
+    assert st == _abi.NTP_ERR_TIMEOUT, st
+    assert elapsed < 1.0
+    torch.cuda.synchronize()
+    run(M, N, K)
+    run(512, 256, 256, relu=1, bias=True, out_kind=1)

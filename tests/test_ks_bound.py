@@ -7,7 +7,7 @@ import math
 import numpy as np
 import pytest
 
-from neutrinotelescopes_gb300.surrogate import ks_noise_bound
+from neutrinotelescopes_gb300.surrogate import HybridSimulator, ks_distance, ks_noise_bound
 
 
 def test_bound_values():
@@ -35,3 +35,23 @@ def test_perfect_samples_exceed_the_bound_rarely():
         d = max(np.max(i / n - u), np.max(u - (i - 1) / n))
         over += d > eps
     assert over / trials <= 0.05 + 3 * math.sqrt(0.05 * 0.95 / trials)
+
+
+def test_non_finite_cdf_fails_the_check():
+    """A model CDF with a NaN (a diverged flow) gives a NaN distance, and a
+    NaN distance with MC hits present is a failed check; without MC hits a
+    check decides nothing."""
+    u = np.linspace(0.001, 0.999, 500)
+    assert abs(ks_distance(u) - 0.001) < 1e-3
+    bad = u.copy()
+    bad[-1] = np.nan
+    assert math.isnan(ks_distance(bad))
+    bad = u.copy()
+    bad[0] = np.inf
+    assert math.isnan(ks_distance(bad))
+    sim = HybridSimulator.__new__(HybridSimulator)
+    sim.ks_threshold, sim.ks_confidence = 0.02, 0.95
+    assert sim.ks_fails(float("nan"), 40_000)
+    assert not sim.ks_fails(float("nan"), 0)
+    assert not sim.ks_fails(0.02, 40_000)
+    assert sim.ks_fails(0.02 + ks_noise_bound(40_000, 0.95) + 1e-6, 40_000)

@@ -10,7 +10,9 @@ bound of such a hit is widened by that factor (capped at 50), with
 cos(incidence) taken from the oracle's hit.  A photon whose hit/miss decision
 falls within float rounding of the sphere edge or the step end can come out
 differently in float and double; at most 0.5% of the hit photons (and at
-least 3) may differ in the set of hit photons.
+least 3) may differ in the set of hit photons.  The widened bound is
+reported: at most 1% of the matched photons (and at least 3) may need it,
+i.e. have an error above the unwidened 1e-4 bound.
 """
 import ctypes as C
 import os
@@ -64,11 +66,21 @@ def compare_replay(g, o, min_hits=20, setup=None):
     # along-path error of the entry point: at most the lateral bound times the slack
     dl = POS_RTOL * scale * slack
     vg = np.maximum(b["dist_travelled"] / np.maximum(b["time"], 1e-9), 0.05)
-    assert np.all(np.abs(a["dist_travelled"] - b["dist_travelled"]) <= POS_RTOL * b["dist_travelled"] + dl + 1e-4)
-    assert np.all(np.abs(a["time"].astype(np.float64) - b["time"]) <= POS_RTOL * np.abs(b["time"]) + dl / vg + 1e-3)
+    ddist = np.abs(a["dist_travelled"] - b["dist_travelled"])
+    dtime = np.abs(a["time"].astype(np.float64) - b["time"])
+    assert np.all(ddist <= POS_RTOL * b["dist_travelled"] + dl + 1e-4)
+    assert np.all(dtime <= POS_RTOL * np.abs(b["time"]) + dl / vg + 1e-3)
     np.testing.assert_allclose(a["direction"], b["direction"], atol=DIR_ATOL, rtol=0)
     np.testing.assert_allclose(a["initial_direction"], b["initial_direction"], atol=DIR_ATOL, rtol=0)
     np.testing.assert_allclose(a["wavelength"], b["wavelength"], rtol=WL_RTOL)
+    # photons that needed the grazing-incidence widening: above the plain bound
+    dl0 = POS_RTOL * scale
+    widened = ((dp > dl0) | (ddist > POS_RTOL * b["dist_travelled"] + dl0 + 1e-4)
+               | (dtime > POS_RTOL * np.abs(b["time"]) + dl0 / vg + 1e-3))
+    n_widened = int(np.sum(widened))
+    print(f"replay: {len(common)} matched, {n_diff} differ in hit/miss, {n_widened} need the widened bound "
+          f"(max slack used {float(np.max(slack[widened])) if n_widened else 1.0:.2f})")
+    assert n_widened <= max(3, int(0.01 * len(b))), f"{n_widened} of {len(b)} photons need the widened bound"
     return len(common)
 
 
@@ -112,9 +124,17 @@ def test_replay_isotropic_close_sphere(orc):
     assert n > 1000
 
 
-def test_replay_point_cone(orc):
-    s = workloads.point_cone_setup(400_000)
-    compare_replay(gpu_hits(s, seed=11), orc.propagate_f64(s, seed=11), min_hits=1, setup=s)
+@pytest.mark.parametrize("seed", [11, 12])
+def test_replay_point_cone(orc, seed):
+    # The 1e6-photon point cone (41.2 degrees about +z, one R = 0.21 m module
+    # 10 m up the axis) is missed by direct light and gives about 16 hits per
+    # 1e6 photons.  1e8 photons under one Philox key are 100 such runs; every
+    # hit photon is replayed by the FP64 oracle (the whole range, on all host
+    # cores), so both directions of the hit set are checked.
+    s = workloads.point_cone_setup(100_000_000)
+    g = nt.propagate_photons(s, seed=seed, reference_columns=False, capacity=1 << 16).sorted_by_photon().records
+    o = orc.propagate_f64(s, seed=seed, threads=os.cpu_count() or 1)
+    assert compare_replay(g, o, min_hits=1000, setup=s) >= 1000
 
 
 def test_replay_cascade_on_pom_string(orc):
@@ -239,26 +259,6 @@ def test_run_stats_counts_steps():
     # photons that hit stop early; the others take all 15 steps
     assert 100_000 * 1 <= st.photon_steps <= 100_000 * 15
     assert st.photon_steps > (100_000 - len(h)) * 15
-
-
-def _chi2_counts(a, b, ids):
-    ca = np.array([np.sum(a == i) for i in ids], dtype=float)
-    cb = np.array([np.sum(b == i) for i in ids], dtype=float)
-    m = (ca + cb) > 0
-    return ca[m], cb[m]
-
-
-def test_statistics_against_float_mirror(orc):
-    # independent seeds: per-module counts within 4 sigma and arrival-time KS p > 0.01
-    from scipy import stats
-    s = cascade_small_setup(2_000_000)
-    g = gpu_hits(s, seed=101)
-    o = orc.propagate_f32(s, seed=202, threads=os.cpu_count() or 1)
-    ids = np.unique(np.concatenate([g["module_id"], o["module_id"]]))
-    ca, cb = _chi2_counts(g["module_id"], o["module_id"], ids)
-    z = (ca - cb) / np.sqrt(ca + cb)
-    assert np.all(np.abs(z) < 4.0), z
-    assert stats.ks_2samp(g["time"], o["time"]).pvalue > 0.01
 
 
 def test_make_hits_matches_oracle(orc):
