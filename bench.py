@@ -19,6 +19,7 @@ import argparse
 import ctypes as C
 import gc
 import json
+import math
 import os
 import statistics
 import subprocess
@@ -78,6 +79,7 @@ def parse():
                     help="comma list of the measurements to run: propagation (the headline line), serving, flow, "
                          "hybrid; compat (the bench cascades in the reference's own water, not in the default "
                          "list) runs when propagation is not among them")
+    ap.add_argument("--details", default=None, help="also write the full per-leg results (JSON) to this path")
     ap.add_argument("--small", action="store_true",
                     help="profiling case: one cascade at 1% of its photons, 64 MB hit buffer, 256 MB L2 flush")
     return ap.parse_args()
@@ -197,9 +199,10 @@ def serving_bench(n_requests: int, budget_bytes: int = 120 * 10 ** 9) -> dict:
 def flow_bench(train_steps: int = 300, n_tuples: int = 100_000_000) -> dict:
     """Flow surrogate workload (5 spline layers of 12 bins on [-20, 1500] ns,
     3 x 256 conditioner, count head, batch 8192, Adam 1e-3):
-      table      -- the MC kernel generates a training table (8192 simulations,
-                    distance 1-200 m log-uniform, direction isotropic, log10 E
-                    2-6, 16 module orientations each) on the device;
+      table      -- the MC kernel generates a training table of about 2e7
+                    rows (65536 simulations, distance 1-200 m log-uniform,
+                    direction isotropic, log10 E 2-6, 16 module orientations
+                    each) on the device;
       training   -- Adam steps on rows of that table already in HBM, run
                     back to back by one multi-step call;
                     samples/s and the conditioner GEMMs' tensor throughput
@@ -218,11 +221,12 @@ def flow_bench(train_steps: int = 300, n_tuples: int = 100_000_000) -> dict:
                     "conditioner on 5 features, BF16 weights / FP32 accumulate and master weights"}
     torch.cuda.synchronize()
     t0 = time.perf_counter()
-    tab = make_flow_table(TableConfig(n_sims=8192, n_orientations=16, target_hits=300, max_photons=10_000_000,
+    n_sims = 65536
+    tab = make_flow_table(TableConfig(n_sims=n_sims, n_orientations=16, target_hits=300, max_photons=10_000_000,
                                       seed=1))
     torch.cuda.synchronize()
     dt = time.perf_counter() - t0
-    out["table"] = {"simulations": 8192, "orientations": 16, "rows": len(tab), "photons": tab.n_photons,
+    out["table"] = {"simulations": n_sims, "orientations": 16, "rows": len(tab), "photons": tab.n_photons,
                     "seconds": dt, "rows_per_s": len(tab) / dt, "photons_per_s": tab.n_photons / dt}
     bs = 8192
     fl = RQNormFlow(RQNormFlowHParams(batch_size=bs), batch_capacity=131072)
@@ -364,61 +368,89 @@ def compat_bench(steps: int = 3, photon_scale: float = 0.25) -> dict:
             "ms_per_step": 1e3 * t / steps}
 
 
-def hybrid_bench(n_events: int = 10_000, batch: int = 256, train_steps: int = 48_000) -> dict:
+def _cosine(lr_max: float, lr_min: float, steps: int):
+    return lambda k: lr_min + 0.5 * (lr_max - lr_min) * (1 + math.cos(math.pi * min(k, steps) / steps))
+
+
+def train_hybrid_models(tab, seed: int, shape_steps: int, count_steps: int):
+    """The hybrid simulator's two models, trained on one MC table: the
+    arrival-time flow (5 spline layers of 12 bins, joint count head with the
+    information-weighted count term, the 5 features) and the count model (the
+    same conditioner with derived input columns, trained on the table's
+    (simulation, orientation, PMT) groups alone, information-weighted).
+    Cosine learning-rate schedules from 1e-3 to 1e-5."""
+    from neutrinotelescopes_gb300.flow import RQNormFlow, RQNormFlowHParams
+    t0 = time.perf_counter()
+    fl = RQNormFlow(RQNormFlowHParams(batch_size=8192, seed=31338 + 101 * seed), batch_capacity=65536)
+    fl.init_from_table(tab)
+    per = len(tab) // 8192
+    sched = _cosine(1e-3, 1e-5, shape_steps)
+    done, ep = 0, 0
+    while done < shape_steps:
+        fl.set_lr(sched(done))
+        done += len(fl.fit_table(tab, epochs=1, seed=1000 * seed + ep, max_steps=min(per, shape_steps - done),
+                                 count_mode="information"))
+        ep += 1
+    t_shape = time.perf_counter() - t0
+    t0 = time.perf_counter()
+    cf = RQNormFlow(RQNormFlowHParams(K=10, n_layers=1, range_min=-20.0, range_max=100.0, batch_size=8192,
+                                      seed=777 + 101 * seed, input_columns="derived"), batch_capacity=8192)
+    import torch
+    cf.init_output_bias(log_expec=float(torch.log1p(tab.group_expec.double()).mean().item()))
+    cf.fit_counts(tab, steps=count_steps, seed=seed, lr_schedule=_cosine(1e-3, 1e-5, count_steps))
+    return fl, cf, {"seed": seed, "shape_steps": shape_steps, "shape_seconds": t_shape, "count_steps": count_steps,
+                    "count_seconds": time.perf_counter() - t0}
+
+
+def hybrid_bench(n_events: int = 10_000, batch: int = 256, shape_steps: int = 48_000, count_steps: int = 24_000,
+                 seeds=(0, 1, 2), eval_per_decade: int = 3, mc_per_decade: int = 2) -> dict:
     """Hybrid serving workload: 10 x 10 strings x 80 POM modules x 16 PMTs
     (50 m, 15 m spacing), n_events cascades with E log-uniform 1e2-1e6 GeV,
     vertex uniform in the detector's bounding box, isotropic direction.  The
-    flow (trained here on an MC table of 8192 simulations, half of them
-    drawn 8-80 m from the module near the Cherenkov angle, each PMT's count
-    weighted by the hits simulated for it) supplies every
-    PMT within 1-200 m of the vertex; events with a module closer than 1 m go
-    to plain MC.  Reported: events/s and per-event latency of the saturated
-    stream (batches of `batch` events), plain MC's events/s on the same
-    stream (its photons/s measured on sample events of this detector, times
-    the stream's mean photons per event), and the error against MC on sample
-    events (expected hits per module, arrival-time KS per module and pooled)."""
-    import math as _m
-
+    surrogate (an arrival-time flow and a count model, trained here on an MC
+    table of 8192 simulations, half of them drawn 8-80 m from the module
+    near the Cherenkov angle) supplies every PMT within 1-200 m of the
+    vertex; events with a module closer than 1 m go to plain MC.
+    Reported: events/s and per-event latency of the saturated stream
+    (batches of `batch` events) and of Poisson arrivals at 1000/s; plain
+    MC's events/s on the same stream, measured on an energy-stratified sample
+    of its events through the MC event server; the error against MC on an
+    energy-stratified sample (per-module expected hits, event hit-time KS
+    against the surrogate's predicted CDF), for models trained from
+    `seeds` (mean and spread over the seeds); the hybrid mode's KS check."""
     import numpy as np
     import torch
 
     from neutrinotelescopes_gb300 import workloads
-    from neutrinotelescopes_gb300.flow import RQNormFlow, RQNormFlowHParams
-    from neutrinotelescopes_gb300.surrogate import HybridSimulator, compare, hybrid_events, mc_truth
+    from neutrinotelescopes_gb300.serving import EventServer
+    from neutrinotelescopes_gb300.surrogate import (HybridSimulator, evaluate_against, hybrid_events,
+                                                    mc_reference)
     from neutrinotelescopes_gb300.tables import TableConfig, make_flow_table
 
     out = {"workload": f"{n_events} cascades 1e2-1e6 GeV, 10 x 10 strings x 80 modules x 16 PMTs (50 m, 15 m), "
-                       "simple water; flow for PMTs 1-200 m from the vertex, MC for events with a module < 1 m"}
+                       "simple water; surrogate for PMTs 1-200 m from the vertex, MC for events with a module "
+                       "< 1 m"}
     tcfg = TableConfig(n_sims=8192, n_orientations=16, target_hits=1000, max_photons=100_000_000, seed=2,
                        focus_fraction=0.5)
     t0 = time.perf_counter()
     tab = make_flow_table(tcfg)
     torch.cuda.synchronize()
-    t_table = time.perf_counter() - t0
-    fl = RQNormFlow(RQNormFlowHParams(batch_size=8192), batch_capacity=65536)
-    fl.init_from_table(tab)
-    per = len(tab) // 8192
-    done, ep = 0, 0
-    t0 = time.perf_counter()
-    while done < train_steps:
-        fl.set_lr(1e-5 + 0.5 * (1e-3 - 1e-5) * (1 + _m.cos(_m.pi * done / train_steps)))
-        done += len(fl.fit_table(tab, epochs=1, seed=ep, max_steps=min(per, train_steps - done),
-                                 count_mode="information"))
-        ep += 1
-    out["training"] = {"table_simulations": tcfg.n_sims, "table_photons": int(tab.n_photons),
-                       "table_rows": len(tab), "table_seconds": t_table, "steps": done,
-                       "count_mode": "information", "seconds": time.perf_counter() - t0}
+    out["table"] = {"simulations": tcfg.n_sims, "photons": int(tab.n_photons), "rows": len(tab),
+                    "seconds": time.perf_counter() - t0}
+    models = [train_hybrid_models(tab, sd, shape_steps, count_steps) for sd in seeds]
+    out["training"] = [m[2] for m in models]
     del tab
     torch.cuda.empty_cache()
     setup = workloads.hybrid_setup()
-    sim = HybridSimulator(setup, fl, seed=workloads.SEED_BASE + 4)
     events = hybrid_events(n_events, setup)
+    fl, cf = models[0][0], models[0][1]
+    sim = HybridSimulator(setup, fl, count_flow=cf, seed=workloads.SEED_BASE + 4)
     sim.simulate(events[:8])  # warm-up
     torch.cuda.synchronize()
     t0 = time.perf_counter()
     lat, n_flow, n_mc, n_hits = [], 0, 0, 0
-    for s in range(0, n_events, batch):
-        res = sim.simulate(events[s:s + batch])
+    for s0 in range(0, n_events, batch):
+        res = sim.simulate(events[s0:s0 + batch])
         torch.cuda.synchronize()
         t = time.perf_counter() - t0
         for r in res:
@@ -436,91 +468,150 @@ def hybrid_bench(n_events: int = 10_000, batch: int = 256, train_steps: int = 48
     rng = np.random.default_rng(9)
     n_rt = min(n_events, 4000)
     arr = np.cumsum(rng.exponential(1e-3, n_rt))
-    # a short replay first (buffer growth at batch sizes the saturated run did not see)
     sim.serve([(float(arr[i]), *events[n_events - 1 - i]) for i in range(200)], max_batch=64)
     gc.collect()
     res_rt = sim.serve([(float(arr[i]), *events[i]) for i in range(n_rt)], max_batch=64)
     lat_rt = np.array([r[2] for r in res_rt])
-    worst = int(np.argmax(lat_rt))
     out["realtime"] = {"arrival_rate_hz": 1000.0, "events": n_rt,
                        "events_per_s": n_rt / (float(arr[-1]) + lat_rt[-1]),
                        "latency_p50_ms": float(np.percentile(lat_rt, 50) * 1e3),
                        "latency_p99_ms": float(np.percentile(lat_rt, 99) * 1e3),
-                       "latency_max_ms": float(lat_rt[worst] * 1e3),
-                       "events_mc": int(sum(r[1] == "mc" for r in res_rt)),
-                       "worst_event": {"index": worst, "method": res_rt[worst][1],
-                                       "log10_energy": float(events[worst][2])}}
-    # the KS check of the hybrid mode: every 25th flow event also through
-    # (oversampled) MC, one-sample KS against the flow's predicted hit-time
-    # distribution; plain MC from the first check whose distance, less the
-    # MC sample's own 95 % noise bound, is above 0.02
-    chk = HybridSimulator(setup, fl, seed=workloads.SEED_BASE + 6, ks_check_every=25, ks_threshold=0.02)
-    chk_events = [e for e in events if e[2] <= 4.0][:100]
-    t1 = time.perf_counter()
-    res_chk = []
-    for s0 in range(0, len(chk_events), 25):
-        res_chk += chk.simulate(chk_events[s0:s0 + 25])
-    out["ks_check"] = {"threshold": 0.02, "every": 25, "events": len(chk_events),
-                       "confidence": chk.ks_confidence,
-                       "checks": [{"event": int(a), "ks": float(b), "mc_hits": int(c),
-                                   "mc_noise_bound": chk.ks_noise_bound(c), "fails": chk.ks_fails(b, c)}
-                                  for a, b, c in chk.checks],
-                       "fell_back_to_mc": chk.fallback,
-                       "events_mc": int(sum(r.method == "mc" for r in res_chk)),
-                       "seconds": time.perf_counter() - t1}
-    # one batch alone: the latency of an event served on arrival with a batch of its own
+                       "latency_max_ms": float(lat_rt.max() * 1e3),
+                       "events_mc": int(sum(r[1] == "mc" for r in res_rt))}
     torch.cuda.synchronize()
     t1 = time.perf_counter()
     sim.simulate(events[:1])
     torch.cuda.synchronize()
     out["single_event_latency_ms"] = (time.perf_counter() - t1) * 1e3
-    # plain MC serving on the same GPU and detector: the continuous-batching
-    # server's photons/s on a sample of the stream, events/s of the stream
-    from neutrinotelescopes_gb300.serving import EventServer
-    mean_photons = float(np.mean([e[1].photons for e in events]))
-    sample = [e for e in events if 3.0 <= e[2] <= 4.0][:16]
-    srv = EventServer(setup, hbm_budget_bytes=60 * 10 ** 9, seed=workloads.SEED_BASE + 5,
-                      reserve_hits_per_photon=5e-3, min_reserve_hits=4096, max_batch_photons=2_000_000_000)
-    for e in sample:
-        srv.submit(e[0], e[1])
-    t_a = srv.stats().clock
-    res_mc = srv.run_all()
-    mc_dt = max(r.t_done for r in res_mc) - t_a
-    srv.close()
-    ph = sum(e[1].photons for e in sample)
-    mc_rate = ph / mc_dt
-    out["plain_mc"] = {"photons_per_s": mc_rate, "mean_photons_per_event": mean_photons,
-                       "events_per_s": mc_rate / mean_photons,
-                       "sample": f"{len(sample)} events of 1e3-1e4 GeV ({ph:.3g} photons) through the MC event "
-                                 f"server, hits kept on the device"}
+
+    # energy strata of the stream (decades of E)
+    le_all = np.array([e[2] for e in events])
+    edges = [2.0, 3.0, 4.0, 5.0, 6.0 + 1e-9]
+    frac = [float(np.mean((le_all >= a) & (le_all < b))) for a, b in zip(edges[:-1], edges[1:])]
+
+    def stratum(k, count, skip=0):
+        a, b = edges[k], edges[k + 1]
+        return [e for e in events if a <= e[2] < b][skip:skip + count]
+
+    # plain MC serving on the same GPU and detector: per decade the MC event
+    # server's time for a few of the stream's events; events/s of the stream
+    # = 1 / sum_d (share of decade d) x (mean time of an event of decade d)
+    mc_rows, t_mean = [], 0.0
+    for k in range(4):
+        sample = stratum(k, mc_per_decade)
+        srv = EventServer(setup, hbm_budget_bytes=120 * 10 ** 9, seed=workloads.SEED_BASE + 5,
+                          reserve_hits_per_photon=2e-3, min_reserve_hits=4096, max_batch_photons=2_000_000_000)
+        for e in sample:
+            srv.submit(e[0], e[1])
+        t_a = srv.stats().clock
+        res_mc = srv.run_all()
+        mc_dt = max(r.t_done for r in res_mc) - t_a
+        srv.close()
+        ph = sum(e[1].photons for e in sample)
+        per_event = mc_dt / len(sample)
+        t_mean += frac[k] * per_event
+        mc_rows.append({"log10_energy": [edges[k], round(edges[k + 1], 3)], "events": len(sample),
+                        "photons": ph, "seconds_per_event": per_event, "photons_per_s": ph / mc_dt,
+                        "stream_share": frac[k]})
+    out["plain_mc"] = {"events_per_s": 1.0 / t_mean, "strata": mc_rows,
+                       "note": "events/s of the stream from the per-decade mean MC time of its events (MC event "
+                               "server, hits kept on the device)"}
     out["speedup_vs_plain_mc"] = out["saturated"]["events_per_s"] / out["plain_mc"]["events_per_s"]
-    # error against MC on sample events
-    errs, ksm, ksp, kspred = [], [], [], []
-    for e in [e for e in events if 3.0 <= e[2] <= 4.0][:14]:
-        c = compare(sim, e[1], e[2], e[0], seed=e[0], oversample=8)
-        if c.get("modules"):
-            errs.extend(list(c["expected_rel_err"]))
-            ksm.extend(list(c["ks_modules"]))
-            ksp.append(c["ks_pooled"])
-            kspred.append((c["ks_predicted"], c["ks_predicted_mc_hits"], c["ks_predicted_bound"]))
-    errs, ksm = np.abs(np.array(errs)), np.array(ksm)
-    out["error_vs_mc"] = {"ks_threshold_of_the_mc_fallback": 0.02,
-                          "events": len(ksp), "modules_expected_ge_100": int(errs.size),
-                          "expected_hits_rel_err_median": float(np.median(errs)) if errs.size else None,
-                          "expected_hits_rel_err_p90": float(np.quantile(errs, 0.9)) if errs.size else None,
-                          "ks_per_module_median": float(np.median(ksm)) if ksm.size else None,
-                          "ks_pooled_median": float(np.median(ksp)) if ksp else None,
-                          "ks_predicted": [{"ks": float(a), "mc_hits": int(b), "mc_noise_bound": float(d)}
-                                           for a, b, d in kspred],
-                          "ks_predicted_median": float(np.median([a for a, _, _ in kspred])) if kspred else None,
-                          "note": "expected hits: MC of 8x the event's photons (sum of weights / 8), modules "
-                                  "with >= 100 expected hits; ks_pooled: flow sample vs MC sample of the event "
-                                  "(~1e3 flow hits, noise ~0.03); ks_predicted: oversampled MC hits vs the "
-                                  "flow's predicted hit-time CDF (MC noise ~0.87/sqrt(mc_hits), 95 % bound "
-                                  "mc_noise_bound)"}
+
+    # error against MC: energy-stratified events, one MC reference each,
+    # every trained model judged against the same references
+    t1 = time.perf_counter()
+    refs = []
+    for k in range(4):
+        for e in stratum(k, eval_per_decade, skip=mc_per_decade):
+            refs.append(mc_reference(sim, e[1], e[2], e[0], seed=workloads.SEED_BASE + 77 + e[0]))
+    per_seed = []
+    for fl_s, cf_s, _ in models:
+        sim_s = HybridSimulator(setup, fl_s, count_flow=cf_s, seed=workloads.SEED_BASE + 4)
+        ev = [evaluate_against(sim_s, r) for r in refs]
+        errs = np.abs(np.concatenate([v["rel_err"] for v in ev]))
+        ks = np.array([v["ks"] for v in ev if v["mc_hits"] > 0])
+        eps = np.array([v["ks_noise_bound"] for v in ev if v["mc_hits"] > 0])
+        dec = []
+        for k in range(4):
+            idx = [i for i, r in enumerate(refs) if edges[k] <= r["log10_energy"] < edges[k + 1]]
+            e_k = np.abs(np.concatenate([ev[i]["rel_err"] for i in idx])) if idx else np.zeros(0)
+            dec.append({"log10_energy": [edges[k], round(edges[k + 1], 3)], "modules": int(e_k.size),
+                        "rel_err_median": float(np.median(e_k)) if e_k.size else None,
+                        "ks_max": float(np.nanmax([ev[i]["ks"] for i in idx])) if idx else None})
+        per_seed.append({"rel_err_median": float(np.median(errs)), "rel_err_p90": float(np.quantile(errs, 0.9)),
+                         "modules": int(errs.size),
+                         "event_total_rel_err_max": float(np.max(np.abs([v["event_expected_rel_err"] for v in ev]))),
+                         "ks_median": float(np.median(ks)), "ks_max": float(np.max(ks)),
+                         "ks_minus_noise_max": float(np.max(ks - eps)), "decades": dec})
+    agg = lambda key: {"mean": float(np.mean([p[key] for p in per_seed])),  # noqa: E731
+                       "sd": float(np.std([p[key] for p in per_seed], ddof=1)) if len(per_seed) > 1 else 0.0}
+    out["error_vs_mc"] = {
+        "events": len(refs), "per_decade": eval_per_decade, "seeds": len(per_seed),
+        "rel_err_median": agg("rel_err_median"), "rel_err_p90": agg("rel_err_p90"),
+        "ks_median": agg("ks_median"), "ks_max": agg("ks_max"), "ks_minus_noise_max": agg("ks_minus_noise_max"),
+        "per_seed": per_seed, "seconds": time.perf_counter() - t1,
+        "note": "per-module expected hits (count model) against MC where the MC module estimate rests on >= 1e4 "
+                "simulated hits (MC noise ~1 %); ks: one-sample KS of the event's MC hit times against the "
+                "predicted hit-time CDF (raw distance; ks_minus_noise subtracts the MC sample's 95 % DKW bound)"}
+    # the hybrid mode's KS check: every 25th flow event also through
+    # oversampled MC; plain MC from the first check whose distance, less the
+    # MC sample's own 95 % noise bound, is above 0.02
+    chk = HybridSimulator(setup, fl, count_flow=cf, seed=workloads.SEED_BASE + 6, ks_check_every=25,
+                          ks_threshold=0.02)
+    chk_events = [e for e in events if e[2] <= 4.0][:100]
+    t1 = time.perf_counter()
+    res_chk = []
+    for s0 in range(0, len(chk_events), 25):
+        res_chk += chk.simulate(chk_events[s0:s0 + 25])
+    raw = [float(b) for _, b, _ in chk.checks]
+    out["ks_check"] = {"threshold": 0.02, "every": 25, "events": len(chk_events), "confidence": chk.ks_confidence,
+                       "checks": len(chk.checks), "ks_raw_max": max(raw) if raw else None,
+                       "raw_at_most_threshold": int(sum(r <= 0.02 for r in raw)),
+                       "fails_after_noise_bound": int(sum(chk.ks_fails(b, c) for _, b, c in chk.checks)),
+                       "fell_back_to_mc": chk.fallback, "events_mc": int(sum(r.method == "mc" for r in res_chk)),
+                       "seconds": time.perf_counter() - t1,
+                       "note": "a check fails when its raw distance minus the MC sample's 95 % noise bound is above "
+                               "the threshold; raw_at_most_threshold counts checks with the raw distance itself "
+                               "<= 0.02"}
     setup.close()
-    fl.close()
+    for a, b, _ in models:
+        a.close()
+        b.close()
     return out
+
+
+def legs_summary(out: dict) -> dict:
+    """The headline numbers of every leg in a few keys, printed last on the
+    JSON line so that a tail of the line keeps them."""
+    s = {}
+    sv = out.get("serving")
+    if sv:
+        s["serving"] = {"events_per_s": sv["saturated"]["events_per_s"],
+                        "p50_ms_at_200hz": sv["realtime"]["latency_p50_ms"],
+                        "p99_ms_at_200hz": sv["realtime"]["latency_p99_ms"]}
+    fl = out.get("flow")
+    if fl:
+        s["flow"] = {"table_rows": fl["table"]["rows"], "train_samples_per_s": fl["training"]["samples_per_s"],
+                     "train_tflops": fl["training"]["roofline"]["achieved"],
+                     "train_frac_of_bf16_sustained": fl["training"]["roofline"]["frac"],
+                     "infer_tuples_per_s": fl["inference"]["tuples_per_s"],
+                     "infer_e2e_tuples_per_s": fl["inference"]["e2e"]["tuples_per_s"]}
+    hy = out.get("hybrid")
+    if hy:
+        err = hy["error_vs_mc"]
+        s["hybrid"] = {"events_per_s": hy["saturated"]["events_per_s"],
+                       "p50_ms_at_1000hz": hy["realtime"]["latency_p50_ms"],
+                       "p99_ms_at_1000hz": hy["realtime"]["latency_p99_ms"],
+                       "plain_mc_events_per_s": hy["plain_mc"]["events_per_s"],
+                       "speedup_vs_plain_mc": hy["speedup_vs_plain_mc"],
+                       "count_err_median": [err["rel_err_median"]["mean"], err["rel_err_median"]["sd"]],
+                       "count_err_p90": [err["rel_err_p90"]["mean"], err["rel_err_p90"]["sd"]],
+                       "ks_median": [err["ks_median"]["mean"], err["ks_median"]["sd"]],
+                       "ks_max": [err["ks_max"]["mean"], err["ks_max"]["sd"]],
+                       "seeds": err["seeds"], "events_judged": err["events"],
+                       "ks_checks_raw_le_0.02": [hy["ks_check"]["raw_at_most_threshold"], hy["ks_check"]["checks"]]}
+    return s
 
 
 def _measured_peak(key: str, fallback: float):
@@ -560,23 +651,45 @@ def barrier(world: int):
         dist.barrier()
 
 
+def sample_ranges(setup, n: int) -> list[tuple[int, int]]:
+    """Photon-index ranges of a bounded sample of n photons spread over every
+    source in proportion to its photons (the first photons of each source),
+    so that the sample has the workload's mix of cascades."""
+    counts = [int(s.photons) for s in setup.sources]
+    total = sum(counts)
+    out, first = [], 0
+    for c in counts:
+        k = min(c, int(round(n * c / total))) if total else 0
+        if k > 0:
+            out.append((first, first + k))
+        first += c
+    return out
+
+
+def run_ranges(oracle, setup, seed: int, ranges, threads: int) -> int:
+    """The oracle's single-precision port over the ranges; photons simulated."""
+    for b, e in ranges:
+        oracle.propagate_f32(setup, seed=seed, gid_begin=b, gid_end=e, threads=threads)
+    return sum(e - b for b, e in ranges)
+
+
 def cpu_baseline(setup, seconds: float, threads: int) -> dict:
     """The oracle's single-precision port on the host cores, on a bounded
-    sample (the first photons of the step's sources)."""
+    sample spread over all of the step's sources."""
     import oracle
     oracle.build()
     total = sum(int(s.photons) for s in setup.sources)
-    n = 20_000
+    n = 40_000
     t0 = time.perf_counter()
-    oracle.propagate_f32(setup, seed=7, gid_begin=0, gid_end=n, threads=threads)
+    n = run_ranges(oracle, setup, 7, sample_ranges(setup, n), threads)
     dt = time.perf_counter() - t0
     n = int(min(total, max(n, n * seconds / max(dt, 1e-6))))
     t0 = time.perf_counter()
-    oracle.propagate_f32(setup, seed=8, gid_begin=0, gid_end=n, threads=threads)
+    n = run_ranges(oracle, setup, 8, sample_ranges(setup, n), threads)
     dt = time.perf_counter() - t0
     return {"value": n / dt, "unit": METRIC, "cores": threads, "kind": "port",
-            "sample": f"first {n} photons of the step's cascades (of {total}), {dt:.1f} s, single-precision "
-                      f"oracle port, OpenMP"}
+            "sample": f"{n} photons of the step's {len(setup.sources)} cascades in proportion to their photons "
+                      f"(of {total}), {dt:.1f} s, single-precision oracle port, OpenMP"}
 
 
 def run_reference(args, world, rank):
@@ -591,17 +704,17 @@ def run_reference(args, world, rank):
     setup = workloads.cascade_string_setup(N_CASCADES, WORKLOAD_SEED)
     threads = os.cpu_count() or 1
     total = sum(int(s.photons) for s in setup.sources)
-    n = 20_000
     t0 = time.perf_counter()
-    oracle.propagate_f32(setup, seed=1, gid_begin=0, gid_end=n, threads=threads)
+    n = run_ranges(oracle, setup, 1, sample_ranges(setup, 40_000), threads)
     per = (time.perf_counter() - t0) / n
-    n = int(min(total, max(n, 5.0 / per)))
+    ranges = sample_ranges(setup, int(min(total, max(n, 5.0 / per))))
+    n = sum(e - b for b, e in ranges)
     for i in range(args.warmup):
-        oracle.propagate_f32(setup, seed=100 + i, gid_begin=0, gid_end=min(n, 20_000), threads=threads)
+        run_ranges(oracle, setup, 100 + i, sample_ranges(setup, 40_000), threads)
     times = []
     for i in range(args.steps):
         t0 = time.perf_counter()
-        oracle.propagate_f32(setup, seed=1000 + i, gid_begin=0, gid_end=n, threads=threads)
+        run_ranges(oracle, setup, 1000 + i, ranges, threads)
         times.append(time.perf_counter() - t0)
     value = n * len(times) / sum(times)
     out = {"metric": METRIC, "value": value, "unit": METRIC, "impl": "reference", "n_gpus": args.gpus,
@@ -611,7 +724,8 @@ def run_reference(args, world, rank):
            "config": {"workload": "cascade_string: 4 EM cascades 1e3-1e5 GeV, 20 POM modules, simple water",
                       "photons_per_step": n, "sample_of": total},
            "cpu_baseline": {"value": value, "unit": METRIC, "cores": threads, "kind": "port",
-                            "sample": f"first {n} photons of the workload per step"},
+                            "sample": f"{n} photons per step over the workload's {len(setup.sources)} cascades "
+                                      f"in proportion to their photons"},
            "e2e": {"value": value, "unit": METRIC, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(out))
 
@@ -642,6 +756,9 @@ def main():
         if "compat" in legs and rank == 0:
             out["compat_medium"] = compat_bench()
         if rank == 0:
+            if args.details:
+                Path(args.details).write_text(json.dumps(out, indent=1))
+            out["legs"] = legs_summary(out)
             print(json.dumps(out))
         return
     if args.small:
@@ -738,6 +855,12 @@ def main():
         out["cpu_baseline"] = cpu_baseline(workloads.cascade_string_setup(N_CASCADES, WORKLOAD_SEED),
                                            args.cpu_seconds, os.cpu_count() or 1)
     if rank == 0:
+        if args.details:
+            Path(args.details).write_text(json.dumps(out, indent=1))
+        hy = out.get("hybrid")
+        if hy:  # the per-seed breakdown stays in the details file
+            hy["error_vs_mc"] = {k: v for k, v in hy["error_vs_mc"].items() if k != "per_seed"}
+        out["legs"] = legs_summary(out)
         print(json.dumps(out))
     if world > 1:
         import torch.distributed as dist

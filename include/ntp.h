@@ -20,7 +20,7 @@
 extern "C" {
 #endif
 
-#define NTP_ABI_VERSION 1
+#define NTP_ABI_VERSION 2
 
 typedef enum ntp_status {
     NTP_OK = 0,
@@ -424,7 +424,8 @@ ntp_status ntp_gemm_set_wait_limit(uint64_t wait_limit_ns, int32_t withhold_firs
  * log expectation; n_layers stacked inverse splines (1 = the reference's
  * model).  Weights BF16 on the tensor cores with FP32 accumulation, FP32
  * master weights and Adam (Flux's defaults).  Parameters form one flat FP32
- * vector: W1 [256 x 64] (only the first 5 input columns used), b1 [256],
+ * vector: W1 [256 x 64] (only the first 5 input columns used, 9 with
+ * derived columns), b1 [256],
  * W2 [256 x 256], b2, W3 [256 x 256], b3, W4 [n_outputs_padded x 256], b4;
  * rows of W4 beyond n_outputs stay zero. */
 typedef struct ntp_flow ntp_flow;
@@ -438,7 +439,21 @@ typedef struct ntp_flow_config {
     float grad_clip;        /* per-sample bound on |dL/draw outputs| x batch (0 = none), e.g. 1e3 */
     float count_weight;     /* weight of the Poisson count term in the loss (1 = the reference's)  */
     uint64_t seed;          /* weight initialisation                                           */
+    int32_t input_columns;  /* enum ntp_flow_input                                              */
+    int32_t reserved;
 } ntp_flow_config;
+
+/* Input columns of the conditioner.  FEATURES: the 5 condition features.
+   DERIVED: the features and four functions of them, computed on the device
+   when the conditions are packed -- the distance / 100 m, the source
+   direction's cosine minus the Cherenkov cosine 1/1.35 and its square, and
+   sin(theta_pmt) cos(phi); a count-only model (hit expectations, trained
+   without time rows) learns the steep count function much better with them,
+   while they hurt the time shapes of a joint model. */
+enum ntp_flow_input {
+    NTP_FLOW_INPUT_FEATURES = 0,
+    NTP_FLOW_INPUT_DERIVED = 1
+};
 
 ntp_status ntp_flow_create(int32_t device, const ntp_flow_config* config, ntp_flow** out);
 void ntp_flow_destroy(ntp_flow* flow);
@@ -528,6 +543,14 @@ ntp_status ntp_flow_mixture_cdf(ntp_flow* flow, const float* cond, int32_t n_con
 ntp_status ntp_flow_sample(ntp_flow* flow, const float* cond, int32_t n_cond, const uint64_t* cond_key, uint64_t seed,
                            uint64_t* counts, int32_t* hit_cond, float* hit_time, uint64_t capacity, uint64_t* n_hits,
                            int32_t on_device);
+/* ntp_flow_sample with the counts drawn from the given log expectations
+   (log_expec [n_cond], host or device as the other buffers; NULL = the
+   flow's own count head) instead of this flow's: the hybrid simulator takes
+   a PMT's expected hits from a separate count model and its arrival times
+   from this flow.  A later ntp_flow_sample_resume draws the same hits. */
+ntp_status ntp_flow_sample_expec(ntp_flow* flow, const float* cond, int32_t n_cond, const uint64_t* cond_key,
+                                 uint64_t seed, const float* log_expec, uint64_t* counts, int32_t* hit_cond,
+                                 float* hit_time, uint64_t capacity, uint64_t* n_hits, int32_t on_device);
 /* The hits of the last ntp_flow_sample call that returned NTP_ERR_OVERFLOW,
    into buffers of at least its *n_hits entries (the same hits that call
    would have written).  Any other call on the flow in between discards the

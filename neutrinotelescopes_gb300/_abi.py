@@ -15,7 +15,7 @@ import numpy as np
 PKG = Path(__file__).resolve().parent
 LIB_PATH = PKG / "libntp.so"
 
-NTP_ABI_VERSION = 1
+NTP_ABI_VERSION = 2
 
 # ntp_status
 NTP_OK = 0
@@ -44,6 +44,10 @@ SPEC_MONOCHROMATIC = 0
 SPEC_TABLE_LINEAR = 1
 SPEC_TABLE_TEXTURE = 2
 SPEC_INV_SQUARE = 3
+
+# ntp_flow_input
+FLOW_INPUT_FEATURES = 0
+FLOW_INPUT_DERIVED = 1
 
 # ntp_hit_policy / flags
 HIT_FIRST_IN_LIST = 0
@@ -198,6 +202,8 @@ class NtpFlowConfig(C.Structure):
         ("grad_clip", C.c_float),
         ("count_weight", C.c_float),
         ("seed", C.c_uint64),
+        ("input_columns", C.c_int32),
+        ("reserved", C.c_int32),
     ]
 
 
@@ -271,6 +277,7 @@ EXPORTED = (
     "ntp_flow_head",
     "ntp_flow_evaluate",
     "ntp_flow_sample",
+    "ntp_flow_sample_expec",
     "ntp_flow_evaluate_grid",
     "ntp_server_create",
     "ntp_server_destroy",
@@ -342,12 +349,13 @@ def _declare(lib: C.CDLL) -> None:
     lib.ntp_flow_head.argtypes = [vp, vp, vp, vp, vp, vp, i32, C.POINTER(C.c_double), vp]
     lib.ntp_flow_evaluate.argtypes = [vp, vp, i32, vp, vp, u64, vp, vp, i32]
     lib.ntp_flow_sample.argtypes = [vp, vp, i32, vp, u64, vp, vp, vp, u64, C.POINTER(u64), i32]
+    lib.ntp_flow_sample_expec.argtypes = [vp, vp, i32, vp, u64, vp, vp, vp, vp, u64, C.POINTER(u64), i32]
     lib.ntp_flow_sample_resume.argtypes = [vp, vp, vp, u64, C.POINTER(u64), i32]
     lib.ntp_flow_evaluate_grid.argtypes = [vp, vp, i32, vp, i32, vp, vp, i32]
     for name in ("ntp_flow_create", "ntp_flow_get_layout", "ntp_flow_set_params", "ntp_flow_get_params",
                  "ntp_flow_train_step", "ntp_flow_forward", "ntp_flow_head", "ntp_flow_evaluate",
                  "ntp_flow_sample", "ntp_flow_evaluate_grid", "ntp_flow_train_steps", "ntp_flow_mixture_cdf",
-                 "ntp_flow_sample_resume"):
+                 "ntp_flow_sample_resume", "ntp_flow_sample_expec"):
         getattr(lib, name).restype = C.c_int
     lib.ntp_server_create.argtypes = [vp, C.POINTER(NtpServerConfig), C.POINTER(vp)]
     lib.ntp_server_destroy.argtypes = [vp]

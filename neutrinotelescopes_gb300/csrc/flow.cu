@@ -47,7 +47,11 @@ namespace ntp {
 namespace {
 
 constexpr int kCond = 5;
+constexpr int kDerived = 4;    // derived input columns of NTP_FLOW_INPUT_DERIVED
 constexpr int kIn = 64;        // padded input width (one K slice of the GEMM)
+constexpr float kHalfLog200 = 2.6491586832740182f;  // ln(200) / 2
+constexpr float kCherenkovCos = 0.74074074f;         // 1 / 1.35
+constexpr float kPi = 3.14159265358979f;
 constexpr int kMaxLayers = 5;
 constexpr float kMinBin = 1e-4f, kMinSlope = 1e-4f;
 constexpr float kLog2Pi = 1.8378770664093453f;
@@ -334,14 +338,32 @@ __device__ __forceinline__ float warp_sum(float x) {
 }
 
 // ------------------------------------------------------------------- kernels
+// Input column j of a condition row f[0..4] (the normalised features: log
+// distance over 1-200 m, cos theta of the source direction, cos theta of the
+// PMT axis, azimuth, log10 E).  With derived columns (input mode
+// NTP_FLOW_INPUT_DERIVED) four more follow, functions of the features that a
+// count model otherwise has to build from them: the distance in units of
+// 100 m, the source direction's cosine offset from the Cherenkov cosine
+// 1 / 1.35 and its square, and sin(theta_pmt) cos(phi).
+__device__ __forceinline__ float input_column(const float* __restrict__ f, int j, int mode) {
+    if (j < kCond) return f[j];
+    if (mode != NTP_FLOW_INPUT_DERIVED || j >= kCond + kDerived) return 0.0f;
+    switch (j - kCond) {
+    case 0: return expf((f[0] + 1.0f) * kHalfLog200) * 0.01f;
+    case 1: return f[1] + kCherenkovCos;
+    case 2: { const float c = f[1] + kCherenkovCos; return c * c; }
+    default: return sqrtf(fmaxf(1.0f - f[2] * f[2], 0.0f)) * cosf(kPi * (f[3] + 1.0f));
+    }
+}
+
 // cond [n x 5] FP32 -> X [n x 64] BF16 (zero padded) and X^T [64 x n];
 // rows >= n_valid are zero
-__global__ void pack_kernel(const float* __restrict__ cond, int n_valid, int n, __nv_bfloat16* __restrict__ x,
-                            __nv_bfloat16* __restrict__ xt) {
+__global__ void pack_kernel(const float* __restrict__ cond, int n_valid, int n, int mode,
+                            __nv_bfloat16* __restrict__ x, __nv_bfloat16* __restrict__ xt) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n * kIn) return;
     const int b = i / kIn, j = i % kIn;
-    const __nv_bfloat16 v = __float2bfloat16(j < kCond && b < n_valid ? cond[b * kCond + j] : 0.0f);
+    const __nv_bfloat16 v = __float2bfloat16(b < n_valid ? input_column(cond + b * kCond, j, mode) : 0.0f);
     x[i] = v;
     xt[static_cast<size_t>(j) * n + b] = v;
 }
@@ -921,6 +943,7 @@ struct ntp_flow {
     cudaEvent_t ev[5] = {};
     int cap = 0;  // batch capacity (multiple of 128)
     int L = 1, K = 12, n_out = 0, n_pad = 0;
+    int in_mode = NTP_FLOW_INPUT_FEATURES;  // input columns: the features, or with the derived ones
     float r0 = -20.0f, r1 = 1500.0f;
     float lr = 1e-3f, b1 = 0.9f, b2 = 0.999f, eps = 1e-8f;
     float clip = 1e3f;  // per-sample bound on |dL/dP| times the batch size (0 = none)
@@ -1036,8 +1059,8 @@ ntp_status pack(ntp_flow* f, const float* cond, int n_valid, int n, int on_devic
         F_CUDA(f, cudaMemcpyAsync(f->cond, cond, sizeof(float) * kCond * n_valid, cudaMemcpyHostToDevice, f->stream));
         dc = f->cond;
     }
-    ntp::pack_kernel<<<ntp::blocks_for(static_cast<long long>(n) * kIn), 256, 0, f->stream>>>(dc, n_valid, n, f->x,
-                                                                                               f->xt);
+    ntp::pack_kernel<<<ntp::blocks_for(static_cast<long long>(n) * kIn), 256, 0, f->stream>>>(
+        dc, n_valid, n, f->in_mode, f->x, f->xt);
     F_CUDA(f, cudaGetLastError());
     return NTP_OK;
 }
@@ -1192,10 +1215,12 @@ ntp_status ntp_flow_create(int32_t device, const ntp_flow_config* cfg, ntp_flow*
         (cfg->n_bins != 10 && cfg->n_bins != 12) ||
         cfg->n_layers > ntp::kMaxLayers || !(cfg->t_max > cfg->t_min) || !(cfg->lr > 0.0f) ||
         !(cfg->beta1 >= 0.0f && cfg->beta1 < 1.0f) || !(cfg->beta2 >= 0.0f && cfg->beta2 < 1.0f) ||
-        !(cfg->eps > 0.0f) || !(cfg->grad_clip >= 0.0f) || !(cfg->count_weight >= 0.0f))
+        !(cfg->eps > 0.0f) || !(cfg->grad_clip >= 0.0f) || !(cfg->count_weight >= 0.0f) ||
+        (cfg->input_columns != NTP_FLOW_INPUT_FEATURES && cfg->input_columns != NTP_FLOW_INPUT_DERIVED))
         return NTP_ERR_INVALID;
     ntp_flow* f = new ntp_flow();
     f->device = device;
+    f->in_mode = cfg->input_columns;
     f->cap = cfg->batch_capacity;
     f->L = cfg->n_layers;
     f->K = cfg->n_bins;
@@ -1262,12 +1287,13 @@ ntp_status ntp_flow_create(int32_t device, const ntp_flow_config* cfg, ntp_flow*
     std::mt19937_64 rng(cfg->seed);
     for (int l = 0; l < 4; ++l) {
         const Block& b = f->blk[2 * l];
-        const int fan_in = l == 0 ? kCond : b.cols;
+        const int n_in = kCond + (f->in_mode == NTP_FLOW_INPUT_DERIVED ? ntp::kDerived : 0);
+        const int fan_in = l == 0 ? n_in : b.cols;
         const float lim = std::sqrt(6.0f / fan_in) * (l == 3 ? 0.1f : 1.0f);
         std::uniform_real_distribution<float> u(-lim, lim);
         for (int r = 0; r < b.rows; ++r)
             for (int c = 0; c < b.cols; ++c) {
-                const bool pad = (l == 0 && c >= kCond) || (l == 3 && r >= f->n_out);
+                const bool pad = (l == 0 && c >= n_in) || (l == 3 && r >= f->n_out);
                 const float val = u(rng);
                 th[b.off + static_cast<size_t>(r) * b.cols + c] = pad ? 0.0f : val;
             }
@@ -1592,6 +1618,13 @@ ntp_status sample_draw(ntp_flow* f, int n_cond, uint2 key, unsigned long long to
 ntp_status ntp_flow_sample(ntp_flow* f, const float* cond, int32_t n_cond, const uint64_t* cond_key, uint64_t seed,
                            uint64_t* counts, int32_t* hit_cond, float* hit_time, uint64_t capacity, uint64_t* n_hits,
                            int32_t on_device) {
+    return ntp_flow_sample_expec(f, cond, n_cond, cond_key, seed, nullptr, counts, hit_cond, hit_time, capacity,
+                                 n_hits, on_device);
+}
+
+ntp_status ntp_flow_sample_expec(ntp_flow* f, const float* cond, int32_t n_cond, const uint64_t* cond_key,
+                                 uint64_t seed, const float* log_expec, uint64_t* counts, int32_t* hit_cond,
+                                 float* hit_time, uint64_t capacity, uint64_t* n_hits, int32_t on_device) {
     if (n_hits) *n_hits = 0;
     if (!f || !cond || !cond_key || n_cond <= 0) return NTP_ERR_INVALID;
     if (n_cond > (1 << 20)) {
@@ -1602,6 +1635,11 @@ ntp_status ntp_flow_sample(ntp_flow* f, const float* cond, int32_t n_cond, const
     cudaStream_t st = f->stream;
     // knots of every condition (the inference pass of ntp_flow_evaluate)
     F_OK(ntp_flow_evaluate(f, cond, n_cond, nullptr, nullptr, 0, nullptr, nullptr, on_device));
+    if (log_expec) {  // the counts' expectations from the caller: into each knot row's last slot
+        const int row = ntp::knot_row(f->L, f->K);
+        F_CUDA(f, cudaMemcpy2DAsync(f->knots + row - 1, sizeof(float) * row, log_expec, sizeof(float), sizeof(float),
+                                    n_cond, on_device ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice, st));
+    }
     const int nb = (n_cond + 1023) / 1024;
     // scratch: keys u64[n] | counts u64[n] | offsets u64[n] | block sums u64[nb + 1] x 2 | total
     const size_t n = static_cast<size_t>(n_cond);

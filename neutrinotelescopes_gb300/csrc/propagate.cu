@@ -68,11 +68,22 @@ __device__ __forceinline__ float rand_gamma(float shape, float scale, uint4 ctr,
 
 // check_intersection(::Spherical, ...), photon_prop_cuda.jl:233-271: the
 // segment pos + t dir, 0 < t < step, enters the sphere (x, y, z, r^2) at t = d.
+// check_intersection(::Spherical), photon_prop_cuda.jl:233-271: with
+// a = dir . (p - c) the segment enters the sphere at d = -a - sqrt(b),
+// b = r^2 - |(p - c) - a dir|^2 (the squared distance of the line from the
+// centre, subtracted from r^2).  The reference evaluates b as
+// a^2 + r^2 - |p - c|^2: mathematically the same, but in single precision
+// that difference of two numbers of order |p - c|^2 loses the r^2 it is
+// compared with once the centre is a few hundred metres away, and a
+// direction whose norm is 1 - e (rounding of the rotations) shifts it by
+// -2 e a^2, a bias of the hit rate on distant modules.  The perpendicular
+// vector form keeps b accurate to the rounding of r^2 at any distance and
+// is insensitive to the norm to first order.
 __device__ __forceinline__ bool sphere_hit(const float4 T, const V3 pos, const V3 dir, float step, float& d) {
     const float dx = pos.x - T.x, dy = pos.y - T.y, dz = pos.z - T.z;
     const float a = dir.x * dx + dir.y * dy + dir.z * dz;
-    const float pp = dx * dx + dy * dy + dz * dz;
-    const float b = fmaf(a, a, T.w - pp);
+    const float qx = fmaf(-a, dir.x, dx), qy = fmaf(-a, dir.y, dy), qz = fmaf(-a, dir.z, dz);
+    const float b = T.w - (qx * qx + qy * qy + qz * qz);
     if (b >= 0.0f) {
         d = -a - fast_sqrt(b);
         return d > 0.0f && d < step;

@@ -21,6 +21,7 @@ import numpy as np
 from . import _abi
 
 N_FEATURES = 5
+INPUT_MODES = {"features": _abi.FLOW_INPUT_FEATURES, "derived": _abi.FLOW_INPUT_DERIVED}
 
 
 def flow_features(distance, cos_theta_src, cos_theta_pmt, phi, log10_energy) -> np.ndarray:
@@ -54,6 +55,11 @@ class RQNormFlowHParams:
     grad_clip: float = 1e3   # per-sample bound on |dL/draw outputs| x batch size; 0 = none
     count_weight: float = 1.0  # weight of the Poisson count term (1 = log_likelihood_with_poisson)
     seed: int = 31338
+    # conditioner inputs: "features" (the 5 condition features) or "derived"
+    # (the features plus the distance / 100 m, the source direction's offset
+    # from the Cherenkov cosine and its square, sin theta_pmt cos phi; for a
+    # count-only model)
+    input_columns: str = "features"
 
 
 def _f32(a, n=None) -> np.ndarray:
@@ -75,7 +81,8 @@ class RQNormFlow:
                                  t_min=float(hp.range_min), t_max=float(hp.range_max), lr=float(hp.lr),
                                  beta1=float(hp.beta1), beta2=float(hp.beta2), eps=float(hp.eps),
                                  grad_clip=float(hp.grad_clip), count_weight=float(hp.count_weight),
-                                 seed=int(hp.seed) & (2 ** 64 - 1))
+                                 seed=int(hp.seed) & (2 ** 64 - 1),
+                                 input_columns=INPUT_MODES[hp.input_columns])
         h = C.c_void_p()
         st = self.lib.ntp_flow_create(int(device), C.byref(cfg), C.byref(h))
         if st != 0:
@@ -259,6 +266,65 @@ class RQNormFlow:
                 return losses
         return losses
 
+    def fit_counts(self, table, *, steps: int, batch_size: int | None = None, seed: int = 0,
+                   lr_schedule=None) -> list[float]:
+        """Trains the count head alone on a FlowTable's groups (one
+        (module orientation, PMT) of one simulation each): the condition, the
+        MC expectation as the target and the information weight of the
+        group (the hits simulated for it, FlowTable.information_weights), no
+        time rows.  For a count-only model next to a shape model; each epoch
+        reshuffles the groups on the device.  lr_schedule(step) -> lr, or
+        None for the configured rate."""
+        import torch
+        if table.sim_scale is None:
+            raise ValueError("the table needs sim_scale")
+        dev = table.group_cond.device
+        G = int(table.group_cond.shape[0])
+        S = int(table.sim_scale.shape[0])
+        c = (1.0 / torch.as_tensor(table.sim_scale, dtype=torch.float64, device=dev)).repeat_interleave(G // S)
+        c = (c / c.mean()).to(torch.float32)
+        target = table.group_expec.to(torch.float32)
+        bs = int(batch_size or self.hparams.batch_size)
+        bs = max(128, min(bs, self.batch_capacity) // 128 * 128)
+        tres = torch.zeros(G, dtype=torch.float32, device=dev)
+        no_time = torch.zeros(G, dtype=torch.int32, device=dev)
+        gen = torch.Generator(device=dev)
+        gen.manual_seed(int(seed))
+        losses: list[float] = []
+        per_epoch = G // bs
+        chunk = 50
+        while len(losses) < steps:
+            perm = torch.randperm(G, device=dev, generator=gen)
+            cond = table.group_cond[perm].contiguous()
+            nh, cw = target[perm].contiguous(), c[perm].contiguous()
+            torch.cuda.synchronize()
+            done = 0
+            while done < per_epoch and len(losses) < steps:
+                k = min(chunk, per_epoch - done, steps - len(losses))
+                if lr_schedule is not None:
+                    self.set_lr(float(lr_schedule(len(losses))))
+                r = done * bs
+                losses.extend(self.train_steps(cond[r:], tres[r:], nh[r:], no_time[r:], bs, k,
+                                               count_weight=cw[r:]))
+                done += k
+        return losses
+
+    def log_expectation(self, cond):
+        """Per condition the log expected hit count of the count head
+        (float32; a CUDA tensor for a CUDA input, else numpy)."""
+        if _is_device(cond):
+            import torch
+            n = int(cond.shape[0])
+            le = torch.empty(n, dtype=torch.float32, device=cond.device)
+            c = cond.to(torch.float32).contiguous()
+            self._check(self.lib.ntp_flow_evaluate(self._h, c.data_ptr(), n, None, None, 0, None, le.data_ptr(), 1))
+            return le
+        c = _f32(cond)
+        le = np.empty(c.shape[0], np.float32)
+        self._check(self.lib.ntp_flow_evaluate(self._h, c.ctypes.data, c.shape[0], None, None, 0, None,
+                                               le.ctypes.data, 0))
+        return le
+
     def train_steps(self, cond, tres, nhits, has_time, batch: int, steps: int, *, count_weight=None,
                     update: bool = True) -> list[float]:
         """`steps` Adam steps on consecutive batches of `batch` rows of CUDA
@@ -373,17 +439,22 @@ class RQNormFlow:
 
     MAX_SAMPLE_CONDITIONS = 1 << 20
 
-    def sample_hits(self, cond, keys, seed: int = 0, capacity: int | None = None):
+    def sample_hits(self, cond, keys, seed: int = 0, capacity: int | None = None, log_expec=None):
         """Hits the surrogate predicts: per condition a Poisson count of its
         expectation and that many times drawn from its density.  keys:
-        64-bit stream key per condition.  Returns (counts, hit condition
-        index, hit time) -- numpy arrays, or CUDA tensors for CUDA inputs.
-        More than 2^20 conditions are sampled in pieces (the draws are keyed
-        by condition, so the result is the same)."""
+        64-bit stream key per condition; log_expec: per condition the log
+        expectation to draw the counts from (None = this flow's count head;
+        e.g. a separate count model's ``log_expectation``).  Returns
+        (counts, hit condition index, hit time) -- numpy arrays, or CUDA
+        tensors for CUDA inputs.  More than 2^20 conditions are sampled in
+        pieces (the draws are keyed by condition, so the result is the
+        same)."""
         n = int(cond.shape[0])
         step = self.MAX_SAMPLE_CONDITIONS
         if n > step:
-            parts = [self.sample_hits(cond[s:s + step], keys[s:s + step], seed, capacity) for s in range(0, n, step)]
+            parts = [self.sample_hits(cond[s:s + step], keys[s:s + step], seed, capacity,
+                                      None if log_expec is None else log_expec[s:s + step])
+                     for s in range(0, n, step)]
             if _is_device(cond):
                 import torch
                 offs = [s for s in range(0, n, step)]
@@ -404,9 +475,12 @@ class RQNormFlow:
             cnt = torch.empty(n, dtype=torch.int64, device=cond.device)
             hc = torch.empty(max(guess, 1), dtype=torch.int32, device=cond.device)
             ht = torch.empty(max(guess, 1), dtype=torch.float32, device=cond.device)
+            le = None if log_expec is None else log_expec.to(torch.float32).contiguous()
             torch.cuda.synchronize()
-            st = self.lib.ntp_flow_sample(self._h, cond.data_ptr(), n, keys.data_ptr(), int(seed) & (2 ** 64 - 1),
-                                          cnt.data_ptr(), hc.data_ptr(), ht.data_ptr(), guess, C.byref(n_hits), 1)
+            st = self.lib.ntp_flow_sample_expec(self._h, cond.data_ptr(), n, keys.data_ptr(),
+                                                int(seed) & (2 ** 64 - 1), le.data_ptr() if le is not None else None,
+                                                cnt.data_ptr(), hc.data_ptr(), ht.data_ptr(), guess, C.byref(n_hits),
+                                                1)
             if st == _abi.NTP_ERR_OVERFLOW and capacity is None:
                 m = int(n_hits.value)
                 hc = torch.empty(m, dtype=torch.int32, device=cond.device)
@@ -422,8 +496,10 @@ class RQNormFlow:
         cnt = np.empty(n, np.uint64)
         hc = np.empty(max(guess, 1), np.int32)
         ht = np.empty(max(guess, 1), np.float32)
-        st = self.lib.ntp_flow_sample(self._h, cond.ctypes.data, n, keys.ctypes.data, int(seed) & (2 ** 64 - 1),
-                                      cnt.ctypes.data, hc.ctypes.data, ht.ctypes.data, guess, C.byref(n_hits), 0)
+        le = None if log_expec is None else _f32(log_expec, n)
+        st = self.lib.ntp_flow_sample_expec(self._h, cond.ctypes.data, n, keys.ctypes.data, int(seed) & (2 ** 64 - 1),
+                                            le.ctypes.data if le is not None else None, cnt.ctypes.data,
+                                            hc.ctypes.data, ht.ctypes.data, guess, C.byref(n_hits), 0)
         if st == _abi.NTP_ERR_OVERFLOW and capacity is None:
             m = int(n_hits.value)
             hc = np.empty(max(m, 1), np.int32)

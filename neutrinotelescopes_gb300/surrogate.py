@@ -57,11 +57,16 @@ class EventHits:
 class HybridSimulator:
     """Flow surrogate with an MC fallback on the detector of ``setup``."""
 
-    def __init__(self, setup: PhotonPropSetup, flow: RQNormFlow, *, d_range=(1.0, 200.0),
-                 log10_energy_range=(2.0, 6.0), seed: int = 0, ks_check_every: int = 0,
+    def __init__(self, setup: PhotonPropSetup, flow: RQNormFlow, *, count_flow: RQNormFlow | None = None,
+                 d_range=(1.0, 200.0), log10_energy_range=(2.0, 6.0), seed: int = 0, ks_check_every: int = 0,
                  ks_threshold: float = 0.02, ks_min_hits: int = 40_000, ks_max_photons: float = 2e10,
                  ks_confidence: float = 0.95):
-        """ks_check_every > 0: every that many flow-served events one is also
+        """count_flow: a separate count model (an RQNormFlow trained on the
+        counts alone, usually with derived input columns) that supplies every
+        PMT's expected hits; the flow then supplies only the arrival times.
+        None: the flow's own count head.
+
+        ks_check_every > 0: every that many flow-served events one is also
         simulated with plain MC (``ks_check``): the one-sample
         Kolmogorov-Smirnov distance D of the MC hit times from the flow's
         predicted hit-time distribution of the event.  The MC run is
@@ -79,6 +84,7 @@ class HybridSimulator:
         threshold."""
         self.setup = setup
         self.flow = flow
+        self.count_flow = count_flow
         self.d_range = (float(d_range[0]), float(d_range[1]))
         self.e_range = log10_energy_range
         self.seed = int(seed)
@@ -126,6 +132,11 @@ class HybridSimulator:
                 C.byref(n_cond), first.ctypes.data, close.ctypes.data, None))
         return cond[:m], key[:m], tgeo[:m], tgt[:m], pmt[:m], first, close
 
+    def log_expectation(self, cond):
+        """Per condition (device tensor) the log expected hit count: the
+        count model's, or the flow's own count head."""
+        return (self.count_flow or self.flow).log_expectation(cond)
+
     def simulate(self, events) -> list[EventHits]:
         """events: (event_id, source, log10 E) triples, one batch.  Hits stay
         on the device (torch tensors)."""
@@ -137,7 +148,8 @@ class HybridSimulator:
         out: list[EventHits | None] = [None] * len(events)
         in_domain = (close == 0) & (le >= self.e_range[0]) & (le <= self.e_range[1]) & (not self.fallback)
         if cond.shape[0] and in_domain.any():
-            cnt, hc, ht = self.flow.sample_hits(cond, key, seed=self.seed)
+            le_c = self.count_flow.log_expectation(cond) if self.count_flow is not None else None
+            cnt, hc, ht = self.flow.sample_hits(cond, key, seed=self.seed, log_expec=le_c)
             hc64 = hc.long()
             dev = hc.device
             # per hit, once for the batch: target, PMT and time (residual +
@@ -195,8 +207,7 @@ class HybridSimulator:
         cond, _, tgeo, tgt, _, _, _ = self.conditions([source], [log10_energy], [event_id])
         if cond.shape[0] == 0:
             return float("nan"), 0
-        idx = torch.zeros(1, dtype=torch.int32, device=cond.device)
-        _, le = self.flow.logpdf(cond, idx, torch.zeros(1, dtype=torch.float32, device=cond.device), log_expec=True)
+        le = self.log_expectation(cond)
         expected = float(torch.exp(le.double()).sum().item())
         k_max = max(1, int(self.ks_max_photons // max(int(source.photons), 1)))
         k = min(max(1, math.ceil(self.ks_min_hits / max(expected, 1e-9))), k_max)
@@ -214,7 +225,8 @@ class HybridSimulator:
         if t.size == 0:
             return float("nan"), 0
         off = tgeo + float(source.time)
-        F = self.flow.mixture_cdf(cond, torch.as_tensor(t.astype(np.float32), device=cond.device), off)
+        w = torch.exp(le.double()).to(torch.float32) if self.count_flow is not None else None
+        F = self.flow.mixture_cdf(cond, torch.as_tensor(t.astype(np.float32), device=cond.device), off, weights=w)
         return ks_distance(F.cpu().numpy()), int(t.size)
 
     def serve(self, arrivals, *, max_batch: int = 64) -> list[tuple[int, str, float]]:
@@ -277,8 +289,8 @@ def mc_truth(setup: PhotonPropSetup, source, *, seed: int = 0) -> dict:
         t_idx = {int(t.module_id): k for k, t in enumerate(setup.targets)}
         tg = np.array([t_idx[int(m)] for m in r["module_id"]], np.int32)
         rows = hits.records[r["hit_index"].astype(np.int64)] if len(r["hit_index"]) else hits.records[:0]
-        return {"expected": summ["weight_sum"], "target": tg, "pmt": r["pmt_id"], "tres": r["tres"],
-                "time": rows["time"].astype(np.float64) if len(rows) else np.zeros(0)}
+        return {"expected": summ["weight_sum"], "raw_hits": summ["hit_count"], "target": tg, "pmt": r["pmt_id"],
+                "tres": r["tres"], "time": rows["time"].astype(np.float64) if len(rows) else np.zeros(0)}
     finally:
         setup.sources = old
 
@@ -311,9 +323,7 @@ def compare(sim: HybridSimulator, source, log10_energy: float, event_id: int, *,
     cond, key, tgeo, tgt, pmt, first, close = sim.conditions([source], [log10_energy], [event_id])
     if cond.shape[0] == 0:
         return {"modules": 0}
-    idx = torch.zeros(1, dtype=torch.int32, device=cond.device)
-    _, le = sim.flow.logpdf(cond, idx, torch.zeros(1, dtype=torch.float32, device=cond.device), log_expec=True)
-    lam = np.exp(le.double().cpu().numpy())
+    lam = np.exp(sim.log_expectation(cond).double().cpu().numpy())
     tg = tgt.cpu().numpy()
     mod_flow: dict[int, float] = {}
     for k, v in zip(tg, lam):
@@ -337,6 +347,65 @@ def compare(sim: HybridSimulator, source, log10_energy: float, event_id: int, *,
             "flow_hits": int(ft.size), "method": ev.method,
             "ks_predicted": ks_pred, "ks_predicted_mc_hits": n_pred,
             "ks_predicted_bound": sim.ks_noise_bound(n_pred)}
+
+
+def mc_reference(sim: HybridSimulator, source, log10_energy: float, event_id: int, *, seed: int = 0,
+                 max_photons: float = 1e10, min_raw_hits: int = 400_000) -> dict:
+    """Plain-MC reference of one event for judging the surrogate: one MC run
+    of f times the event's photons, f chosen (from the surrogate's expected
+    hits) for about min_raw_hits simulated hits and at most max_photons
+    photons (f < 1 for the brightest events: the expectations are divided by
+    f, so they stay unbiased).  Returns the per-(target, PMT) expectations of
+    the event and raw simulated hits, and the resampled MC hit times of the
+    modules in the surrogate's domain (the sample of the one-sample KS test
+    against the surrogate's predicted hit-time CDF).  Independent of the
+    surrogate's parameters: one reference serves every trained model."""
+    import torch
+    cond, _, tgeo, tgt, _, _, _ = sim.conditions([source], [log10_energy], [event_id])
+    photons = max(int(source.photons), 1)
+    expected = float(torch.exp(sim.log_expectation(cond).double()).sum().item()) if cond.shape[0] else 0.0
+    # raw hits per expected hit: the weights (acceptance x absorption) average about 0.1
+    f = min(max_photons / photons, max(1.0, min_raw_hits / max(10.0 * expected, 1.0)))
+    n_mc = max(1, int(round(photons * f)))
+    truth = mc_truth(sim.setup, dataclasses.replace(source, photons=n_mc), seed=seed)
+    scale = photons / n_mc
+    domain = np.unique(tgt.cpu().numpy()) if cond.shape[0] else np.zeros(0, np.int32)
+    keep = np.isin(truth["target"], domain)
+    return {"event_id": int(event_id), "log10_energy": float(log10_energy), "photons": photons, "mc_photons": n_mc,
+            "expected": truth["expected"] * scale, "raw_hits": truth["raw_hits"],
+            "ks_times": np.sort(truth["time"][keep]), "cond": cond, "tgeo": tgeo, "tgt": tgt,
+            "time_offset": float(source.time)}
+
+
+def evaluate_against(sim: HybridSimulator, ref: dict, *, min_raw_hits: int = 10_000) -> dict:
+    """The surrogate of `sim` against an MC reference (mc_reference):
+    per module the relative error of the expected hits (the PMTs' expected
+    counts summed over the module) where the MC's module estimate rests on
+    at least min_raw_hits simulated hits (relative MC noise about 1 %), and
+    the one-sample KS distance of the MC hit times from the surrogate's
+    predicted hit-time CDF of the event with its 95 % DKW noise bound."""
+    import torch
+    cond = ref["cond"]
+    if cond.shape[0] == 0:
+        return {"modules": 0, "rel_err": np.zeros(0), "ks": float("nan"), "mc_hits": 0}
+    le = sim.log_expectation(cond)
+    lam = np.exp(le.double().cpu().numpy())
+    tg = ref["tgt"].cpu().numpy()
+    flow_mod = np.bincount(tg, weights=lam, minlength=ref["expected"].shape[0])
+    mc_mod = ref["expected"].sum(axis=1)
+    raw_mod = ref["raw_hits"].sum(axis=1)
+    sel = np.flatnonzero((raw_mod >= min_raw_hits) & (mc_mod > 0))
+    rel = flow_mod[sel] / mc_mod[sel] - 1.0
+    t = ref["ks_times"]
+    ks = float("nan")
+    if t.size:
+        w = torch.exp(le.double()).to(torch.float32)
+        F = sim.flow.mixture_cdf(cond, torch.as_tensor(t.astype(np.float32), device=cond.device),
+                                 ref["tgeo"] + ref["time_offset"], weights=w)
+        ks = ks_distance(F.cpu().numpy())
+    return {"modules": int(sel.size), "rel_err": rel, "ks": ks, "mc_hits": int(t.size),
+            "ks_noise_bound": ks_noise_bound(int(t.size), 0.95) if t.size else float("inf"),
+            "event_expected_rel_err": float(flow_mod.sum() / max(mc_mod[np.unique(tg)].sum(), 1e-30) - 1.0)}
 
 
 def hybrid_events(n: int, setup: PhotonPropSetup, *, seed: int = 4, log10_energy=(2.0, 6.0),

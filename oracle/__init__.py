@@ -43,6 +43,8 @@ def lib() -> C.CDLL:
                   C.POINTER(_abi.NtpTarget), i32, u64, C.POINTER(_abi.NtpPropOpts), u64, u64, vp, u64]
         L.ntpo_propagate_f64.argtypes = common
         L.ntpo_propagate_f64.restype = u64
+        L.ntpo_propagate_f64_binned.argtypes = common
+        L.ntpo_propagate_f64_binned.restype = u64
         L.ntpo_propagate_f32.argtypes = common + [i32]
         L.ntpo_propagate_f32.restype = u64
         L.ntpo_propagate_f32_binned.argtypes = common + [i32]
@@ -161,31 +163,34 @@ class World:
         self.total = sum(int(s.photons) for s in setup.sources)
 
 
-def _f64_range(w, seed, b, e, cap):
+def _f64_range(w, seed, b, e, cap, binned=False):
     cap = cap or max(1024, (e - b) // 20)
+    fn = lib().ntpo_propagate_f64_binned if binned else lib().ntpo_propagate_f64
     while True:
         out = np.zeros(cap, dtype=_abi.HIT_DTYPE)
-        n = lib().ntpo_propagate_f64(w.sources, w.n_sources, C.byref(w.medium), C.byref(w.spectrum), w.targets,
-                                     w.n_targets, seed, C.byref(w.opts), b, e, out.ctypes.data, cap)
+        n = fn(w.sources, w.n_sources, C.byref(w.medium), C.byref(w.spectrum), w.targets, w.n_targets, seed,
+               C.byref(w.opts), b, e, out.ctypes.data, cap)
         if n <= cap:
             return out[:n]
         cap = int(n)
 
 
-def propagate_f64(setup, seed=0, gid_begin=0, gid_end=None, cap=None, threads=1) -> np.ndarray:
+def propagate_f64(setup, seed=0, gid_begin=0, gid_end=None, cap=None, threads=1, binned=False) -> np.ndarray:
     """Double-precision oracle run over photons [gid_begin, gid_end); hits
     ordered by photon.  threads > 1 splits the range into pieces run on that
     many host threads (each a ctypes call, which releases the GIL) and joins
-    them in order: the same hits as one call."""
+    them in order: the same hits as one call.  binned=True looks targets up
+    in a bucket grid instead of scanning all of them (same hits)."""
     w = World(setup)
     gid_end = w.total if gid_end is None else min(gid_end, w.total)
     if threads <= 1 or gid_end - gid_begin < 4096:
-        return _f64_range(w, seed, gid_begin, gid_end, cap)
+        return _f64_range(w, seed, gid_begin, gid_end, cap, binned)
     from concurrent.futures import ThreadPoolExecutor
     n_pieces = 4 * threads
     edges = np.linspace(gid_begin, gid_end, n_pieces + 1).astype(np.int64)
     with ThreadPoolExecutor(max_workers=threads) as ex:
-        parts = list(ex.map(lambda i: _f64_range(w, seed, int(edges[i]), int(edges[i + 1]), None), range(n_pieces)))
+        parts = list(ex.map(lambda i: _f64_range(w, seed, int(edges[i]), int(edges[i + 1]), None, binned),
+                            range(n_pieces)))
     return np.concatenate(parts) if parts else np.zeros(0, dtype=_abi.HIT_DTYPE)
 
 

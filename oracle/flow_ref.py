@@ -198,10 +198,26 @@ def unpack(theta: np.ndarray, n_pad: int):
     return out
 
 
+def derived_columns(cond) -> np.ndarray:
+    """The conditioner inputs of the derived-column mode: the 5 features
+    followed by the distance / 100 m, the source direction's cosine minus
+    1/1.35 and its square, and sin(theta_pmt) cos(phi), computed in float32
+    from the float32 features (features: log distance over 1-200 m mapped to
+    [-1, 1], cos theta_src, cos theta_pmt, azimuth over [0, 2 pi) mapped to
+    [-1, 1], log10 E)."""
+    f = np.asarray(cond, np.float32)
+    one = np.float32(1.0)
+    d100 = np.exp((f[:, 0] + one) * np.float32(math.log(200.0) / 2)) * np.float32(0.01)
+    c = f[:, 1] + np.float32(1.0 / 1.35)
+    s = np.sqrt(np.maximum(one - f[:, 2] * f[:, 2], np.float32(0.0))) * np.cos(np.float32(math.pi) * (f[:, 3] + one))
+    return np.concatenate([f, np.stack([d100, c, c * c, s], axis=1)], axis=1).astype(np.float32)
+
+
 def conditioner(layers, cond: torch.Tensor, bf16: bool = False) -> torch.Tensor:
-    """The MLP: cond [n x 5] -> raw outputs [n x n_pad].  With bf16 the
-    input, weights and hidden activations are rounded to bfloat16 as in the
-    tensor-core path (accumulation stays float64)."""
+    """The MLP: cond [n x c] (the c input columns, c <= 64) -> raw outputs
+    [n x n_pad].  With bf16 the input, weights and hidden activations are
+    rounded to bfloat16 as in the tensor-core path (accumulation stays
+    float64)."""
     x = torch.zeros(cond.shape[0], 64, dtype=DT)
     x[:, :cond.shape[1]] = cond
     r = bf16_round if bf16 else (lambda t: t)
@@ -216,10 +232,11 @@ def conditioner(layers, cond: torch.Tensor, bf16: bool = False) -> torch.Tensor:
 
 
 def full_loss(theta: np.ndarray, cond, tres, nhits, has_time, L: int, K: int, r0: float, r1: float,
-              n_pad: int, bf16: bool = False, count_weight=None):
-    """Loss and its gradient by the flat parameters (float64 numpy)."""
+              n_pad: int, bf16: bool = False, count_weight=None, derived: bool = False):
+    """Loss and its gradient by the flat parameters (float64 numpy);
+    derived: the conditioner reads derived_columns(cond)."""
     layers = [(W.clone().requires_grad_(True), b.clone().requires_grad_(True)) for W, b in unpack(theta, n_pad)]
-    c = torch.as_tensor(np.asarray(cond, np.float64))
+    c = torch.as_tensor(np.asarray(derived_columns(cond) if derived else cond, np.float64))
     raw = conditioner(layers, c, bf16=bf16)
     n_out = L * (3 * K + 1) + 3
     loss = head_loss(raw[:, :n_out], torch.as_tensor(np.asarray(tres, np.float64)),

@@ -150,24 +150,45 @@ static int ntpo_source_of(const uint64_t* prefix, int n_src, uint64_t gid) {
    concatenated in order (double precision); writes hits in increasing global
    index.  Returns the number of hits, which may exceed cap (then only the
    first cap are written). */
-uint64_t ntpo_propagate_f64(const ntp_source* src, int n_src, const ntp_medium_desc* m,
-                            const ntp_spectrum_desc* sp, const ntp_target* tg, int n_tg,
-                            uint64_t seed, const ntp_prop_opts* o, uint64_t gid_begin,
-                            uint64_t gid_end, ntp_hit* out, uint64_t cap) {
+static uint64_t ntpo_f64_run(const ntp_source* src, int n_src, const ntp_medium_desc* m,
+                             const ntp_spectrum_desc* sp, const ntp_target* tg, int n_tg, uint64_t seed,
+                             const ntp_prop_opts* o, uint64_t gid_begin, uint64_t gid_end, ntp_hit* out,
+                             uint64_t cap, int binned) {
     uint64_t* prefix = (uint64_t*)malloc(sizeof(uint64_t) * (size_t)(n_src + 1));
     prefix[0] = 0;
     for (int i = 0; i < n_src; ++i) prefix[i + 1] = prefix[i] + src[i].photons;
+    ntpo_bins bins;
+    if (n_tg == 0) binned = 0;
+    if (binned) ntpo_bins_build(&bins, tg, n_tg);
     uint64_t n = 0;
     for (uint64_t gid = gid_begin; gid < gid_end && gid < prefix[n_src]; ++gid) {
         int s = ntpo_source_of(prefix, n_src, gid);
         ntp_hit h;
-        if (propagate_one_f64(&src[s], (uint32_t)s, gid - prefix[s], m, sp, tg, n_tg, seed, o, NULL, &h)) {
+        if (propagate_one_f64(&src[s], (uint32_t)s, gid - prefix[s], m, sp, tg, n_tg, seed, o,
+                              binned ? &bins : NULL, &h)) {
             if (n < cap) out[n] = h;
             ++n;
         }
     }
+    if (binned) ntpo_bins_free(&bins);
     free(prefix);
     return n;
+}
+
+uint64_t ntpo_propagate_f64(const ntp_source* src, int n_src, const ntp_medium_desc* m,
+                            const ntp_spectrum_desc* sp, const ntp_target* tg, int n_tg,
+                            uint64_t seed, const ntp_prop_opts* o, uint64_t gid_begin,
+                            uint64_t gid_end, ntp_hit* out, uint64_t cap) {
+    return ntpo_f64_run(src, n_src, m, sp, tg, n_tg, seed, o, gid_begin, gid_end, out, cap, 0);
+}
+
+/* The same with the bucket-grid candidate lookup (ntpo_bins): the same hits
+   as the scan over every target, for detectors of thousands of modules. */
+uint64_t ntpo_propagate_f64_binned(const ntp_source* src, int n_src, const ntp_medium_desc* m,
+                                   const ntp_spectrum_desc* sp, const ntp_target* tg, int n_tg,
+                                   uint64_t seed, const ntp_prop_opts* o, uint64_t gid_begin,
+                                   uint64_t gid_end, ntp_hit* out, uint64_t cap) {
+    return ntpo_f64_run(src, n_src, m, sp, tg, n_tg, seed, o, gid_begin, gid_end, out, cap, 1);
 }
 
 static uint64_t ntpo_f32_run(const ntp_source* src, int n_src, const ntp_medium_desc* m,

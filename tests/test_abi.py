@@ -47,7 +47,7 @@ def test_record_layouts():
     # ntp_flow_config: 3 int32, 8 floats (t_min .. count_weight), then the u64 seed
     assert _abi.NtpFlowConfig.count_weight.offset == 40
     assert _abi.NtpFlowConfig.seed.offset == 48
-    assert C.sizeof(_abi.NtpFlowConfig) == 56
+    assert C.sizeof(_abi.NtpFlowConfig) == 64
 
 
 def test_missing_library_fails_loudly(tmp_path):

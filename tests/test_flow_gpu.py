@@ -390,3 +390,94 @@ def test_invalid_arguments():
         assert e.value.status == _abi.NTP_ERR_INVALID
         with pytest.raises(ValueError):
             fl.set_params(np.zeros(3, np.float32))
+
+
+def make_derived(L=1, K=10, r0=-20.0, r1=100.0, cap=2048, seed=2):
+    return RQNormFlow(RQNormFlowHParams(K=K, n_layers=L, range_min=r0, range_max=r1, batch_size=cap, seed=seed,
+                                        grad_clip=0.0, input_columns="derived"))
+
+
+def test_derived_columns_forward():
+    """The count model's conditioner reads four derived input columns
+    computed on the device; the oracle computes them in float32 from the
+    same features.  Same bound as the plain forward; a derived column whose
+    float32 value lies at a BF16 rounding boundary may round the other way
+    on one side (rare: at most 0.5 % of the rows may exceed the bound, by at
+    most 5x)."""
+    rng = np.random.default_rng(4)
+    cond = rng.uniform(-1, 1, (1000, 5)).astype(np.float32)
+    with make_derived() as fl:
+        P = fl.forward_params(cond)
+        theta = fl.get_params()
+        n_pad = fl.n_outputs_padded
+        W1 = theta[:256 * 64].reshape(256, 64)
+        assert np.all(W1[:, 9:] == 0.0) and np.all(W1[:, 5:9] != 0.0)
+    x = torch.as_tensor(R.derived_columns(cond).astype(np.float64))
+    ref = R.conditioner(R.unpack(theta, n_pad), x, bf16=True).numpy()[:, :P.shape[1]]
+    bound = 2e-3 * (1 + np.abs(ref))
+    over = np.any(np.abs(P - ref) > bound, axis=1)
+    assert np.mean(over) <= 0.005, np.mean(over)
+    assert np.all(np.abs(P - ref) <= 5 * bound)
+
+
+def test_derived_columns_count_only_gradient():
+    """A count-only batch (no time rows, expectations as targets, per-row
+    information weights) through the derived-column model: the full
+    gradient against the float64 oracle, as test_full_gradient."""
+    rng = np.random.default_rng(26)
+    B = 1024
+    L, K, r0, r1 = 1, 10, -20.0, 100.0
+    cond = rng.uniform(-1, 1, (B, 5)).astype(np.float32)
+    nhits = (rng.gamma(0.5, 20.0, B)).astype(np.float32)
+    tres = np.zeros(B, np.float32)
+    has = np.zeros(B, np.int32)
+    cw = rng.uniform(0.2, 2.0, B).astype(np.float32)
+    with make_derived() as fl:
+        dev = lambda x: torch.as_tensor(x, device="cuda")  # noqa: E731
+        loss = fl.train_steps(dev(cond), dev(tres), dev(nhits), dev(has), B, 1, count_weight=dev(cw),
+                              update=False)[0]
+        g = fl.gradient()
+        theta = fl.get_params()
+        layout = fl.layout()
+        n_pad = fl.n_outputs_padded
+    ref_loss, g_ref = R.full_loss(theta, cond, tres, nhits, has.astype(bool), L, K, r0, r1, n_pad, bf16=True,
+                                  count_weight=cw, derived=True)
+    assert loss == pytest.approx(ref_loss, rel=1e-3)
+    for name, shape, off in layout:
+        size = int(np.prod(shape))
+        a, b = g[off:off + size].astype(np.float64), g_ref[off:off + size]
+        if name == "W1":
+            assert np.all(a.reshape(shape)[:, 9:] == 0.0)
+        nb = np.linalg.norm(b)
+        if nb == 0.0:
+            assert np.all(a == 0.0), name
+            continue
+        assert np.linalg.norm(a - b) <= 3e-2 * nb + 1e-7, (name, np.linalg.norm(a - b) / nb)
+        assert np.dot(a, b) >= 0.999 * np.linalg.norm(a) * nb, name
+
+
+def test_sampling_with_external_expectations():
+    """Counts drawn from given log expectations: the same keys and
+    expectations give the same hits whichever flow supplies the times'
+    knots' own count head, and the counts follow the given expectations."""
+    rng = np.random.default_rng(41)
+    n = 4000
+    cond = torch.as_tensor(rng.uniform(-1, 1, (n, 5)).astype(np.float32), device="cuda")
+    keys = torch.as_tensor(np.arange(n, dtype=np.int64) * 7919 + 11, device="cuda")
+    le = torch.as_tensor(rng.uniform(-1.0, 2.5, n).astype(np.float32), device="cuda")
+    with make(5, 12, -20.0, 1500.0) as fl:
+        own_le = fl.log_expectation(cond)
+        cnt, hc, ht = fl.sample_hits(cond, keys, seed=5, log_expec=le)
+        cnt2, hc2, ht2 = fl.sample_hits(cond, keys, seed=5, log_expec=le)
+        cnt0, _, _ = fl.sample_hits(cond, keys, seed=5)
+        cnt_h, hc_h, ht_h = fl.sample_hits(cond.cpu().numpy(), keys.cpu().numpy(), seed=5,
+                                           log_expec=le.cpu().numpy())
+    assert torch.equal(cnt, cnt2) and torch.equal(hc, hc2) and torch.equal(ht, ht2)
+    np.testing.assert_array_equal(cnt.cpu().numpy().astype(np.uint64), cnt_h)
+    np.testing.assert_array_equal(ht.cpu().numpy(), ht_h)
+    lam = np.exp(le.double().cpu().numpy())
+    c = cnt.double().cpu().numpy()
+    assert abs(c.sum() - lam.sum()) < 4 * np.sqrt(lam.sum())
+    lam0 = np.exp(own_le.double().cpu().numpy())
+    assert abs(cnt0.double().sum().item() - lam0.sum()) < 4 * np.sqrt(lam0.sum())
+    assert not np.allclose(lam0, lam)

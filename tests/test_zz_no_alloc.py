@@ -108,11 +108,11 @@ def test_noalloc_rejects_bad_medium_and_spectrum():
     md, sd, tg, keep = _descriptors(setup)
     nh, ns = C.c_uint64(), C.c_uint64()
     ref_index = keep[0][0]
-    ref_index[3] = 0.9  # n <= 1
+    ref_index[1] = 0.9  # n <= 1
     st = lib.ntp_propagate_noalloc(C.byref(md), C.byref(sd), tg, 1, pack_sources([src]), 1, 0, None, None, 0,
                                    C.byref(nh), C.byref(ns))
     assert st == _abi.NTP_ERR_INVALID and b"n > 1" in lib.ntp_last_error(None)
-    ref_index[3] = ref_index[2]
+    ref_index[1] = ref_index[0]
     bad = np.array([300.0, -1.0, 600.0], dtype=np.float32)
     sd_bad = _abi.NtpSpectrumDesc(kind=_abi.SPEC_TABLE_LINEAR, n_knots=3, icdf_knots=_abi.fptr(bad))
     st = lib.ntp_propagate_noalloc(C.byref(md), C.byref(sd_bad), tg, 1, pack_sources([src]), 1, 0, None, None, 0,
