@@ -568,10 +568,15 @@ ntp_status ntp_flow_sample_resume(ntp_flow* flow, int32_t* hit_cond, float* hit_
  * the arena, and keeps its hits there until ntp_server_release.  Admitted
  * events are packed into one propagation launch per batch (a CUDA graph
  * replayed with new parameters); two batch slots on two streams let a new
- * batch start while the previous one drains.  An event whose hits exceed its
- * reservation is re-run alone with the exact size (same hits).  The server
- * uses the medium, spectrum and targets of its context, which must not change
- * while the server exists. */
+ * batch start while the previous one drains.  With chunk_photons > 0 an
+ * event enters a batch with at most that many of its photons (a chunk: the
+ * photon indices a .. b-1 of its stream, written to the event's own arena
+ * range) and goes back to the end of the queue for its next chunk, so a
+ * batch stays short and events that arrive meanwhile join the next one
+ * instead of waiting behind a large event; an event has at most one chunk in
+ * flight.  An event whose hits exceed its reservation is re-run whole with
+ * the exact size (same hits).  The server uses the medium, spectrum and
+ * targets of its context, which must not change while the server exists. */
 typedef struct ntp_server ntp_server;
 
 typedef struct ntp_server_config {
@@ -584,6 +589,7 @@ typedef struct ntp_server_config {
     double reserve_hits_per_photon; /* initial hit reservation per photon                    */
     uint64_t min_reserve_hits;      /* smallest reservation of an event                      */
     uint64_t max_batch_photons;     /* photons per batch before it is closed                 */
+    uint64_t chunk_photons;         /* an event's photons per batch (0 = the whole event)     */
 } ntp_server_config;
 
 typedef struct ntp_event_result {

@@ -144,6 +144,7 @@ class NtpServerConfig(C.Structure):
         ("reserve_hits_per_photon", C.c_double),
         ("min_reserve_hits", C.c_uint64),
         ("max_batch_photons", C.c_uint64),
+        ("chunk_photons", C.c_uint64),
     ]
 
 

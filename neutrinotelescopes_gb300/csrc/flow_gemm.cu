@@ -28,6 +28,7 @@
 #include <algorithm>
 #include <atomic>
 #include <cstdint>
+#include <cstdlib>
 #include <mutex>
 
 #include "ntp_internal.h"
@@ -45,6 +46,12 @@ constexpr unsigned long long kWaitLimitNs = 2000000000ull;  // by default a wait
 // failure-detection controls (ntp_gemm_set_wait_limit), read at each launch
 std::atomic<unsigned long long> g_wait_limit_ns{kWaitLimitNs};
 std::atomic<int> g_withhold_first{0};
+// programmatic dependent launch of the GEMMs (NTP_GEMM_PDL=0 in the
+// environment turns it off)
+std::atomic<int> g_pdl{[] {
+    const char* e = std::getenv("NTP_GEMM_PDL");
+    return (e && e[0] == '0') ? 0 : 1;
+}()};
 
 __device__ __forceinline__ uint32_t smem_u32(const void* p) {
     return static_cast<uint32_t>(__cvta_generic_to_shared(p));
@@ -185,6 +192,12 @@ __global__ void __launch_bounds__(kThreads, 1)
     asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
     const uint32_t tmem = s->tmem;
     bool ok = true;
+    // Programmatic dependent launch: the set-up above (tensor memory,
+    // barriers) may overlap the previous kernel of the stream; its outputs
+    // are read only after this wait, which returns once that kernel has
+    // completed and its writes are visible (a no-op without the launch
+    // attribute).
+    asm volatile("griddepcontrol.wait;" ::: "memory");
 
     if (threadIdx.x == 0 && kt1 > kt0) {
         constexpr uint32_t kStageBytes = (kBM + BN) * kBK * sizeof(__nv_bfloat16);
@@ -235,6 +248,10 @@ __global__ void __launch_bounds__(kThreads, 1)
         }
     }
     __syncwarp();
+    // the next kernel of the stream may start its own set-up now; it reads
+    // this kernel's outputs only after its griddepcontrol.wait, i.e. after
+    // this grid has completed
+    asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
     // the accumulator is complete when `done` flips (a thread that timed out
     // above still committed, so this wait ends once its MMAs drain)
     const bool have = (kt1 > kt0) && mbar_wait(&s->done, 0, wait_ns);
@@ -409,9 +426,21 @@ cudaError_t launch_bn(const CUtensorMap& ma, const CUtensorMap& mb, int M, int N
     if (e != cudaSuccess) return e;
     const int per = (k_tiles + splits - 1) / splits;
     dim3 grid((M + kBM - 1) / kBM, (N + BN - 1) / BN, (k_tiles + per - 1) / per);
-    gemm_bf16_kernel<BN><<<grid, kThreads, smem, st>>>(ma, mb, M, N, per, k_tiles, ep, vec_ok, error,
-                                                        g_wait_limit_ns.load(), g_withhold_first.load());
-    return cudaGetLastError();
+    // launched with programmatic stream serialisation: the kernel's prologue
+    // overlaps the tail of the previous kernel on the stream (see the
+    // griddepcontrol instructions in the kernel)
+    cudaLaunchConfig_t cfg{};
+    cfg.gridDim = grid;
+    cfg.blockDim = dim3(kThreads);
+    cfg.dynamicSmemBytes = smem;
+    cfg.stream = st;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+    attr[0].val.programmaticStreamSerializationAllowed = g_pdl.load();
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    return cudaLaunchKernelEx(&cfg, gemm_bf16_kernel<BN>, ma, mb, M, N, per, k_tiles, ep, vec_ok, error,
+                              g_wait_limit_ns.load(), g_withhold_first.load());
 }
 
 int sm_count() {

@@ -93,11 +93,19 @@ struct PropParams {
     const uint32_t* src_stream;
 
     // Per-source output (serving): when src_hit_count != nullptr, hits of
-    // source s go to hits[src_hit_base[s] + k] for k < src_hit_cap[s], with
-    // src_hit_count[s] counting every hit of s (exact even past the cap).
+    // source s go to hits[src_hit_base[o] + k] for k < src_hit_cap[o], with
+    // src_hit_count[o] counting every hit (exact even past the cap), where
+    // o = src_out[s] (nullptr: o = s).  Several sources of a launch, or of
+    // successive launches, may share one output slot: the serving loop
+    // splits an event into photon chunks that all write to the event's slot.
     unsigned long long* src_hit_count;
     const unsigned long long* src_hit_base;
     const unsigned long long* src_hit_cap;
+    const uint32_t* src_out;
+    // First photon index of each source entry within its Philox stream
+    // (nullptr: 0): a chunk [a, b) of an event draws exactly the photons a
+    // .. b-1 that the whole event draws.
+    const unsigned long long* src_photon_offset;
 
     ntp_hit* hits;                        // device
     unsigned long long capacity;

@@ -227,9 +227,10 @@ __device__ __forceinline__ void init_photon(Photon& ph, const ntp_source* __rest
                                          const PropParams& p, const SpectrumView& spec,
                                          const float4* medium, unsigned long long gid, int s) {
     const ntp_source* src = sources + s;
-    const unsigned long long pk = gid - __ldg(p.prefix + s);
+    const unsigned long long pk =
+        gid - __ldg(p.prefix + s) + (p.src_photon_offset ? __ldg(p.src_photon_offset + s) : 0ull);
     ph.src = p.src_stream ? __ldg(p.src_stream + s) : static_cast<uint32_t>(s);
-    ph.slot = s;
+    ph.slot = p.src_out ? static_cast<int>(__ldg(p.src_out + s)) : s;
     ph.pk_lo = static_cast<uint32_t>(pk);
     ph.pk_hi = static_cast<uint32_t>(pk >> 32);
     const uint4 base = make_uint4(kDrawInitA, ph.pk_lo, ph.pk_hi, ph.src);

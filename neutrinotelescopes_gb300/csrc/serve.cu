@@ -8,17 +8,22 @@
 // and keeps their hits in the arena until the caller releases them.
 //
 // Each of two batch slots owns a stream, pinned input / output blocks and a
-// CUDA graph captured once: H2D copy of the batch tables, counter reset, the
-// propagation kernel, D2H copy of the per-event hit counts.  A launch rewrites
-// the pinned input block, updates the kernel node's parameters and replays the
-// graph.  With two slots a new batch is queued while the previous one runs, so
-// its blocks take over SMs as the previous launch drains.
+// CUDA graph captured once: H2D copy of the batch tables, a set-up kernel that
+// installs the arena ranges of newly placed events (and zeroes their hit
+// counters), the propagation kernel, a kernel gathering the batch's event
+// hit counts, D2H copy of those counts.  A launch rewrites the pinned input
+// block, updates the propagation node's parameters and replays the graph.
+// With two slots a new batch is queued while the previous one runs, so its
+// blocks take over SMs as the previous launch drains.
 //
 // Photon k of event e draws from Philox counter (draw, k, e): an event's hits
-// are the same whatever batch it runs in.  The kernel writes each event's hits
-// to its own arena range (per-source output mode); a count above the
-// reservation is exact, and the event goes back to the head of the queue with
-// the exact reservation.
+// are the same whatever batch it runs in, and whether it runs whole or in
+// chunks (a chunk [a, b) passes a as its photon offset).  Every placed event
+// owns an output slot (device hit counter, arena base and reservation); its
+// chunks write to it.  An event has at most one chunk in flight, so the
+// count gathered after its last chunk is final; a count above the
+// reservation is exact, and the event goes back to the head of the queue
+// with the exact reservation and runs again from its first photon.
 #include <algorithm>
 #include <chrono>
 #include <cmath>
@@ -86,10 +91,41 @@ struct Event {
     ntp_source src{};
     State state = State::Queued;
     uint64_t reserve = 0, offset = 0, n_hits = 0;
+    uint64_t launched = 0;  // photons handed to batches so far
     bool placed = false;
+    bool in_flight = false;
+    int out = -1;           // output slot (device counter, base, cap) while placed
     int reruns = 0, batch_events = 0;
     double t_submit = 0, t_launch = 0, t_done = 0;
 };
+
+constexpr int kOutSlots = 65536;  // events placed at one time
+
+// Installs the arena ranges of the events placed for this batch: header
+// word 1 = their number, then (slot, base, cap) triples.
+__global__ void serve_setup_kernel(const uint32_t* __restrict__ hdr, const uint32_t* __restrict__ slot,
+                                   const unsigned long long* __restrict__ base,
+                                   const unsigned long long* __restrict__ cap, unsigned long long* __restrict__ count,
+                                   unsigned long long* __restrict__ ev_base, unsigned long long* __restrict__ ev_cap) {
+    const uint32_t n = hdr[1];
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        const uint32_t o = slot[i];
+        if (o >= static_cast<uint32_t>(kOutSlots)) continue;
+        ev_base[o] = base[i];
+        ev_cap[o] = cap[i];
+        count[o] = 0;
+    }
+}
+
+// The hit counts of the batch's entries (header word 0 = their number).
+__global__ void serve_gather_kernel(const uint32_t* __restrict__ hdr, const uint32_t* __restrict__ out_slot,
+                                    const unsigned long long* __restrict__ count, unsigned long long* __restrict__ dst) {
+    const uint32_t n = hdr[0];
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        const uint32_t o = out_slot[i];
+        dst[i] = o < static_cast<uint32_t>(kOutSlots) ? count[o] : 0ull;
+    }
+}
 
 struct Slot {
     cudaStream_t stream = nullptr;
@@ -117,10 +153,14 @@ struct ntp_server {
     size_t smem = 0;
     int n_max = 0;
     // byte offsets inside a slot's input / output blocks
-    size_t off_src = 0, off_prefix = 0, off_stream = 0, off_base = 0, off_cap = 0, in_bytes = 0;
+    size_t off_hdr = 0, off_src = 0, off_prefix = 0, off_stream = 0, off_poff = 0, off_out = 0;
+    size_t off_nslot = 0, off_nbase = 0, off_ncap = 0, in_bytes = 0;
     size_t off_count = 0, off_counters = 0, out_bytes = 0;
     ntp_hit* d_arena = nullptr;
     Arena arena;
+    // output slots: device hit counters, arena bases and reservations
+    unsigned long long* d_ev = nullptr;  // count[kOutSlots] | base[kOutSlots] | cap[kOutSlots]
+    std::vector<int> free_out;
     std::deque<uint32_t> queue;
     std::unordered_map<uint32_t, Event> events;
     Slot slots[2];
@@ -140,31 +180,46 @@ bool fail_cuda(ntp_server* s, cudaError_t e, const char* what) {
     return true;
 }
 
+template <typename T>
+T* at(unsigned char* base, size_t off) {
+    return reinterpret_cast<T*>(base + off);
+}
+
 void fill_slot_params(const ntp_server* s, const Slot& sl, ntp::PropParams& p) {
     p = s->world;
-    p.sources = reinterpret_cast<const ntp_source*>(sl.d_in + s->off_src);
-    p.prefix = reinterpret_cast<const unsigned long long*>(sl.d_in + s->off_prefix);
-    p.src_stream = reinterpret_cast<const uint32_t*>(sl.d_in + s->off_stream);
-    p.src_hit_base = reinterpret_cast<const unsigned long long*>(sl.d_in + s->off_base);
-    p.src_hit_cap = reinterpret_cast<const unsigned long long*>(sl.d_in + s->off_cap);
-    p.src_hit_count = reinterpret_cast<unsigned long long*>(sl.d_out + s->off_count);
-    p.counters = reinterpret_cast<unsigned long long*>(sl.d_out + s->off_counters);
+    p.sources = at<const ntp_source>(sl.d_in, s->off_src);
+    p.prefix = at<const unsigned long long>(sl.d_in, s->off_prefix);
+    p.src_stream = at<const uint32_t>(sl.d_in, s->off_stream);
+    p.src_photon_offset = at<const unsigned long long>(sl.d_in, s->off_poff);
+    p.src_out = at<const uint32_t>(sl.d_in, s->off_out);
+    p.src_hit_count = s->d_ev;
+    p.src_hit_base = s->d_ev + kOutSlots;
+    p.src_hit_cap = s->d_ev + 2 * kOutSlots;
+    p.counters = at<unsigned long long>(sl.d_out, s->off_counters);
     p.hits = s->d_arena;
     p.capacity = s->arena.size();
 }
 
-// Captures the slot's graph: inputs H2D, counters zeroed, propagation, counts D2H.
+// Captures the slot's graph: inputs H2D, counters zeroed, newly placed
+// events installed, propagation, the batch's counts gathered and copied D2H.
 bool capture_slot(ntp_server* s, Slot& sl) {
     ntp::PropParams p;
     fill_slot_params(s, sl, p);
     p.n_src = 1;
     p.total = 0;  // replaced at every launch
     p.chunk = 32;
+    const uint32_t* hdr = at<const uint32_t>(sl.d_in, s->off_hdr);
     if (fail_cuda(s, cudaStreamBeginCapture(sl.stream, cudaStreamCaptureModeThreadLocal), "cudaStreamBeginCapture"))
         return false;
     cudaMemcpyAsync(sl.d_in, sl.h_in, s->in_bytes, cudaMemcpyHostToDevice, sl.stream);
     cudaMemsetAsync(sl.d_out, 0, s->out_bytes, sl.stream);
+    serve_setup_kernel<<<64, 256, 0, sl.stream>>>(hdr, at<const uint32_t>(sl.d_in, s->off_nslot),
+                                                  at<const unsigned long long>(sl.d_in, s->off_nbase),
+                                                  at<const unsigned long long>(sl.d_in, s->off_ncap), s->d_ev,
+                                                  s->d_ev + kOutSlots, s->d_ev + 2 * kOutSlots);
     ntp::launch_propagate(p, s->grid, sl.stream);
+    serve_gather_kernel<<<64, 256, 0, sl.stream>>>(hdr, at<const uint32_t>(sl.d_in, s->off_out), s->d_ev,
+                                                   at<unsigned long long>(sl.d_out, s->off_count));
     cudaMemcpyAsync(sl.h_out, sl.d_out, s->out_bytes, cudaMemcpyDeviceToHost, sl.stream);
     if (fail_cuda(s, cudaStreamEndCapture(sl.stream, &sl.graph), "cudaStreamEndCapture")) return false;
     if (fail_cuda(s, cudaGraphInstantiate(&sl.exec, sl.graph, 0), "cudaGraphInstantiate")) return false;
@@ -172,11 +227,19 @@ bool capture_slot(ntp_server* s, Slot& sl) {
     if (fail_cuda(s, cudaGraphGetNodes(sl.graph, nullptr, &n), "cudaGraphGetNodes")) return false;
     std::vector<cudaGraphNode_t> nodes(n);
     if (fail_cuda(s, cudaGraphGetNodes(sl.graph, nodes.data(), &n), "cudaGraphGetNodes")) return false;
+    // the propagation node: by its function, else by its launch shape (the
+    // set-up and gather kernels run 64 blocks, the propagation one per SM slot)
+    cudaGraphNode_t by_shape = nullptr;
     for (auto nd : nodes) {
         cudaGraphNodeType t;
         cudaGraphNodeGetType(nd, &t);
-        if (t == cudaGraphNodeTypeKernel) sl.kernel_node = nd;
+        if (t != cudaGraphNodeTypeKernel) continue;
+        cudaKernelNodeParams kp{};
+        if (cudaGraphKernelNodeGetParams(nd, &kp) != cudaSuccess) continue;
+        if (kp.func == ntp::propagate_kernel_fn()) sl.kernel_node = nd;
+        if (static_cast<int>(kp.gridDim.x) == s->grid && kp.sharedMemBytes == s->smem) by_shape = nd;
     }
+    if (!sl.kernel_node) sl.kernel_node = by_shape;
     if (!sl.kernel_node) {
         ntp::set_ctx_error(s->ctx, "ntp_server: captured graph has no kernel node");
         return false;
@@ -187,6 +250,10 @@ bool capture_slot(ntp_server* s, Slot& sl) {
 void finish_event(ntp_server* s, Event& e, int status) {
     e.state = State::Done;
     e.t_done = s->now();
+    if (e.out >= 0) {  // no kernel writes to the slot any more
+        s->free_out.push_back(e.out);
+        e.out = -1;
+    }
     ntp_event_result r{};
     r.event_id = e.id;
     r.status = status;
@@ -202,18 +269,27 @@ void finish_event(ntp_server* s, Event& e, int status) {
     ++s->n_completed;
 }
 
-// Reads a finished batch: events either complete or, on a reservation
-// overflow, go back to the head of the queue with the exact size.
+// Reads a finished batch.  An event whose last chunk ran completes or, on a
+// reservation overflow, goes back to the head of the queue with the exact
+// size (to run again from its first photon); an event with photons left goes
+// to the end of the queue for its next chunk.
 void collect(ntp_server* s, Slot& sl) {
-    const unsigned long long* counts = reinterpret_cast<const unsigned long long*>(sl.h_out + s->off_count);
+    const unsigned long long* counts = at<const unsigned long long>(sl.h_out, s->off_count);
     std::vector<uint32_t> rerun;
     for (size_t i = 0; i < sl.events.size(); ++i) {
         Event& e = s->events[sl.events[i]];
+        e.in_flight = false;
+        if (e.launched < e.src.photons) {
+            e.state = State::Queued;
+            s->queue.push_back(e.id);
+            continue;
+        }
         const uint64_t n = counts[i];
         if (n > e.reserve) {
             s->arena.release(e.offset, e.reserve);
             e.placed = false;
             e.reserve = n;
+            e.launched = 0;
             ++e.reruns;
             e.state = State::Queued;
             rerun.push_back(e.id);
@@ -227,46 +303,77 @@ void collect(ntp_server* s, Slot& sl) {
     sl.busy = false;
 }
 
-// Admits queued events into an idle slot and launches its graph.
+// Admits queued events (whole, or their next chunk) into an idle slot and
+// launches its graph.
 bool launch(ntp_server* s, Slot& sl) {
-    auto* src = reinterpret_cast<ntp_source*>(sl.h_in + s->off_src);
-    auto* prefix = reinterpret_cast<unsigned long long*>(sl.h_in + s->off_prefix);
-    auto* stream_ids = reinterpret_cast<uint32_t*>(sl.h_in + s->off_stream);
-    auto* base = reinterpret_cast<unsigned long long*>(sl.h_in + s->off_base);
-    auto* cap = reinterpret_cast<unsigned long long*>(sl.h_in + s->off_cap);
-    int k = 0;
+    auto* hdr = at<uint32_t>(sl.h_in, s->off_hdr);
+    auto* src = at<ntp_source>(sl.h_in, s->off_src);
+    auto* prefix = at<unsigned long long>(sl.h_in, s->off_prefix);
+    auto* stream_ids = at<uint32_t>(sl.h_in, s->off_stream);
+    auto* poff = at<unsigned long long>(sl.h_in, s->off_poff);
+    auto* outs = at<uint32_t>(sl.h_in, s->off_out);
+    auto* nslot = at<uint32_t>(sl.h_in, s->off_nslot);
+    auto* nbase = at<unsigned long long>(sl.h_in, s->off_nbase);
+    auto* ncap = at<unsigned long long>(sl.h_in, s->off_ncap);
+    const uint64_t chunk_max = s->cfg.chunk_photons;
+    int k = 0, n_new = 0;
     unsigned long long total = 0;
     prefix[0] = 0;
+    const double t = s->now();
     while (!s->queue.empty() && k < s->n_max && total < s->cfg.max_batch_photons) {
         Event& e = s->events[s->queue.front()];
+        if (e.src.photons == 0) {  // nothing to simulate
+            s->queue.pop_front();
+            e.launched = 0;
+            finish_event(s, e, NTP_OK);
+            continue;
+        }
         if (!e.placed) {
             if (e.reserve > s->arena.size()) {  // can never fit
                 s->queue.pop_front();
                 finish_event(s, e, NTP_ERR_NOMEM);
                 continue;
             }
+            if (e.out < 0 && s->free_out.empty()) break;  // every output slot in use
             uint64_t off = 0;
             if (!s->arena.alloc(e.reserve, &off)) break;  // wait for releases (FIFO)
+            if (e.out < 0) {
+                e.out = s->free_out.back();
+                s->free_out.pop_back();
+            }
             e.offset = off;
             e.placed = true;
+            nslot[n_new] = static_cast<uint32_t>(e.out);
+            nbase[n_new] = e.offset;
+            ncap[n_new] = e.reserve;
+            ++n_new;
+        }
+        uint64_t take = e.src.photons - e.launched;
+        if (chunk_max > 0) {
+            take = std::min<uint64_t>(take, chunk_max);
+            if (k > 0) take = std::min<uint64_t>(take, s->cfg.max_batch_photons - total);
         }
         s->queue.pop_front();
         src[k] = e.src;
+        src[k].photons = take;
         stream_ids[k] = e.id;
-        base[k] = e.offset;
-        cap[k] = e.reserve;
-        total += e.src.photons;
+        poff[k] = e.launched;
+        outs[k] = static_cast<uint32_t>(e.out);
+        if (e.launched == 0 && e.reruns == 0) e.t_launch = t;
+        e.launched += take;
+        e.in_flight = true;
+        total += take;
         prefix[k + 1] = total;
         sl.events.push_back(e.id);
         ++k;
     }
     if (k == 0) return true;
-    const double t = s->now();
+    hdr[0] = static_cast<uint32_t>(k);
+    hdr[1] = static_cast<uint32_t>(n_new);
     for (uint32_t id : sl.events) {
         Event& e = s->events[id];
         e.state = State::Running;
-        e.t_launch = t;
-        e.batch_events = k;
+        e.batch_events = std::max(e.batch_events, k);
     }
     ntp::PropParams p;
     fill_slot_params(s, sl, p);
@@ -353,12 +460,18 @@ ntp_status ntp_server_create(ntp_ctx* ctx, const ntp_server_config* cfg, ntp_ser
     s->world.refill_min = 8;
     s->n_max = cfg->max_events_per_batch;
     const size_t N = static_cast<size_t>(s->n_max);
-    s->off_src = 0;
+    s->off_hdr = 0;
+    s->off_src = 16;
     s->off_prefix = align8(s->off_src + sizeof(ntp_source) * N);
     s->off_stream = align8(s->off_prefix + sizeof(unsigned long long) * (N + 1));
-    s->off_base = align8(s->off_stream + sizeof(uint32_t) * N);
-    s->off_cap = align8(s->off_base + sizeof(unsigned long long) * N);
-    s->in_bytes = align8(s->off_cap + sizeof(unsigned long long) * N);
+    s->off_poff = align8(s->off_stream + sizeof(uint32_t) * N);
+    s->off_out = align8(s->off_poff + sizeof(unsigned long long) * N);
+    s->off_nslot = align8(s->off_out + sizeof(uint32_t) * N);
+    s->off_nbase = align8(s->off_nslot + sizeof(uint32_t) * N);
+    s->off_ncap = align8(s->off_nbase + sizeof(unsigned long long) * N);
+    s->in_bytes = align8(s->off_ncap + sizeof(unsigned long long) * N);
+    s->free_out.reserve(kOutSlots);
+    for (int i = kOutSlots - 1; i >= 0; --i) s->free_out.push_back(i);
     s->off_count = 0;
     s->off_counters = align8(sizeof(unsigned long long) * N);
     s->out_bytes = s->off_counters + 4 * sizeof(unsigned long long);
@@ -377,6 +490,10 @@ ntp_status ntp_server_create(ntp_ctx* ctx, const ntp_server_config* cfg, ntp_ser
         return NTP_ERR_NOMEM;
     }
     s->arena = Arena(arena_hits);
+    if ((e = cudaMalloc(&s->d_ev, 3 * sizeof(unsigned long long) * kOutSlots)) != cudaSuccess)
+        return bail(e, "cudaMalloc");
+    if ((e = cudaMemset(s->d_ev, 0, 3 * sizeof(unsigned long long) * kOutSlots)) != cudaSuccess)
+        return bail(e, "cudaMemset");
     ntp::PropParams probe;
     fill_slot_params(s, s->slots[0], probe);
     int per_sm = 0;
@@ -412,6 +529,7 @@ void ntp_server_destroy(ntp_server* s) {
     cudaSetDevice(ntp::ctx_device(s->ctx));
     for (Slot& sl : s->slots) destroy_slot(sl);
     if (s->d_arena) cudaFree(s->d_arena);
+    if (s->d_ev) cudaFree(s->d_ev);
     delete s;
 }
 
@@ -494,6 +612,14 @@ ntp_status ntp_server_get_stats(const ntp_server* s, ntp_server_stats* out) {
     ntp_server_stats st{};
     st.queued = s->queue.size();
     for (const Slot& sl : s->slots) st.running += sl.events.size();
+    // events between chunks wait in the queue: count them as running
+    for (uint32_t id : s->queue) {
+        auto it = s->events.find(id);
+        if (it != s->events.end() && it->second.launched > 0) {
+            --st.queued;
+            ++st.running;
+        }
+    }
     st.completed = s->n_completed;
     st.released = s->n_released;
     st.batches = s->n_batches;

@@ -34,11 +34,13 @@ class EventResult:
 
 
 class EventServer:
-    """Serving loop over the medium, spectrum and targets of ``setup``."""
+    """Serving loop over the medium, spectrum and targets of ``setup``.
+    chunk_photons > 0 splits events into chunks of at most that many
+    photons, one chunk per batch (see ntp_server_config)."""
 
     def __init__(self, setup: PhotonPropSetup, *, hbm_budget_bytes: int = 1 << 30, seed: int = 0,
                  max_events_per_batch: int = 1024, reserve_hits_per_photon: float = 2e-3,
-                 min_reserve_hits: int = 1024, max_batch_photons: int = 4_000_000_000):
+                 min_reserve_hits: int = 1024, max_batch_photons: int = 4_000_000_000, chunk_photons: int = 0):
         self.lib, ctx = setup.context()
         self.setup = setup
         cfg = _abi.NtpServerConfig(
@@ -46,7 +48,7 @@ class EventServer:
             max_events_per_batch=int(max_events_per_batch), max_steps=setup.max_steps,
             hit_policy=setup.prop_opts().hit_policy, flags=setup.prop_opts().flags,
             reserve_hits_per_photon=float(reserve_hits_per_photon), min_reserve_hits=int(min_reserve_hits),
-            max_batch_photons=int(max_batch_photons))
+            max_batch_photons=int(max_batch_photons), chunk_photons=int(chunk_photons))
         self._ctx = ctx
         srv = C.c_void_p()
         _check(self.lib, ctx, self.lib.ntp_server_create(ctx, C.byref(cfg), C.byref(srv)))

@@ -379,9 +379,11 @@ def mc_reference(sim: HybridSimulator, source, log10_energy: float, event_id: in
 
 def evaluate_against(sim: HybridSimulator, ref: dict, *, min_raw_hits: int = 10_000) -> dict:
     """The surrogate of `sim` against an MC reference (mc_reference):
-    per module the relative error of the expected hits (the PMTs' expected
-    counts summed over the module) where the MC's module estimate rests on
-    at least min_raw_hits simulated hits (relative MC noise about 1 %), and
+    per module in the surrogate's domain (1-200 m from the vertex) the
+    relative error of the expected hits (the PMTs' expected counts summed
+    over the module) where the MC's module estimate rests on at least
+    min_raw_hits simulated hits (relative MC noise about 1 %), the share of
+    the event's MC light on modules outside the domain, and
     the one-sample KS distance of the MC hit times from the surrogate's
     predicted hit-time CDF of the event with its 95 % DKW noise bound."""
     import torch
@@ -394,7 +396,9 @@ def evaluate_against(sim: HybridSimulator, ref: dict, *, min_raw_hits: int = 10_
     flow_mod = np.bincount(tg, weights=lam, minlength=ref["expected"].shape[0])
     mc_mod = ref["expected"].sum(axis=1)
     raw_mod = ref["raw_hits"].sum(axis=1)
-    sel = np.flatnonzero((raw_mod >= min_raw_hits) & (mc_mod > 0))
+    in_domain = np.zeros(mc_mod.shape[0], bool)
+    in_domain[np.unique(tg)] = True
+    sel = np.flatnonzero(in_domain & (raw_mod >= min_raw_hits) & (mc_mod > 0))
     rel = flow_mod[sel] / mc_mod[sel] - 1.0
     t = ref["ks_times"]
     ks = float("nan")
@@ -405,7 +409,8 @@ def evaluate_against(sim: HybridSimulator, ref: dict, *, min_raw_hits: int = 10_
         ks = ks_distance(F.cpu().numpy())
     return {"modules": int(sel.size), "rel_err": rel, "ks": ks, "mc_hits": int(t.size),
             "ks_noise_bound": ks_noise_bound(int(t.size), 0.95) if t.size else float("inf"),
-            "event_expected_rel_err": float(flow_mod.sum() / max(mc_mod[np.unique(tg)].sum(), 1e-30) - 1.0)}
+            "event_expected_rel_err": float(flow_mod.sum() / max(mc_mod[in_domain].sum(), 1e-30) - 1.0),
+            "mc_light_outside_domain": float(mc_mod[~in_domain].sum() / max(mc_mod.sum(), 1e-30))}
 
 
 def hybrid_events(n: int, setup: PhotonPropSetup, *, seed: int = 4, log10_energy=(2.0, 6.0),

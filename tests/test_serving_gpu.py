@@ -2,6 +2,8 @@
 and in any mix (bit-exact: its photons draw from the Philox stream of its
 event id), admission respects the HBM budget, reservation overflows re-run
 with exact sizes, impossible events are refused."""
+import time
+
 import numpy as np
 import pytest
 
@@ -109,4 +111,50 @@ def test_refuses_impossible_and_duplicate_events():
     res = server.run_all()
     assert len(res) == 1 and res[0].status == _abi.NTP_ERR_NOMEM
     server.close()
+    setup.close()
+
+
+@pytest.mark.parametrize("chunk,reserve", [(0, 5e-3), (60_000, 5e-3), (60_000, 0.0)])
+def test_events_submitted_while_others_run(chunk, reserve):
+    """Continuous batching: events arrive while earlier ones are on the GPU
+    (submitted between polls whenever the server has events running), with
+    large events split into chunks of `chunk` photons (one chunk per batch)
+    and, in the last case, reservations so small that every event with hits
+    overflows and re-runs.  Each event's hits equal those of the event
+    simulated alone, whole and unchunked (bit-exact)."""
+    setup = detector_setup()
+    evs = events(30, seed=5, lo=3e4, hi=1.5e6)
+    srv = EventServer(setup, hbm_budget_bytes=1 << 28, seed=77, max_events_per_batch=8, chunk_photons=chunk,
+                      max_batch_photons=1_000_000, reserve_hits_per_photon=reserve, min_reserve_hits=16)
+    pending = list(evs)
+    got, batch_mix, submitted_while_running = {}, 0, 0
+    for _ in range(2):
+        srv.submit(*pending.pop(0))
+    while len(got) < len(evs):
+        # poll without waiting: it launches what it can and returns, so the
+        # next submission usually finds a batch on the GPU
+        done = srv.poll(0)
+        st = srv.stats()
+        if pending and (st.running > 0 or st.queued == 0):
+            submitted_while_running += st.running > 0
+            srv.submit(*pending.pop(0))
+        if not done:
+            time.sleep(50e-6)
+        for r in done:
+            assert r.status == _abi.NTP_OK
+            got[r.event_id] = (r, sorted_hits(srv.hits(r.event_id)))
+            batch_mix = max(batch_mix, r.batch_events)
+            srv.release(r.event_id)
+    assert submitted_while_running >= 10 and batch_mix > 1
+    if reserve == 0.0:
+        assert sum(r.reruns > 0 for r, _ in got.values()) >= 10
+    assert sum(len(h) for _, h in got.values()) > 500
+    alone = EventServer(setup, hbm_budget_bytes=1 << 28, seed=77, max_events_per_batch=1)
+    for eid, src in evs:
+        r1, h1 = run(alone, [(eid, src)])
+        assert r1[eid].batch_events == 1
+        assert np.array_equal(h1[eid], got[eid][1]), eid
+        alone.release(eid)
+    alone.close()
+    srv.close()
     setup.close()
