@@ -376,14 +376,15 @@ def _cosine(lr_max: float, lr_min: float, steps: int):
     return lambda k: lr_min + 0.5 * (lr_max - lr_min) * (1 + math.cos(math.pi * min(k, steps) / steps))
 
 
-def train_hybrid_models(tab, seed: int, shape_steps: int, count_steps: int):
-    """The hybrid simulator's two models, trained on one MC table: the
+def train_hybrid_models(tab, seed: int, shape_steps: int, count_steps: int, count_members: int = 3):
+    """The hybrid simulator's models, trained on one MC table: the
     arrival-time flow (5 spline layers of 12 bins, joint count head with the
-    information-weighted count term, the 5 features) and the count model (the
-    same conditioner with derived input columns, trained on the table's
-    (simulation, orientation, PMT) groups alone, information-weighted).
-    Cosine learning-rate schedules from 1e-3 to 1e-5."""
-    from neutrinotelescopes_gb300.flow import RQNormFlow, RQNormFlowHParams
+    information-weighted count term, the 5 features) and the count model, an
+    ensemble of count_members conditioners with derived input columns, each
+    trained on the table's (simulation, orientation, PMT) groups alone,
+    information-weighted, from its own initialisation and shuffle.  Cosine
+    learning-rate schedules from 1e-3 to 1e-5."""
+    from neutrinotelescopes_gb300.flow import CountEnsemble, RQNormFlow, RQNormFlowHParams
     t0 = time.perf_counter()
     fl = RQNormFlow(RQNormFlowHParams(batch_size=8192, seed=31338 + 101 * seed), batch_capacity=65536)
     fl.init_from_table(tab)
@@ -397,13 +398,18 @@ def train_hybrid_models(tab, seed: int, shape_steps: int, count_steps: int):
         ep += 1
     t_shape = time.perf_counter() - t0
     t0 = time.perf_counter()
-    cf = RQNormFlow(RQNormFlowHParams(K=10, n_layers=1, range_min=-20.0, range_max=100.0, batch_size=8192,
-                                      seed=777 + 101 * seed, input_columns="derived"), batch_capacity=8192)
     import torch
-    cf.init_output_bias(log_expec=float(torch.log1p(tab.group_expec.double()).mean().item()))
-    cf.fit_counts(tab, steps=count_steps, seed=seed, lr_schedule=_cosine(1e-3, 1e-5, count_steps))
-    return fl, cf, {"seed": seed, "shape_steps": shape_steps, "shape_seconds": t_shape, "count_steps": count_steps,
-                    "count_seconds": time.perf_counter() - t0}
+    members = []
+    for j in range(count_members):
+        cf = RQNormFlow(RQNormFlowHParams(K=10, n_layers=1, range_min=-20.0, range_max=100.0, batch_size=8192,
+                                          seed=777 + 101 * seed + 13 * j, input_columns="derived"),
+                        batch_capacity=8192)
+        cf.init_output_bias(log_expec=float(torch.log1p(tab.group_expec.double()).mean().item()))
+        cf.fit_counts(tab, steps=count_steps, seed=100 * seed + j, lr_schedule=_cosine(1e-3, 1e-5, count_steps))
+        members.append(cf)
+    return fl, CountEnsemble(members), {"seed": seed, "shape_steps": shape_steps, "shape_seconds": t_shape,
+                                        "count_members": count_members, "count_steps_per_member": count_steps,
+                                        "count_seconds": time.perf_counter() - t0}
 
 
 def hybrid_bench(n_events: int = 10_000, batch: int = 256, shape_steps: int = 48_000, count_steps: int = 24_000,

@@ -57,12 +57,13 @@ class EventHits:
 class HybridSimulator:
     """Flow surrogate with an MC fallback on the detector of ``setup``."""
 
-    def __init__(self, setup: PhotonPropSetup, flow: RQNormFlow, *, count_flow: RQNormFlow | None = None,
+    def __init__(self, setup: PhotonPropSetup, flow: RQNormFlow, *, count_flow=None,
                  d_range=(1.0, 200.0), log10_energy_range=(2.0, 6.0), seed: int = 0, ks_check_every: int = 0,
                  ks_threshold: float = 0.02, ks_min_hits: int = 40_000, ks_max_photons: float = 2e10,
                  ks_confidence: float = 0.95):
         """count_flow: a separate count model (an RQNormFlow trained on the
-        counts alone, usually with derived input columns) that supplies every
+        counts alone, usually with derived input columns, or a CountEnsemble
+        of them; anything with log_expectation(cond)) that supplies every
         PMT's expected hits; the flow then supplies only the arrival times.
         None: the flow's own count head.
 
