@@ -571,10 +571,10 @@ ntp_status ntp_flow_sample_resume(ntp_flow* flow, int32_t* hit_cond, float* hit_
  * batch start while the previous one drains.  With chunk_photons > 0 an
  * event enters a batch with at most that many of its photons (a chunk: the
  * photon indices a .. b-1 of its stream, written to the event's own arena
- * range) and goes back to the end of the queue for its next chunk, so a
- * batch stays short and events that arrive meanwhile join the next one
- * instead of waiting behind a large event; an event has at most one chunk in
- * flight.  An event whose hits exceed its reservation is re-run whole with
+ * range) and goes back to the head of the queue for its next chunk (events
+ * keep their arrival order), so a batch stays short and events that arrive
+ * meanwhile join the next one instead of waiting behind a large event; an
+ * event has at most one chunk in flight.  An event whose hits exceed its reservation is re-run whole with
  * the exact size (same hits).  The server uses the medium, spectrum and
  * targets of its context, which must not change while the server exists. */
 typedef struct ntp_server ntp_server;

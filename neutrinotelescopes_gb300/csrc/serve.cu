@@ -272,16 +272,19 @@ void finish_event(ntp_server* s, Event& e, int status) {
 // Reads a finished batch.  An event whose last chunk ran completes or, on a
 // reservation overflow, goes back to the head of the queue with the exact
 // size (to run again from its first photon); an event with photons left goes
-// to the end of the queue for its next chunk.
+// back to the head of the queue too, behind those, for its next chunk: events
+// keep their arrival order (the tail latency of a large event is its own
+// chunks, not the queue behind it), and every batch still has room for the
+// events that arrived meanwhile (a chunk is at most half a batch).
 void collect(ntp_server* s, Slot& sl) {
     const unsigned long long* counts = at<const unsigned long long>(sl.h_out, s->off_count);
-    std::vector<uint32_t> rerun;
+    std::vector<uint32_t> rerun, cont;
     for (size_t i = 0; i < sl.events.size(); ++i) {
         Event& e = s->events[sl.events[i]];
         e.in_flight = false;
         if (e.launched < e.src.photons) {
             e.state = State::Queued;
-            s->queue.push_back(e.id);
+            cont.push_back(e.id);
             continue;
         }
         const uint64_t n = counts[i];
@@ -298,6 +301,7 @@ void collect(ntp_server* s, Slot& sl) {
             finish_event(s, e, NTP_OK);
         }
     }
+    for (auto it = cont.rbegin(); it != cont.rend(); ++it) s->queue.push_front(*it);
     for (auto it = rerun.rbegin(); it != rerun.rend(); ++it) s->queue.push_front(*it);
     sl.events.clear();
     sl.busy = false;
