@@ -542,6 +542,8 @@ def hybrid_bench(n_events: int = 10_000, batch: int = 256, shape_steps: int = 48
         errs = np.abs(np.concatenate([v["rel_err"] for v in ev]))
         ks = np.array([v["ks"] for v in ev if v["mc_hits"] > 0])
         eps = np.array([v["ks_noise_bound"] for v in ev if v["mc_hits"] > 0])
+        share = np.array([v["top_module_share"] for v in ev if v["mc_hits"] > 0])
+        spread = share <= 0.5
         dec = []
         for k in range(4):
             idx = [i for i, r in enumerate(refs) if edges[k] <= r["log10_energy"] < edges[k + 1]]
@@ -554,17 +556,25 @@ def hybrid_bench(n_events: int = 10_000, batch: int = 256, shape_steps: int = 48
                          "event_total_rel_err_max": float(np.max(np.abs([v["event_expected_rel_err"] for v in ev]))),
                          "mc_light_outside_domain_max": float(np.max([v["mc_light_outside_domain"] for v in ev])),
                          "ks_median": float(np.median(ks)), "ks_max": float(np.max(ks)),
-                         "ks_minus_noise_max": float(np.max(ks - eps)), "decades": dec})
+                         "ks_minus_noise_max": float(np.max(ks - eps)),
+                         "ks_max_spread_events": float(np.max(ks[spread])) if spread.any() else None,
+                         "ks_max_single_module_events": float(np.max(ks[~spread])) if (~spread).any() else None,
+                         "single_module_events": int((~spread).sum()), "decades": dec})
     agg = lambda key: {"mean": float(np.mean([p[key] for p in per_seed])),  # noqa: E731
                        "sd": float(np.std([p[key] for p in per_seed], ddof=1)) if len(per_seed) > 1 else 0.0}
     out["error_vs_mc"] = {
         "events": len(refs), "per_decade": eval_per_decade, "seeds": len(per_seed),
         "rel_err_median": agg("rel_err_median"), "rel_err_p90": agg("rel_err_p90"),
         "ks_median": agg("ks_median"), "ks_max": agg("ks_max"), "ks_minus_noise_max": agg("ks_minus_noise_max"),
+        "ks_max_spread_events": agg("ks_max_spread_events") if all(p["ks_max_spread_events"] is not None
+                                                                    for p in per_seed) else None,
+        "single_module_events": per_seed[0]["single_module_events"],
         "per_seed": per_seed, "seconds": time.perf_counter() - t1,
         "note": "per-module expected hits (count model) against MC where the MC module estimate rests on >= 1e4 "
                 "simulated hits (MC noise ~1 %); ks: one-sample KS of the event's MC hit times against the "
-                "predicted hit-time CDF (raw distance; ks_minus_noise subtracts the MC sample's 95 % DKW bound)"}
+                "predicted hit-time CDF (raw distance; ks_minus_noise subtracts the MC sample's 95 % DKW bound); "
+                "single-module events: one module holds more than half of the event's MC light, so the event's "
+                "KS is that module's"}
     # the hybrid mode's KS check: every 25th flow event also through
     # oversampled MC; plain MC from the first check whose distance, less the
     # MC sample's own 95 % noise bound, is above 0.02
@@ -620,6 +630,9 @@ def legs_summary(out: dict) -> dict:
                        "count_err_p90": [err["rel_err_p90"]["mean"], err["rel_err_p90"]["sd"]],
                        "ks_median": [err["ks_median"]["mean"], err["ks_median"]["sd"]],
                        "ks_max": [err["ks_max"]["mean"], err["ks_max"]["sd"]],
+                       "ks_max_spread_events": ([err["ks_max_spread_events"]["mean"],
+                                                 err["ks_max_spread_events"]["sd"]]
+                                                if err.get("ks_max_spread_events") else None),
                        "seeds": err["seeds"], "events_judged": err["events"],
                        "ks_checks_raw_le_0.02": [hy["ks_check"]["raw_at_most_threshold"], hy["ks_check"]["checks"]]}
     return s

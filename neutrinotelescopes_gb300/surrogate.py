@@ -384,7 +384,8 @@ def evaluate_against(sim: HybridSimulator, ref: dict, *, min_raw_hits: int = 10_
     relative error of the expected hits (the PMTs' expected counts summed
     over the module) where the MC's module estimate rests on at least
     min_raw_hits simulated hits (relative MC noise about 1 %), the share of
-    the event's MC light on modules outside the domain, and
+    the event's MC light on modules outside the domain, the share of its
+    in-domain MC light on its brightest module, and
     the one-sample KS distance of the MC hit times from the surrogate's
     predicted hit-time CDF of the event with its 95 % DKW noise bound."""
     import torch
@@ -411,7 +412,8 @@ def evaluate_against(sim: HybridSimulator, ref: dict, *, min_raw_hits: int = 10_
     return {"modules": int(sel.size), "rel_err": rel, "ks": ks, "mc_hits": int(t.size),
             "ks_noise_bound": ks_noise_bound(int(t.size), 0.95) if t.size else float("inf"),
             "event_expected_rel_err": float(flow_mod.sum() / max(mc_mod[in_domain].sum(), 1e-30) - 1.0),
-            "mc_light_outside_domain": float(mc_mod[~in_domain].sum() / max(mc_mod.sum(), 1e-30))}
+            "mc_light_outside_domain": float(mc_mod[~in_domain].sum() / max(mc_mod.sum(), 1e-30)),
+            "top_module_share": float(mc_mod[in_domain].max() / max(mc_mod[in_domain].sum(), 1e-30))}
 
 
 def hybrid_events(n: int, setup: PhotonPropSetup, *, seed: int = 4, log10_energy=(2.0, 6.0),
