@@ -53,6 +53,16 @@ OPS_PER_GEOMETRY_TEST = 12
 OPS_PHOTON_INIT = 140 + 70 + 15 + 20 + 10 + 15 + 40 + 10
 
 
+# DRAM traffic of one full-size launch of this workload, from an ncu capture
+# (dram__bytes_read.sum + dram__bytes_write.sum, one pass, the timed step of
+# `bench.py --legs propagation --steps 1 --warmup 1`): 1.20 MB read (the
+# medium, spectrum and target tables) and 341.95 MB written for 6092214 hits
+# (the 64-byte hit records that leave the L2).  A step's traffic is scaled
+# by its hits.
+TRAFFIC_READ_BYTES = 1_195_264
+TRAFFIC_WRITE_BYTES_PER_HIT = 341_950_720 / 6_092_214
+
+
 def algo_ops_per_step(n_strings: int) -> int:
     return OPS_BASE + OPS_PER_GEOMETRY_TEST * n_strings
 
@@ -386,7 +396,9 @@ def train_hybrid_models(tab, seed: int, shape_steps: int, count_steps: int, coun
     learning-rate schedules from 1e-3 to 1e-5."""
     from neutrinotelescopes_gb300.flow import CountEnsemble, RQNormFlow, RQNormFlowHParams
     t0 = time.perf_counter()
-    fl = RQNormFlow(RQNormFlowHParams(batch_size=8192, seed=31338 + 101 * seed), batch_capacity=65536)
+    # the batch capacity also sets the chunk of conditions an inference pass
+    # takes at once: the hybrid evaluates millions of PMT conditions per batch
+    fl = RQNormFlow(RQNormFlowHParams(batch_size=8192, seed=31338 + 101 * seed), batch_capacity=131072)
     fl.init_from_table(tab)
     per = len(tab) // 8192
     sched = _cosine(1e-3, 1e-5, shape_steps)
@@ -403,7 +415,7 @@ def train_hybrid_models(tab, seed: int, shape_steps: int, count_steps: int, coun
     for j in range(count_members):
         cf = RQNormFlow(RQNormFlowHParams(K=10, n_layers=1, range_min=-20.0, range_max=100.0, batch_size=8192,
                                           seed=777 + 101 * seed + 13 * j, input_columns="derived"),
-                        batch_capacity=8192)
+                        batch_capacity=131072)
         cf.init_output_bias(log_expec=float(torch.log1p(tab.group_expec.double()).mean().item()))
         cf.fit_counts(tab, steps=count_steps, seed=100 * seed + j, lr_schedule=_cosine(1e-3, 1e-5, count_steps))
         members.append(cf)
@@ -841,7 +853,9 @@ def main():
                 "peak_source": f"nominal issue rate 152 SM x 4 schedulers x 32 lanes at the sampled {sm_mhz:.0f} MHz",
                 "ops_per_photon_step": ops_step, "ops_per_photon_init": OPS_PHOTON_INIT,
                 "photon_steps_per_step": int(statistics.mean(steps_taken)),
-                "traffic": None}
+                "traffic": None if args.small else
+                TRAFFIC_READ_BYTES + TRAFFIC_WRITE_BYTES_PER_HIT * statistics.mean(hit_counts),
+                "traffic_unit": "bytes per launch (ncu capture of this workload, scaled by the launch's hits)"}
 
     # e2e through the public call with host buffers
     e2e_t, e2e_hits = [], []
