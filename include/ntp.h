@@ -505,6 +505,12 @@ ntp_status ntp_flow_head(ntp_flow* flow, const float* params, const float* tres,
 ntp_status ntp_flow_evaluate(ntp_flow* flow, const float* cond, int32_t n_cond, const int32_t* cond_index,
                              const float* times, uint64_t n_tuples, float* logpdf, float* log_expec,
                              int32_t on_device);
+/* Only the log expectation of each condition (the count head, clamped as in
+   ntp_flow_evaluate), without building spline knots: the count model's query
+   in the hybrid simulator.  Leaves a pending ntp_flow_sample resumable.
+   Host, or device buffers with on_device. */
+ntp_status ntp_flow_log_expectation(ntp_flow* flow, const float* cond, int32_t n_cond, float* log_expec,
+                                    int32_t on_device);
 /* The model call on a time grid shared by the conditions, as the reference
    evaluates a module's density (`model(repeat(times), repeat(input))` on a
    111-point grid, extended_cascade_model.jl:416-437 and the scripts):

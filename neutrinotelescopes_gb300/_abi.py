@@ -279,6 +279,7 @@ EXPORTED = (
     "ntp_flow_evaluate",
     "ntp_flow_sample",
     "ntp_flow_sample_expec",
+    "ntp_flow_log_expectation",
     "ntp_flow_evaluate_grid",
     "ntp_server_create",
     "ntp_server_destroy",
@@ -352,11 +353,12 @@ def _declare(lib: C.CDLL) -> None:
     lib.ntp_flow_sample.argtypes = [vp, vp, i32, vp, u64, vp, vp, vp, u64, C.POINTER(u64), i32]
     lib.ntp_flow_sample_expec.argtypes = [vp, vp, i32, vp, u64, vp, vp, vp, vp, u64, C.POINTER(u64), i32]
     lib.ntp_flow_sample_resume.argtypes = [vp, vp, vp, u64, C.POINTER(u64), i32]
+    lib.ntp_flow_log_expectation.argtypes = [vp, vp, i32, vp, i32]
     lib.ntp_flow_evaluate_grid.argtypes = [vp, vp, i32, vp, i32, vp, vp, i32]
     for name in ("ntp_flow_create", "ntp_flow_get_layout", "ntp_flow_set_params", "ntp_flow_get_params",
                  "ntp_flow_train_step", "ntp_flow_forward", "ntp_flow_head", "ntp_flow_evaluate",
                  "ntp_flow_sample", "ntp_flow_evaluate_grid", "ntp_flow_train_steps", "ntp_flow_mixture_cdf",
-                 "ntp_flow_sample_resume", "ntp_flow_sample_expec"):
+                 "ntp_flow_sample_resume", "ntp_flow_sample_expec", "ntp_flow_log_expectation"):
         getattr(lib, name).restype = C.c_int
     lib.ntp_server_create.argtypes = [vp, C.POINTER(NtpServerConfig), C.POINTER(vp)]
     lib.ntp_server_destroy.argtypes = [vp]

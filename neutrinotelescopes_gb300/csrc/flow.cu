@@ -700,6 +700,13 @@ __global__ void knots_kernel(const float* __restrict__ P, int ldp, int L, int n,
     o[L * (3 * (K + 1)) + 2] = clamp_le(p[L * (3 * K + 1) + 2]);
 }
 
+// The log expectation column of the conditioner's raw outputs, with the
+// knot tables' clamp (the count-only query: no spline knots are built).
+__global__ void log_expec_kernel(const float* __restrict__ P, int ldp, int col, int n, float* __restrict__ out) {
+    const int r = blockIdx.x * blockDim.x + threadIdx.x;
+    if (r < n) out[r] = clamp_le(P[static_cast<size_t>(r) * ldp + col]);
+}
+
 // log p(t | condition) for (condition index, time) tuples
 template <int K>
 __global__ void logpdf_kernel(const float* __restrict__ knots, int L, int n_cond, const int* __restrict__ cidx,
@@ -1706,6 +1713,43 @@ ntp_status ntp_flow_sample_resume(ntp_flow* f, int32_t* hit_cond, float* hit_tim
     const int n = f->samp_n;
     f->samp_n = 0;
     return sample_draw(f, n, f->samp_key, f->samp_total, hit_cond, hit_time, on_device);
+}
+
+ntp_status ntp_flow_log_expectation(ntp_flow* f, const float* cond, int32_t n_cond, float* log_expec,
+                                    int32_t on_device) {
+    if (!f || !cond || !log_expec || n_cond <= 0) return NTP_ERR_INVALID;
+    F_CUDA(f, cudaSetDevice(f->device));
+    cudaStream_t st = f->stream;
+    F_CUDA(f, cudaMemsetAsync(f->gemm_err, 0, sizeof(int), st));
+    float* dout = log_expec;
+    void* stage = nullptr;
+    if (!on_device) {
+        F_CUDA(f, cudaMalloc(&stage, sizeof(float) * static_cast<size_t>(n_cond)));
+        dout = static_cast<float*>(stage);
+    }
+    const int col = f->L * (3 * f->K + 1) + 2;
+    ntp_status status = NTP_OK;
+    for (int c0 = 0; c0 < n_cond && status == NTP_OK; c0 += f->cap) {
+        const int m = std::min(f->cap, n_cond - c0);
+        const int mp = (m + 127) / 128 * 128;
+        status = pack(f, cond + static_cast<size_t>(c0) * kCond, m, mp, on_device);
+        if (status == NTP_OK) status = forward(f, mp, false);
+        if (status == NTP_OK) {
+            ntp::log_expec_kernel<<<ntp::blocks_for(m), 256, 0, st>>>(f->P, f->n_pad, col, m, dout + c0);
+            const cudaError_t e = cudaGetLastError();
+            if (e != cudaSuccess) status = ferr(f, e, "ntp_flow_log_expectation");
+        }
+    }
+    if (status == NTP_OK && stage) {
+        const cudaError_t e = cudaMemcpyAsync(log_expec, stage, sizeof(float) * n_cond, cudaMemcpyDeviceToHost, st);
+        if (e != cudaSuccess) status = ferr(f, e, "ntp_flow_log_expectation");
+    }
+    if (stage) {
+        cudaStreamSynchronize(st);
+        cudaFree(stage);
+    }
+    if (status != NTP_OK) return status;
+    return check_gemm(f);
 }
 
 ntp_status ntp_flow_evaluate_grid(ntp_flow* f, const float* cond, int32_t n_cond, const float* times, int32_t n_times,

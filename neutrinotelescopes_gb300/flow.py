@@ -317,12 +317,11 @@ class RQNormFlow:
             n = int(cond.shape[0])
             le = torch.empty(n, dtype=torch.float32, device=cond.device)
             c = cond.to(torch.float32).contiguous()
-            self._check(self.lib.ntp_flow_evaluate(self._h, c.data_ptr(), n, None, None, 0, None, le.data_ptr(), 1))
+            self._check(self.lib.ntp_flow_log_expectation(self._h, c.data_ptr(), n, le.data_ptr(), 1))
             return le
         c = _f32(cond)
         le = np.empty(c.shape[0], np.float32)
-        self._check(self.lib.ntp_flow_evaluate(self._h, c.ctypes.data, c.shape[0], None, None, 0, None,
-                                               le.ctypes.data, 0))
+        self._check(self.lib.ntp_flow_log_expectation(self._h, c.ctypes.data, c.shape[0], le.ctypes.data, 0))
         return le
 
     def train_steps(self, cond, tres, nhits, has_time, batch: int, steps: int, *, count_weight=None,

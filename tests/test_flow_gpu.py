@@ -481,3 +481,19 @@ def test_sampling_with_external_expectations():
     lam0 = np.exp(own_le.double().cpu().numpy())
     assert abs(cnt0.double().sum().item() - lam0.sum()) < 4 * np.sqrt(lam0.sum())
     assert not np.allclose(lam0, lam)
+
+
+def test_log_expectation_query_matches_evaluate():
+    """The knot-free count query gives the log expectations of the full
+    model call, bit for bit, across chunks of the batch capacity, with host
+    and device buffers."""
+    rng = np.random.default_rng(42)
+    n = 5000  # more than the capacity below: three chunks
+    cond = rng.uniform(-1, 1, (n, 5)).astype(np.float32)
+    with RQNormFlow(RQNormFlowHParams(K=12, n_layers=5, batch_size=2048, seed=3), batch_capacity=2048) as fl:
+        le_h = fl.log_expectation(cond)
+        le_d = fl.log_expectation(torch.as_tensor(cond, device="cuda")).cpu().numpy()
+        ref = np.empty(n, np.float32)
+        fl._check(fl.lib.ntp_flow_evaluate(fl._h, cond.ctypes.data, n, None, None, 0, None, ref.ctypes.data, 0))
+    np.testing.assert_array_equal(le_h, ref)
+    np.testing.assert_array_equal(le_d, ref)
