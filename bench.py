@@ -402,12 +402,33 @@ def train_hybrid_models(tab, seed: int, shape_steps: int, count_steps: int, coun
     fl.init_from_table(tab)
     per = len(tab) // 8192
     sched = _cosine(1e-3, 1e-5, shape_steps)
+    # the time density's NLL on a fixed sample of timed rows after every
+    # epoch; the parameters of the best epoch are kept, so that a run that
+    # degrades late does not end in its degraded state (two of about
+    # fourteen runs of this configuration ended with event KS medians of
+    # 0.04-0.5 against the usual 0.012; the training is not bit-reproducible:
+    # the weight gradients are summed with floating-point atomics)
+    import numpy as np
+    import torch
+    gen = torch.Generator(device=tab.tres.device)
+    gen.manual_seed(97 + seed)
+    timed = torch.nonzero(tab.has_time, as_tuple=True)[0]
+    vi = timed[torch.randperm(timed.numel(), device=timed.device, generator=gen)[:32768]]
+    vc, vt, vh = tab.cond[vi].contiguous(), tab.tres[vi].contiguous(), tab.has_time[vi].contiguous()
+    vn, vw = torch.zeros_like(vt), torch.zeros_like(vt)  # count term off: the time NLL alone
+    best_nll, best_theta, nll_per_epoch = math.inf, None, []
     done, ep = 0, 0
     while done < shape_steps:
         fl.set_lr(sched(done))
         done += len(fl.fit_table(tab, epochs=1, seed=1000 * seed + ep, max_steps=min(per, shape_steps - done),
                                  count_mode="information"))
         ep += 1
+        nll = float(np.mean(fl.train_steps(vc, vt, vn, vh, 8192, 4, count_weight=vw, update=False)))
+        nll_per_epoch.append(nll)
+        if nll < best_nll:
+            best_nll, best_theta = nll, fl.get_params()
+    if best_theta is not None and best_nll < nll_per_epoch[-1]:
+        fl.set_params(best_theta)
     t_shape = time.perf_counter() - t0
     t0 = time.perf_counter()
     import torch
@@ -420,6 +441,9 @@ def train_hybrid_models(tab, seed: int, shape_steps: int, count_steps: int, coun
         cf.fit_counts(tab, steps=count_steps, seed=100 * seed + j, lr_schedule=_cosine(1e-3, 1e-5, count_steps))
         members.append(cf)
     return fl, CountEnsemble(members), {"seed": seed, "shape_steps": shape_steps, "shape_seconds": t_shape,
+                                        "time_nll_last": nll_per_epoch[-1], "time_nll_best": best_nll,
+                                        "best_epoch": int(np.argmin(nll_per_epoch)) + 1, "epochs": ep,
+                                        "time_nll_per_epoch": [round(x, 5) for x in nll_per_epoch],
                                         "count_members": count_members, "count_steps_per_member": count_steps,
                                         "count_seconds": time.perf_counter() - t0}
 
@@ -896,8 +920,9 @@ def main():
         if args.details:
             Path(args.details).write_text(json.dumps(out, indent=1))
         hy = out.get("hybrid")
-        if hy:  # the per-seed breakdown stays in the details file
+        if hy:  # the per-seed breakdowns stay in the details file
             hy["error_vs_mc"] = {k: v for k, v in hy["error_vs_mc"].items() if k != "per_seed"}
+            hy["training"] = [{k: v for k, v in t.items() if k != "time_nll_per_epoch"} for t in hy["training"]]
         out["legs"] = legs_summary(out)
         print(json.dumps(out))
     if world > 1:
