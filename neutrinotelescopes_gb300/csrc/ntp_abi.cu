@@ -58,6 +58,8 @@ struct ntp_ctx {
     int* d_cell_items = nullptr;
     int grid_nx = 0, grid_ny = 0, n_cell_items = 0;
     float grid_x0 = 0, grid_y0 = 0, grid_h = 0;
+    int grid_lattice = 0;     // every cell holds at most its centred column
+    float lat_rcull2 = 0.0f;  // the largest r_cull^2
     double* d_axes = nullptr;  // PMT axes for the current orientation
     double* d_tgeo = nullptr;  // per-target tgeo for time residuals
 
@@ -155,6 +157,8 @@ bool fill_world_params(const ntp_ctx* ctx, PropParams& p) {
     p.grid_y0 = ctx->grid_y0;
     p.grid_h = ctx->grid_h;
     p.grid_inv_h = ctx->grid_h > 0 ? 1.0f / ctx->grid_h : 0.0f;
+    p.grid_lattice = ctx->grid_lattice;
+    p.lat_rcull2 = ctx->lat_rcull2;
     p.medium = ctx->d_med;
     p.n_medium = ctx->n_med;
     p.wl_min = ctx->wl_min;
@@ -461,6 +465,7 @@ ntp_status ntp_set_targets(ntp_ctx* ctx, const ntp_target* t, int32_t n, const f
     dfree(ctx->d_cell_start);
     dfree(ctx->d_cell_items);
     ctx->grid_nx = ctx->grid_ny = ctx->n_cell_items = 0;
+    ctx->grid_lattice = 0;
     if (use_cols) {
         NTP_CUDA(ctx, dupload(ctx->d_cols, cols.data(), cols.size(), ctx->stream));
         NTP_CUDA(ctx, dupload(ctx->d_members, members.data(), members.size(), ctx->stream));
@@ -521,6 +526,22 @@ ntp_status ntp_set_targets(ntp_ctx* ctx, const ntp_target* t, int32_t n, const f
         ctx->grid_x0 = static_cast<float>(x0);
         ctx->grid_y0 = static_cast<float>(y0);
         ctx->grid_h = static_cast<float>(h);
+        // lattice mode: each cell lists at most one column, each column is
+        // listed once, at the centre of its cell (within 1e-4 of the side)
+        bool lattice = items.size() == cols.size();
+        float rc2 = 0.0f;
+        for (size_t c = 0; c < cells.size() && lattice; ++c) {
+            if (cells[c].size() > 1) lattice = false;
+            if (cells[c].size() == 1) {
+                const ntp::Column& col = cols[cells[c][0]];
+                const double cx = x0 + (static_cast<double>(c % nx) + 0.5) * h;
+                const double cy = y0 + (static_cast<double>(c / nx) + 0.5) * h;
+                if (std::fabs(col.cx - cx) > 1e-4 * h || std::fabs(col.cy - cy) > 1e-4 * h) lattice = false;
+                rc2 = std::max(rc2, col.r_cull * col.r_cull);
+            }
+        }
+        ctx->grid_lattice = lattice ? 1 : 0;
+        ctx->lat_rcull2 = rc2;
     }
     NTP_CUDA(ctx, dupload(ctx->d_tgt, tg.data(), n, ctx->stream));
     NTP_CUDA(ctx, dupload(ctx->d_tgt_id, ids.data(), n, ctx->stream));

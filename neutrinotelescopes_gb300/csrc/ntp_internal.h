@@ -60,6 +60,12 @@ struct PropParams {
     const int* cell_items;                // device, column indices
     int grid_nx, grid_ny, n_cell_items;
     float grid_x0, grid_y0, grid_h, grid_inv_h;
+    // Lattice mode (grid_lattice != 0): every cell holds at most one column,
+    // sitting at the cell's centre (strings on a regular lattice); a step
+    // then tests the lattice points near its line directly instead of
+    // walking every cell it crosses.  lat_rcull2: the largest r_cull^2.
+    int grid_lattice;
+    float lat_rcull2;
 
     const float4* medium;                 // device, per knot (n, v_group, l_scatter, 0)
     int n_medium;

@@ -221,6 +221,46 @@ __device__ __forceinline__ void grid_candidates(const PropParams& p, const int* 
     }
 }
 
+// The lattice form of grid_candidates (grid_lattice): the columns sit at the
+// cell centres (i + 1/2, j + 1/2) h of a regular lattice, at most one per
+// cell.  In lattice units (u, v) along the step's major horizontal axis u,
+// a column within R of the segment has |u - u(segment)| <= R / h and lies
+// within R of the line, i.e. |v_col - v_line(u_col)| <= R / (h cos phi) <=
+// sqrt(2) R / h (cos phi >= 1/sqrt 2 on the major axis).  With R^2 the
+// largest r_cull^2 plus the single-precision envelope of the step (as in
+// column_candidates) and a 1e-3 margin for the rounding of u and v, the
+// points kept include every column column_candidates could accept; each
+// goes through column_candidates, so the hits equal the plain scan's.  A
+// step costs one short loop over the lattice rows its u range spans
+// (usually one to four), with no cell-crossing bookkeeping.
+__device__ __forceinline__ void lattice_candidates(const PropParams& p, const int* __restrict__ cstart,
+                                                   const int* __restrict__ citems, const Column* __restrict__ cols,
+                                                   const int* __restrict__ mem, const float4* __restrict__ tg,
+                                                   const SegmentView& sg, int& hit_t, float& hit_d) {
+    const float inv_h = p.grid_inv_h;
+    const float ua = (sg.pos.x - p.grid_x0) * inv_h - 0.5f, va = (sg.pos.y - p.grid_y0) * inv_h - 0.5f;
+    const float du = sg.dir.x * sg.step * inv_h, dv = sg.dir.y * sg.step * inv_h;
+    const float delta = fast_sqrt(2.0f * (p.lat_rcull2 + sg.slack2)) * inv_h + 1e-3f;
+    const bool u_major = fabsf(du) >= fabsf(dv);
+    // major axis a (extent n_a), minor axis b (extent n_b)
+    const float a0 = u_major ? ua : va, b0 = u_major ? va : ua;
+    const float da = u_major ? du : dv, db = u_major ? dv : du;
+    const int n_a = u_major ? p.grid_nx : p.grid_ny, n_b = u_major ? p.grid_ny : p.grid_nx;
+    const float slope = da != 0.0f ? db / da : 0.0f;  // |slope| <= 1
+    const int a_lo = max(0, static_cast<int>(ceilf(fminf(a0, a0 + da) - delta)));
+    const int a_hi = min(n_a - 1, static_cast<int>(floorf(fmaxf(a0, a0 + da) + delta)));
+    for (int ia = a_lo; ia <= a_hi; ++ia) {
+        const float b = fmaf(static_cast<float>(ia) - a0, slope, b0);
+        const int b_lo = max(0, static_cast<int>(ceilf(b - delta)));
+        const int b_hi = min(n_b - 1, static_cast<int>(floorf(b + delta)));
+        for (int ib = b_lo; ib <= b_hi; ++ib) {
+            const int c = u_major ? ib * p.grid_nx + ia : ia * p.grid_nx + ib;
+            if (cstart[c + 1] > cstart[c])
+                column_candidates(cols[citems[cstart[c]]], mem, tg, sg, p.hit_policy, hit_t, hit_d);
+        }
+    }
+}
+
 // initialize_photon_state methods, photon_prop_cuda.jl:133-200 and
 // sample_cherenkov_direction :107-125.
 __device__ __forceinline__ void init_photon(Photon& ph, const ntp_source* __restrict__ sources,
@@ -413,7 +453,10 @@ __global__ void __launch_bounds__(kPropBlock, kMinBlocks) propagate_kernel(const
             if (cols) {
                 const SegmentView sg = make_segment(ph.pos, ph.dir, step);
                 if (cstart) {
-                    grid_candidates(p, cstart, citems, cols, mem, tg, sg, hit_t, hit_d);
+                    if (p.grid_lattice)
+                        lattice_candidates(p, cstart, citems, cols, mem, tg, sg, hit_t, hit_d);
+                    else
+                        grid_candidates(p, cstart, citems, cols, mem, tg, sg, hit_t, hit_d);
                 } else {
                     for (int c = 0; c < p.n_columns; ++c)
                         column_candidates(cols[c], mem, tg, sg, p.hit_policy, hit_t, hit_d);

@@ -212,6 +212,29 @@ def test_grid_culling_matches_plain_scan_on_string_grid():
         b.close()
 
 
+def test_grid_walk_matches_plain_scan_on_irregular_strings():
+    # 16 strings at random positions (no lattice): the cell walk, not the
+    # lattice form, culls; both policies keep exactly the hits of the full scan
+    rng = np.random.default_rng(9)
+    targets = []
+    for k in range(16):
+        x, y = rng.uniform(-60.0, 60.0, 2)
+        targets += nt.string_of_modules(12, 15.0, x=float(x), y=float(y), z_start=0.0, pmt_area=workloads.PMT_AREA,
+                                        id_offset=len(targets))
+    srcs = workloads.cascade_sources(3, np.random.default_rng(6), photon_scale=2e-4, string_z=(0.0, 165.0),
+                                     distance=8.0)
+    m = nt.make_simple_water()
+    for policy in ("first", "nearest"):
+        a = nt.PhotonPropSetup(srcs, targets, m, nt.InverseSquareSpectrum(300.0, 600.0), hit_policy=policy)
+        b = nt.PhotonPropSetup(srcs, targets, m, nt.InverseSquareSpectrum(300.0, 600.0), hit_policy=policy,
+                               plain_scan=True)
+        ha, hb = gpu_hits(a, seed=23), gpu_hits(b, seed=23)
+        assert len(ha) > 100
+        assert ha.tobytes() == hb.tobytes()
+        a.close()
+        b.close()
+
+
 def test_axicone_pole_quirk_half_cone():
     # rot_from_ez_fast at a = e_z (utils.jl:230-232): every photon of a cone about +z has y >= 0
     src = nt.AxiconeEmitter((0.0, 0.0, 0.0), (0.0, 0.0, 1.0), 0.0, 100_000, 0.7)
