@@ -87,8 +87,9 @@ def parse():
     ap.add_argument("--flow", type=int, default=1, help="1: include the flow surrogate measurement")
     ap.add_argument("--legs", default="propagation,serving,flow,hybrid",
                     help="comma list of the measurements to run: propagation (the headline line), serving, flow, "
-                         "hybrid; compat (the bench cascades in the reference's own water, not in the default "
-                         "list) runs when propagation is not among them")
+                         "hybrid; compat (the bench cascades in the reference's own water) and grid (propagation "
+                         "on the 10 x 10 string grid), not in the default list, run when propagation is not among "
+                         "them")
     ap.add_argument("--details", default=None, help="also write the full per-leg results (JSON) to this path")
     ap.add_argument("--small", action="store_true",
                     help="profiling case: one cascade at 1% of its photons, 64 MB hit buffer, 256 MB L2 flush")
@@ -446,6 +447,51 @@ def train_hybrid_models(tab, seed: int, shape_steps: int, count_steps: int, coun
                                         "time_nll_per_epoch": [round(x, 5) for x in nll_per_epoch],
                                         "count_members": count_members, "count_steps_per_member": count_steps,
                                         "count_seconds": time.perf_counter() - t0}
+
+
+def grid_bench(steps: int = 3, photon_scale: float = 0.01) -> dict:
+    """Propagation on the serving detector's geometry: three EM cascades
+    (1e3-1e5 GeV at photon_scale of their photons) 8 m from the centre of a
+    10 x 10 grid of strings (50 m apart, 20 POM modules each), simple water;
+    hits kept on the device.  Device photons/s (CUDA events, two warm-up
+    launches)."""
+    import numpy as np
+    import torch
+
+    from neutrinotelescopes_gb300 import _abi, workloads
+    from neutrinotelescopes_gb300.medium import make_simple_water
+    from neutrinotelescopes_gb300.photon_prop import PhotonPropSetup, pack_sources
+    from neutrinotelescopes_gb300.spectrum import InverseSquareSpectrum
+
+    srcs = workloads.cascade_sources(3, np.random.default_rng(5), photon_scale=photon_scale, string_z=(0.0, 285.0),
+                                     distance=8.0)
+    setup = PhotonPropSetup(srcs, workloads.string_grid(10, 10, 50.0, 20, 15.0), make_simple_water(),
+                            InverseSquareSpectrum(300.0, 600.0))
+    lib, ctx = setup.context()
+    psrc = pack_sources(setup.sources)
+    photons = sum(int(s.photons) for s in setup.sources)
+    cap = 1 << 22
+    hits = torch.empty((cap, 64), dtype=torch.uint8, device="cuda")
+    stream = torch.cuda.current_stream()
+    opts = setup.prop_opts(stream=stream.cuda_stream)
+    nh, ns = C.c_uint64(), C.c_uint64()
+    ms = []
+    for i in range(2 + steps):
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        a.record(stream)
+        st = lib.ntp_propagate(ctx, psrc, len(setup.sources), 100 + i, C.byref(opts), hits.data_ptr(), cap, 1,
+                               C.byref(nh), C.byref(ns))
+        b.record(stream)
+        torch.cuda.synchronize()
+        if st != _abi.NTP_OK:
+            raise _abi.NtpError(st, lib.ntp_last_error(ctx).decode())
+        if i >= 2:
+            ms.append(a.elapsed_time(b))
+    setup.close()
+    t = sum(ms) / 1e3
+    return {"workload": f"3 EM cascades at {photon_scale} of their photons, 10 x 10 strings x 20 POM modules "
+                        "(50 m, 15 m), simple water", "photons_per_step": photons, "steps": steps,
+            "photons_per_s": photons * steps / t, "ms_per_step": 1e3 * t / steps, "hits_last_step": int(nh.value)}
 
 
 def hybrid_bench(n_events: int = 10_000, batch: int = 256, shape_steps: int = 48_000, count_steps: int = 24_000,
@@ -815,6 +861,8 @@ def main():
             out["hybrid"] = hybrid_bench()
         if "compat" in legs and rank == 0:
             out["compat_medium"] = compat_bench()
+        if "grid" in legs and rank == 0:
+            out["string_grid"] = grid_bench()
         if rank == 0:
             if args.details:
                 Path(args.details).write_text(json.dumps(out, indent=1))
