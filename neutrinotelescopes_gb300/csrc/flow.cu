@@ -976,6 +976,9 @@ struct ntp_flow {
     float* lr_dev = nullptr;  // Adam's step size on the device
     // the training step captured as a CUDA graph (per batch size and update flag)
     bool use_graph = true;
+    // the conditioner's forward pass and the backward chain of activation
+    // gradients as one fused kernel each (NTP_FLOW_CHAIN=0: one GEMM per layer)
+    bool use_chain = true;
     cudaGraphExec_t gexec = nullptr;
     int g_B = 0, g_update = -1, g_rows_w = -1;
     // per-step losses and skip flags of a multi-step call (grown on demand)
@@ -1036,6 +1039,34 @@ ntp_status gemm(ntp_flow* f, const bf16* A, int lda, const bf16* B, int ldb, int
 // P = conditioner(X) for n rows (X packed, n a multiple of 128); for
 // training also the transposed activations the weight gradients read
 ntp_status forward(ntp_flow* f, int n, bool keep_transposed) {
+    if (f->use_chain) {
+        // X -> H1 -> H2 -> H3 -> P in one kernel per 128-row tile; for
+        // training the activations (the backward pass's ReLU masks) and their
+        // transposes (the weight gradients' operands) go to global memory too
+        ntp::ChainSpec cs{};
+        cs.n_stages = 4;
+        cs.m = n;
+        for (int l = 0; l < 3; ++l) {
+            ntp::ChainStage& s = cs.st[l];
+            s.n = kHid;
+            s.k = l == 0 ? kIn : kHid;
+            s.bias = f->theta + f->blk[2 * l + 1].off;
+            s.relu = 1;
+            s.c = keep_transposed ? f->h[l] : nullptr;
+            s.ldc = kHid;
+            s.ct = keep_transposed ? f->ht[l] : nullptr;
+            s.ldct = n;
+        }
+        ntp::ChainStage& o = cs.st[3];
+        o.n = f->n_pad;
+        o.k = kHid;
+        o.bias = f->theta + f->blk[7].off;
+        o.c32 = f->P;
+        o.ldc32 = f->n_pad;
+        const void* w[4] = {f->wb[0], f->wb[1], f->wb[2], f->wb[3]};
+        F_CUDA(f, ntp::layer_chain(f->x, kIn, w, cs, f->gemm_err, f->stream));
+        return NTP_OK;
+    }
     ntp::GemmEpilogue e{};
     e.out_kind = 1;
     e.relu = 1;
@@ -1148,9 +1179,41 @@ ntp_status record_step(ntp_flow* f, int B, bool update, bool rows_w) {
     ew.ldc = kHid;
     ew.c = gw(3);
     F_OK(gemm(f, f->dpt, B, f->ht[2], B, f->n_pad, kHid, B, ew, 0, s2));
+    if (f->use_chain) {
+        // dP -> dZ3 -> dZ2 -> dZ1 in one kernel per 128-row tile: each stage
+        // masked by its layer's activations, its transpose and column sums
+        // (the bias gradient) to global memory; then the three weight
+        // gradients dW_l = dZ_l^T X_l on the second stream
+        ntp::ChainSpec cs{};
+        cs.n_stages = 3;
+        cs.m = B;
+        for (int i = 0; i < 3; ++i) {
+            const int l = 2 - i;
+            ntp::ChainStage& s = cs.st[i];
+            s.n = kHid;
+            s.k = i == 0 ? f->n_pad : kHid;
+            s.mask = f->h[l];
+            s.ldm = kHid;
+            s.ct = f->dzt[l];
+            s.ldct = B;
+            s.colsum = gb(l);
+        }
+        const void* w[3] = {f->wt[3], f->wt[2], f->wt[1]};
+        F_CUDA(f, ntp::layer_chain(f->dp, f->n_pad, w, cs, f->gemm_err, st));
+        F_CUDA(f, cudaEventRecord(f->ev[1], st));
+        F_CUDA(f, cudaStreamWaitEvent(s2, f->ev[1], 0));
+        for (int l = 2; l >= 0; --l) {
+            ntp::GemmEpilogue eg{};
+            eg.out_kind = 2;
+            eg.c = gw(l);
+            eg.ldc = l == 0 ? kIn : kHid;
+            const bf16* xt = l == 0 ? f->xt : f->ht[l - 1];
+            F_OK(gemm(f, f->dzt[l], B, xt, B, kHid, l == 0 ? kIn : kHid, B, eg, 0, l == 1 ? st : s2));
+        }
+    }
     const bf16* dnext = f->dp;
     int k_next = f->n_pad;
-    for (int l = 2; l >= 0; --l) {
+    for (int l = 2; !f->use_chain && l >= 0; --l) {
         // dZ_l = (dZ_{l+1} W_{l+1}) masked by H_l > 0, its transpose, and its
         // column sums (the bias gradient of layer l)
         ntp::GemmEpilogue ed{};
@@ -1202,6 +1265,7 @@ ntp_status record_step(ntp_flow* f, int B, bool update, bool rows_w) {
 // Function attributes the step's kernels need, set before a capture.
 cudaError_t prepare_kernels(ntp_flow* f) {
     cudaError_t e = ntp::gemm_prepare();
+    if (e == cudaSuccess) e = ntp::layer_chain_prepare();
     if (e != cudaSuccess) return e;
     const size_t smem = sizeof(float) * ntp::head_smem_floats(f->L, f->K, f->n_pad);
     with_bins(f->K, [&](auto kc) {
@@ -1243,6 +1307,8 @@ ntp_status ntp_flow_create(int32_t device, const ntp_flow_config* cfg, ntp_flow*
     {
         const char* eg = std::getenv("NTP_FLOW_GRAPH");
         f->use_graph = !(eg && eg[0] == '0');
+        const char* ec = std::getenv("NTP_FLOW_CHAIN");
+        f->use_chain = !(ec && ec[0] == '0');
     }
     f->count_w = cfg->count_weight;
     const int dims[4][2] = {{kHid, kIn}, {kHid, kHid}, {kHid, kHid}, {f->n_pad, kHid}};

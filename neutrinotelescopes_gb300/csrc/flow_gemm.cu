@@ -32,14 +32,15 @@
 #include <mutex>
 
 #include "ntp_internal.h"
+#include "tc_ptx.cuh"
 
 namespace ntp {
 
 namespace {
 
+using namespace tc;
+
 constexpr int kBM = 128;   // rows of a tile (UMMA M)
-constexpr int kBK = 64;    // K slice per stage: 64 bf16 = 128 bytes = one swizzle row
-constexpr int kUK = 16;    // K of one tcgen05.mma for 16-bit inputs
 constexpr int kThreads = 128;
 constexpr unsigned long long kWaitLimitNs = 2000000000ull;  // by default a wait gives up after 2 s
 
@@ -52,96 +53,6 @@ std::atomic<int> g_pdl{[] {
     const char* e = std::getenv("NTP_GEMM_PDL");
     return (e && e[0] == '0') ? 0 : 1;
 }()};
-
-__device__ __forceinline__ uint32_t smem_u32(const void* p) {
-    return static_cast<uint32_t>(__cvta_generic_to_shared(p));
-}
-
-__device__ __forceinline__ void mbar_init(uint64_t* bar, uint32_t count) {
-    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count));
-}
-
-__device__ __forceinline__ void mbar_expect_tx(uint64_t* bar, uint32_t bytes) {
-    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)), "r"(bytes)
-                 : "memory");
-}
-
-__device__ __forceinline__ unsigned long long global_ns() {
-    unsigned long long t;
-    asm volatile("mov.u64 %0, %globaltimer;" : "=l"(t));
-    return t;
-}
-
-// Bounded wait for the phase with the given parity; false after limit_ns.
-__device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity, unsigned long long limit_ns) {
-    const uint32_t a = smem_u32(bar);
-    const unsigned long long t0 = global_ns();
-    for (unsigned i = 0;; ++i) {
-        uint32_t done;
-        asm volatile(
-            "{\n.reg .pred p;\nmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\nselp.b32 %0, 1, 0, p;\n}\n"
-            : "=r"(done)
-            : "r"(a), "r"(parity)
-            : "memory");
-        if (done) return true;
-        if ((i & 255u) == 255u && global_ns() - t0 > limit_ns) return false;
-    }
-}
-
-__device__ __forceinline__ void tma_load_2d(void* dst, const CUtensorMap* map, uint64_t* bar, int x, int y) {
-    asm volatile(
-        "cp.async.bulk.tensor.2d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%3, %4}], [%2];"
-        ::"r"(smem_u32(dst)), "l"(reinterpret_cast<uint64_t>(map)), "r"(smem_u32(bar)), "r"(x), "r"(y)
-        : "memory");
-}
-
-// Shared-memory matrix descriptor of a K-major tile with 128-byte swizzle:
-// 8-row groups of 128-byte rows, 1024 bytes apart (stride byte offset),
-// descriptor version 1, layout type 2 (SWIZZLE_128B).
-__device__ __forceinline__ uint64_t smem_desc_sw128(const void* p) {
-    const uint64_t addr = smem_u32(p);
-    uint64_t d = (addr & 0x3FFFFull) >> 4;
-    d |= static_cast<uint64_t>(1) << 16;             // leading byte offset (unused for swizzled K-major)
-    d |= static_cast<uint64_t>(1024 >> 4) << 32;     // stride byte offset
-    d |= static_cast<uint64_t>(1) << 46;             // version
-    d |= static_cast<uint64_t>(2) << 61;             // SWIZZLE_128B
-    return d;
-}
-
-// Instruction descriptor, kind::f16: FP32 accumulator, BF16 A and B, both
-// K-major, N and M encoded as N/8 and M/16.
-__host__ __device__ constexpr uint32_t instr_desc_bf16(int m, int n) {
-    return (1u << 4) | (1u << 7) | (1u << 10) | (static_cast<uint32_t>(n >> 3) << 17) |
-           (static_cast<uint32_t>(m >> 4) << 24);
-}
-
-__device__ __forceinline__ void umma_bf16(uint32_t tmem_d, uint64_t adesc, uint64_t bdesc, uint32_t idesc,
-                                          uint32_t accumulate) {
-    asm volatile(
-        "{\n.reg .pred p;\nsetp.ne.b32 p, %4, 0;\ntcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}\n"
-        ::"r"(tmem_d), "l"(adesc), "l"(bdesc), "r"(idesc), "r"(accumulate)
-        : "memory");
-}
-
-__device__ __forceinline__ void umma_commit(uint64_t* bar) {
-    asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(smem_u32(bar))
-                 : "memory");
-}
-
-__device__ __forceinline__ void tmem_ld32(uint32_t taddr, float* v) {
-    uint32_t r[32];
-    asm volatile(
-        "tcgen05.ld.sync.aligned.32x32b.x32.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15,"
-        "%16,%17,%18,%19,%20,%21,%22,%23,%24,%25,%26,%27,%28,%29,%30,%31}, [%32];"
-        : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),
-          "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15]),
-          "=r"(r[16]), "=r"(r[17]), "=r"(r[18]), "=r"(r[19]), "=r"(r[20]), "=r"(r[21]), "=r"(r[22]), "=r"(r[23]),
-          "=r"(r[24]), "=r"(r[25]), "=r"(r[26]), "=r"(r[27]), "=r"(r[28]), "=r"(r[29]), "=r"(r[30]), "=r"(r[31])
-        : "r"(taddr));
-    asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
-#pragma unroll
-    for (int i = 0; i < 32; ++i) v[i] = __uint_as_float(r[i]);
-}
 
 // pipeline depth: 4 stages (3 for the widest tile), within 227 KB of shared memory
 template <int BN>
@@ -254,7 +165,9 @@ __global__ void __launch_bounds__(kThreads, 1)
     asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
     // the accumulator is complete when `done` flips (a thread that timed out
     // above still committed, so this wait ends once its MMAs drain)
-    const bool have = (kt1 > kt0) && mbar_wait(&s->done, 0, wait_ns);
+    // warp-uniform: tcgen05.ld below is .sync.aligned, and lanes whose
+    // bounded waits end on either side of the limit must not split a warp
+    const bool have = __all_sync(0xffffffffu, (kt1 > kt0) && mbar_wait(&s->done, 0, wait_ns));
     if (kt1 > kt0 && !have && lane == 0) atomicExch(error, 2);
     asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
 
@@ -457,6 +370,39 @@ int sm_count() {
 }
 
 }  // namespace
+
+namespace tc {
+bool tensor_map_bf16(CUtensorMap* map, const void* base, int rows, int cols, int ld, int box_rows) {
+    return make_map(map, base, rows, cols, ld, box_rows);
+}
+bool tensor_map_bf16_plain(CUtensorMap* map, const void* base, int rows, int cols, int ld, int box_cols,
+                           int box_rows) {
+    EncodeTiled enc = encode_fn();
+    if (!enc) return false;
+    const cuuint64_t dims[2] = {static_cast<cuuint64_t>(cols), static_cast<cuuint64_t>(rows)};
+    const cuuint64_t strides[1] = {static_cast<cuuint64_t>(ld) * 2};
+    const cuuint32_t box[2] = {static_cast<cuuint32_t>(box_cols), static_cast<cuuint32_t>(box_rows)};
+    const cuuint32_t estr[2] = {1, 1};
+    return enc(map, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2, const_cast<void*>(base), dims, strides, box, estr,
+               CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+               CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
+}
+bool tensor_map_f32_sw128(CUtensorMap* map, const void* base, int rows, int cols, int ld, int box_rows) {
+    EncodeTiled enc = encode_fn();
+    if (!enc) return false;
+    const cuuint64_t dims[2] = {static_cast<cuuint64_t>(cols), static_cast<cuuint64_t>(rows)};
+    const cuuint64_t strides[1] = {static_cast<cuuint64_t>(ld) * 4};
+    const cuuint32_t box[2] = {32, static_cast<cuuint32_t>(box_rows)};
+    const cuuint32_t estr[2] = {1, 1};
+    return enc(map, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 2, const_cast<void*>(base), dims, strides, box, estr,
+               CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+               CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
+}
+int device_sm_count() { return sm_count(); }
+unsigned long long wait_limit_ns() { return g_wait_limit_ns.load(); }
+int withhold_first() { return g_withhold_first.load(); }
+int pdl_enabled() { return g_pdl.load(); }
+}  // namespace tc
 
 // C = A * B^T on the tensor cores with the epilogue ep; see the file comment.
 // lda / ldb in elements; A's and B's rows must start on 16-byte boundaries

@@ -230,6 +230,37 @@ cudaError_t gemm_prepare();
 cudaError_t gemm_bf16(const void* A, int lda, const void* B, int ldb, void* C, int ldc, int M, int N, int K,
                       const float* bias, int relu, int out_kind, int splits, int* error, cudaStream_t st);
 
+// One stage of a layer chain (flow_chain.cu): D = A W^T with n output and k
+// input columns, value = D (+ bias[col]) (ReLU) (zeroed where
+// mask[row][col] <= 0), stored as BF16 row-major to c, FP32 row-major to c32,
+// BF16 transposed to ct (ct[col * ldct + row]) and summed per column into
+// colsum (FP32 atomics); every output pointer may be NULL.  The value also
+// becomes the next stage's A (BF16, on chip).
+constexpr int kMaxChainStages = 4;
+struct ChainStage {
+    int n, k;
+    const float* bias;
+    int relu;
+    const __nv_bfloat16* mask;
+    int ldm;
+    __nv_bfloat16* c;
+    int ldc;
+    float* c32;
+    int ldc32;
+    __nv_bfloat16* ct;
+    int ldct;
+    float* colsum;
+};
+struct ChainSpec {
+    int n_stages;
+    int m;  // rows
+    ChainStage st[kMaxChainStages];
+};
+cudaError_t layer_chain(const void* a, int lda, const void* const* w, const ChainSpec& spec, int* error,
+                        cudaStream_t stream);
+// Sets the chain kernel's function attributes (before a stream capture).
+cudaError_t layer_chain_prepare();
+
 // training-table generator passes (tables.cu)
 cudaError_t launch_table_count(const ntp_hit* hits, unsigned long long n, const double* w, const double* scale,
                                int n_sims, int R, int P, float3 center, const float* axes, float cos_open,

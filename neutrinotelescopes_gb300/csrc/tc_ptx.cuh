@@ -1,0 +1,125 @@
+// tc_ptx.cuh -- inline-PTX building blocks of the tcgen05 kernels (the BF16
+// GEMM and the fused layer chain of the flow's conditioner): shared-memory
+// barriers with bounded waits, 2-D TMA loads, shared-memory matrix and
+// instruction descriptors, tcgen05.mma / commit and tensor-memory loads.
+#pragma once
+
+#include <cuda.h>
+#include <cstdint>
+
+namespace ntp {
+namespace tc {
+
+constexpr int kBK = 64;  // K slice of a pipeline stage: 64 bf16 = 128 bytes = one swizzle row
+constexpr int kUK = 16;  // K of one tcgen05.mma for 16-bit inputs
+
+// Host side (flow_gemm.cu).  Tensor map of a row-major bf16 matrix [rows x
+// cols] (leading dimension ld elements) read in boxes of box_rows x 64 with
+// 128-byte swizzle, zero fill beyond the matrix; false if the driver's
+// encoder is missing or rejects the layout.
+bool tensor_map_bf16(CUtensorMap* map, const void* base, int rows, int cols, int ld, int box_rows);
+// The same matrix read or written in boxes of box_rows x box_cols without
+// swizzle (shared-memory box row-major, box_cols contiguous).
+bool tensor_map_bf16_plain(CUtensorMap* map, const void* base, int rows, int cols, int ld, int box_cols,
+                           int box_rows);
+// A row-major FP32 matrix in boxes of box_rows x 32 with 128-byte swizzle.
+bool tensor_map_f32_sw128(CUtensorMap* map, const void* base, int rows, int cols, int ld, int box_rows);
+int device_sm_count();
+// the failure-detection controls of ntp_gemm_set_wait_limit and the
+// programmatic-dependent-launch switch (NTP_GEMM_PDL), read at each launch
+unsigned long long wait_limit_ns();
+int withhold_first();
+int pdl_enabled();
+
+__device__ __forceinline__ uint32_t smem_u32(const void* p) {
+    return static_cast<uint32_t>(__cvta_generic_to_shared(p));
+}
+
+__device__ __forceinline__ void mbar_init(uint64_t* bar, uint32_t count) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count));
+}
+
+__device__ __forceinline__ void mbar_expect_tx(uint64_t* bar, uint32_t bytes) {
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)), "r"(bytes)
+                 : "memory");
+}
+
+__device__ __forceinline__ unsigned long long global_ns() {
+    unsigned long long t;
+    asm volatile("mov.u64 %0, %globaltimer;" : "=l"(t));
+    return t;
+}
+
+// Bounded wait for the phase with the given parity; false after limit_ns.
+__device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity, unsigned long long limit_ns) {
+    const uint32_t a = smem_u32(bar);
+    const unsigned long long t0 = global_ns();
+    for (unsigned i = 0;; ++i) {
+        uint32_t done;
+        asm volatile(
+            "{\n.reg .pred p;\nmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\nselp.b32 %0, 1, 0, p;\n}\n"
+            : "=r"(done)
+            : "r"(a), "r"(parity)
+            : "memory");
+        if (done) return true;
+        if ((i & 255u) == 255u && global_ns() - t0 > limit_ns) return false;
+    }
+}
+
+__device__ __forceinline__ void tma_load_2d(void* dst, const CUtensorMap* map, uint64_t* bar, int x, int y) {
+    asm volatile(
+        "cp.async.bulk.tensor.2d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%3, %4}], [%2];"
+        ::"r"(smem_u32(dst)), "l"(reinterpret_cast<uint64_t>(map)), "r"(smem_u32(bar)), "r"(x), "r"(y)
+        : "memory");
+}
+
+// Shared-memory matrix descriptor of a K-major tile with 128-byte swizzle:
+// 8-row groups of 128-byte rows, 1024 bytes apart (stride byte offset),
+// descriptor version 1, layout type 2 (SWIZZLE_128B).
+__device__ __forceinline__ uint64_t smem_desc_sw128(const void* p) {
+    const uint64_t addr = smem_u32(p);
+    uint64_t d = (addr & 0x3FFFFull) >> 4;
+    d |= static_cast<uint64_t>(1) << 16;             // leading byte offset (unused for swizzled K-major)
+    d |= static_cast<uint64_t>(1024 >> 4) << 32;     // stride byte offset
+    d |= static_cast<uint64_t>(1) << 46;             // version
+    d |= static_cast<uint64_t>(2) << 61;             // SWIZZLE_128B
+    return d;
+}
+
+// Instruction descriptor, kind::f16: FP32 accumulator, BF16 A and B, both
+// K-major, N and M encoded as N/8 and M/16.
+__host__ __device__ constexpr uint32_t instr_desc_bf16(int m, int n) {
+    return (1u << 4) | (1u << 7) | (1u << 10) | (static_cast<uint32_t>(n >> 3) << 17) |
+           (static_cast<uint32_t>(m >> 4) << 24);
+}
+
+__device__ __forceinline__ void umma_bf16(uint32_t tmem_d, uint64_t adesc, uint64_t bdesc, uint32_t idesc,
+                                          uint32_t accumulate) {
+    asm volatile(
+        "{\n.reg .pred p;\nsetp.ne.b32 p, %4, 0;\ntcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}\n"
+        ::"r"(tmem_d), "l"(adesc), "l"(bdesc), "r"(idesc), "r"(accumulate)
+        : "memory");
+}
+
+__device__ __forceinline__ void umma_commit(uint64_t* bar) {
+    asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(smem_u32(bar))
+                 : "memory");
+}
+
+__device__ __forceinline__ void tmem_ld32(uint32_t taddr, float* v) {
+    uint32_t r[32];
+    asm volatile(
+        "tcgen05.ld.sync.aligned.32x32b.x32.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15,"
+        "%16,%17,%18,%19,%20,%21,%22,%23,%24,%25,%26,%27,%28,%29,%30,%31}, [%32];"
+        : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),
+          "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15]),
+          "=r"(r[16]), "=r"(r[17]), "=r"(r[18]), "=r"(r[19]), "=r"(r[20]), "=r"(r[21]), "=r"(r[22]), "=r"(r[23]),
+          "=r"(r[24]), "=r"(r[25]), "=r"(r[26]), "=r"(r[27]), "=r"(r[28]), "=r"(r[29]), "=r"(r[30]), "=r"(r[31])
+        : "r"(taddr));
+    asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+#pragma unroll
+    for (int i = 0; i < 32; ++i) v[i] = __uint_as_float(r[i]);
+}
+
+}  // namespace tc
+}  // namespace ntp

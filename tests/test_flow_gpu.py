@@ -497,3 +497,60 @@ def test_log_expectation_query_matches_evaluate():
         fl._check(fl.lib.ntp_flow_evaluate(fl._h, cond.ctypes.data, n, None, None, 0, None, ref.ctypes.data, 0))
     np.testing.assert_array_equal(le_h, ref)
     np.testing.assert_array_equal(le_d, ref)
+
+
+def _flow_with_chain(monkeypatch, chain, L, K, r0, r1, cap=2048, seed=1):
+    monkeypatch.setenv("NTP_FLOW_CHAIN", "1" if chain else "0")
+    return make(L, K, r0, r1, cap=cap, seed=seed)
+
+
+@pytest.mark.parametrize("L,K,r0,r1", CASES)
+def test_layer_chain_matches_per_layer_gemms(monkeypatch, L, K, r0, r1):
+    """The fused layer chain (forward X -> H1 -> H2 -> H3 -> P and backward
+    dP -> dZ3 -> dZ2 -> dZ1 in one kernel per 128-row tile) against one
+    tensor-core GEMM per layer on the same weights and batch.  Both
+    accumulate every output over K in the same slice order in FP32 and round
+    the same activations to BF16, so P, the loss and the gradient agree to
+    the last bits (atomic column sums and split-K weight gradients add in
+    varying order: 1e-5 relative per parameter block)."""
+    rng = np.random.default_rng(50 + L)
+    B = 1024
+    cond, tres, nhits, has = batch(rng, B, r0, r1)
+    out = {}
+    for chain in (True, False):
+        with _flow_with_chain(monkeypatch, chain, L, K, r0, r1) as fl:
+            P = fl.forward_params(cond[:1000])  # not a multiple of 128: the last tile is partly padding
+            loss = fl.train_step(cond, tres, nhits, has, update=False)
+            out[chain] = (P, loss, fl.gradient().astype(np.float64), fl.layout())
+    (P1, l1, g1, layout), (P0, l0, g0, _) = out[True], out[False]
+    np.testing.assert_array_equal(P1, P0)
+    assert l1 == pytest.approx(l0, rel=1e-6)
+    for name, shape, off in layout:
+        size = int(np.prod(shape))
+        a, b = g1[off:off + size], g0[off:off + size]
+        assert np.linalg.norm(a - b) <= 1e-5 * np.linalg.norm(b) + 1e-9, (name, np.abs(a - b).max())
+
+
+def test_layer_chain_wait_runs_out(monkeypatch):
+    """Failure detection of the fused chain: with its input tile withheld the
+    first barrier is a flag that nothing completes; the bounded wait gives up
+    after 1 ms, the call returns NTP_ERR_TIMEOUT and the context stays usable
+    (the same forward pass succeeds afterwards)."""
+    import time
+
+    lib = _abi.load_library()
+    rng = np.random.default_rng(5)
+    cond = rng.uniform(-1, 1, (256, 5)).astype(np.float32)
+    with _flow_with_chain(monkeypatch, True, 5, 12, -20.0, 1500.0) as fl:
+        ref = fl.forward_params(cond)
+        assert lib.ntp_gemm_set_wait_limit(1_000_000, 1) == _abi.NTP_OK
+        try:
+            t0 = time.perf_counter()
+            with pytest.raises(_abi.NtpError) as ei:
+                fl.forward_params(cond)
+            elapsed = time.perf_counter() - t0
+        finally:
+            assert lib.ntp_gemm_set_wait_limit(0, 0) == _abi.NTP_OK
+        assert ei.value.status == _abi.NTP_ERR_TIMEOUT
+        assert elapsed < 1.0
+        np.testing.assert_array_equal(fl.forward_params(cond), ref)
