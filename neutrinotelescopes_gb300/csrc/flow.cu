@@ -357,15 +357,26 @@ __device__ __forceinline__ float input_column(const float* __restrict__ f, int j
 }
 
 // cond [n x 5] FP32 -> X [n x 64] BF16 (zero padded) and X^T [64 x n];
-// rows >= n_valid are zero
+// rows >= n_valid are zero.  Thread (b, g) writes columns 8g .. 8g + 7 of
+// row b, with b fastest across threads: the transposed stores of a warp are
+// contiguous, the row stores one 16-byte vector each.
 __global__ void pack_kernel(const float* __restrict__ cond, int n_valid, int n, int mode,
                             __nv_bfloat16* __restrict__ x, __nv_bfloat16* __restrict__ xt) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= n * kIn) return;
-    const int b = i / kIn, j = i % kIn;
-    const __nv_bfloat16 v = __float2bfloat16(b < n_valid ? input_column(cond + b * kCond, j, mode) : 0.0f);
-    x[i] = v;
-    xt[static_cast<size_t>(j) * n + b] = v;
+    if (i >= n * (kIn / 8)) return;
+    const int b = i % n, g = i / n;
+    const float* f = cond + static_cast<size_t>(b) * kCond;
+    uint32_t w[4];
+#pragma unroll
+    for (int e = 0; e < 4; ++e) {
+        const int j = 8 * g + 2 * e;
+        const __nv_bfloat162 h = __floats2bfloat162_rn(b < n_valid ? input_column(f, j, mode) : 0.0f,
+                                                       b < n_valid ? input_column(f, j + 1, mode) : 0.0f);
+        w[e] = *reinterpret_cast<const uint32_t*>(&h);
+        xt[static_cast<size_t>(j) * n + b] = h.x;
+        xt[static_cast<size_t>(j + 1) * n + b] = h.y;
+    }
+    *reinterpret_cast<uint4*>(x + static_cast<size_t>(b) * kIn + 8 * g) = make_uint4(w[0], w[1], w[2], w[3]);
 }
 
 // Shared-memory layout of the head kernel for L layers of K bins and a
@@ -377,7 +388,8 @@ __host__ __device__ constexpr int head_smem_floats(int L, int K, int ldp) {
            + L * 32 * 7                               // adjoint dL/du
            + 32 * 4                                   // per sample: dL/dx innermost, shift, scale, log expectation
            + L * 32 + 32                              // per layer and sample: squared gradient norm; clip factor
-           + 32 * ldp / 2;                            // the block's rows of dL/dP in BF16
+           + 32 * (ldp + 2) / 2                       // the block's rows of dL/dP in BF16 (padded stride)
+           + 32 * (ldp + 1);                          // the block's rows of P (padded stride)
 }
 
 // Loss and gradient of the head.  P [B x ldp] FP32.  A block takes 32
@@ -394,10 +406,13 @@ __host__ __device__ constexpr int head_smem_floats(int L, int K, int ldp) {
 //                   the sample's row of dL/dP scaled to an L2 norm of at most
 //                   clip / B; warp 0 adds shift, scale, log expectation and
 //                   the padding
-// Outputs: dL/dP as BF16 row-major dp [B x ldp] (rows staged in shared memory,
-// written as 16-byte vectors) and transposed dpt [ldp x B]; optionally FP32
-// row-major gf; the output layer's bias gradient into gbias (a warp-sum and
-// one atomic per column and warp); the batch-mean loss into *loss.
+// The block's 32 rows of P are first copied to shared memory with coalesced
+// 16-byte loads (a row stride of ldp + 1 words keeps each lane's reads of
+// its own row in its own bank).
+// Outputs: dL/dP as BF16 row-major dp [B x ldp] (rows staged in shared memory)
+// and transposed dpt [ldp x B]; optionally FP32 row-major gf; the output
+// layer's bias gradient into gbias (per warp a transpose-reduce of 32 columns
+// and one atomic per column); the batch-mean loss into *loss.
 template <int K>
 __global__ void __launch_bounds__(32 * kMaxLayers) head_grad_kernel(
     const float* __restrict__ P, int ldp, int L, const float* __restrict__ y, const float* __restrict__ nhits,
@@ -416,10 +431,47 @@ __global__ void __launch_bounds__(32 * kMaxLayers) head_grad_kernel(
     float* s_s = s_g + S * 7;                  // [32][4]
     float* s_n2 = s_s + 32 * 4;                // [L][32]
     float* s_f = s_n2 + S;                     // [32]
-    uint16_t* s_dp = reinterpret_cast<uint16_t*>(s_f + 32);  // [32][ldp]
+    // [32][ldp + 2]: the row stride of 97 words puts the lanes' stores to one
+    // column in 32 different banks
+    const int lds = ldp + 2;
+    uint16_t* s_dp = reinterpret_cast<uint16_t*>(s_f + 32);
+    const int ldsp = ldp + 1;
+    float* s_p = reinterpret_cast<float*>(s_dp) + 16 * lds;  // [32][ldp + 1]
+    // warp w copies rows w, w + L, ..., four rows at a time (all loads in
+    // flight before the stores); lane c the row's 16-byte columns c, c + 32
+    // (ldp <= 256: at most two per lane)
+    for (int r0 = warp; r0 < 32; r0 += 4 * L) {
+        float4 v[4][2];
+#pragma unroll
+        for (int u = 0; u < 4; ++u) {
+            const int r = r0 + u * L, rb = blockIdx.x * 32 + r;
+            const float4* src = reinterpret_cast<const float4*>(P + static_cast<size_t>(rb) * ldp);
+#pragma unroll
+            for (int h = 0; h < 2; ++h) {
+                const int c = lane + 32 * h;
+                v[u][h] = (r < 32 && rb < B && c < ldp / 4) ? __ldg(src + c) : make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+            }
+        }
+#pragma unroll
+        for (int u = 0; u < 4; ++u) {
+            const int r = r0 + u * L;
+#pragma unroll
+            for (int h = 0; h < 2; ++h) {
+                const int c = lane + 32 * h;
+                if (r < 32 && c < ldp / 4) {
+                    float* d = s_p + r * ldsp + 4 * c;
+                    d[0] = v[u][h].x;
+                    d[1] = v[u][h].y;
+                    d[2] = v[u][h].z;
+                    d[3] = v[u][h].w;
+                }
+            }
+        }
+    }
+    __syncthreads();
     const int b = blockIdx.x * 32 + lane;
     const bool act = b < B;
-    const float* p = P + static_cast<size_t>(act ? b : 0) * ldp;
+    const float* p = s_p + lane * ldsp;
     const int li = warp;
     const int slot = li * 32 + lane;
     const int o_shift = L * NP, o_scale = o_shift + 1, o_le = o_shift + 2;
@@ -460,8 +512,11 @@ __global__ void __launch_bounds__(32 * kMaxLayers) head_grad_kernel(
                 const float* q = s_kn + (k * 32 + lane) * KN;
                 s_y[k * 32 + lane] = cur;
                 s_bin[k * 32 + lane] = cur <= q[NK] ? -1 : (cur >= q[NK + K] ? K : find_bin<K>(q + NK, cur));
+                // the chain with the hardware reciprocal and logarithm
+                // (relative error ~1e-6; the gradient's dual numbers below
+                // are exact to FP32)
                 float x, ld;
-                inv_spline<K>(q, q + NK, q + 2 * NK, cur, x, ld);
+                inv_spline_fast<K>(q, q + NK, q + 2 * NK, cur, x, ld);
                 cur = x;
                 ldsum += ld;
             }
@@ -522,16 +577,18 @@ __global__ void __launch_bounds__(32 * kMaxLayers) head_grad_kernel(
     }
     __syncthreads();
     // P5
-    auto emit = [&](int col, float v) {
+    // stores of column col (not its bias-gradient sum)
+    auto store_col = [&](int col, float v) {
         if (act) {
-            s_dp[lane * ldp + col] = __bfloat16_as_ushort(__float2bfloat16(v));
+            s_dp[lane * lds + col] = __bfloat16_as_ushort(__float2bfloat16(v));
             dpt[static_cast<size_t>(col) * B + b] = __float2bfloat16(v);
             if (gf) gf[static_cast<size_t>(b) * ldp + col] = v;
         }
-        if (gbias) {
-            const float sum = warp_sum(act ? v : 0.0f);
-            if (lane == 0 && sum != 0.0f) atomicAdd(gbias + col, sum);
-        }
+    };
+    // the bias gradient of column col: the warp's sum, one atomic
+    auto sum_col = [&](int col, float v) {
+        const float sum = warp_sum(act ? v : 0.0f);
+        if (lane == 0 && sum != 0.0f) atomicAdd(gbias + col, sum);
     };
     float g[NP];
     {
@@ -587,27 +644,56 @@ __global__ void __launch_bounds__(32 * kMaxLayers) head_grad_kernel(
     __syncthreads();
     const float fs = s_f[lane];
 #pragma unroll
-    for (int i = 0; i < NP; ++i) emit(li * NP + i, g[i] * fs);
+    for (int i = 0; i < NP; ++i) {
+        g[i] *= fs;
+        store_col(li * NP + i, g[i]);
+    }
+    if (gbias) {
+        // the layer's first 32 columns by a transpose-reduce (after the five
+        // halving steps lane l holds the warp's sum of column l; 31 shuffles
+        // and one atomic instruction instead of 32 warp sums), the rest by
+        // warp sums
+        float v[32];
+#pragma unroll
+        for (int k = 0; k < 32; ++k) v[k] = (act && k < NP) ? g[k < NP ? k : 0] : 0.0f;
+#pragma unroll
+        for (int o = 16; o >= 1; o >>= 1) {
+            const bool upper = (lane & o) != 0;
+#pragma unroll
+            for (int k = 0; k < o; ++k) {
+                const float send = upper ? v[k] : v[k + o];
+                const float keep = upper ? v[k + o] : v[k];
+                v[k] = keep + __shfl_xor_sync(0xffffffffu, send, o);
+            }
+        }
+        if (lane < NP && v[0] != 0.0f) atomicAdd(gbias + li * NP + lane, v[0]);
+#pragma unroll
+        for (int i = 32; i < NP; ++i) sum_col(li * NP + i, g[i]);
+    }
     if (warp == 0) {
-        emit(o_shift, s_s[lane * 4 + 1] * fs);
-        emit(o_scale, s_s[lane * 4 + 2] * fs);
-        emit(o_le, s_s[lane * 4 + 3] * fs);
+        const float tail[3] = {s_s[lane * 4 + 1] * fs, s_s[lane * 4 + 2] * fs, s_s[lane * 4 + 3] * fs};
+#pragma unroll
+        for (int e = 0; e < 3; ++e) {
+            store_col(o_shift + e, tail[e]);
+            if (gbias) sum_col(o_shift + e, tail[e]);
+        }
         if (act)
             for (int col = o_le + 1; col < ldp; ++col) {
-                s_dp[lane * ldp + col] = 0;
+                s_dp[lane * lds + col] = 0;
                 dpt[static_cast<size_t>(col) * B + b] = __float2bfloat16(0.0f);
                 if (gf) gf[static_cast<size_t>(b) * ldp + col] = 0.0f;
             }
     }
     __syncthreads();
-    // the block's rows of dp: 32 rows of ldp BF16 values, 16 bytes at a time
-    const int per_row = ldp / 8;
-    for (int i = threadIdx.x; i < 32 * per_row; i += blockDim.x) {
-        const int r = i / per_row, c = i % per_row;
+    // the block's rows of dp: 32 rows of ldp BF16 values, 4 bytes at a time
+    // (warp w rows w, w + L, ...; lane c words c, c + 32, ...)
+    for (int r = warp; r < 32; r += L) {
         const int rb = blockIdx.x * 32 + r;
-        if (rb < B)
-            reinterpret_cast<uint4*>(dp + static_cast<size_t>(rb) * ldp)[c] =
-                reinterpret_cast<const uint4*>(s_dp + r * ldp)[c];
+        if (rb >= B) break;
+        uint32_t* dst = reinterpret_cast<uint32_t*>(dp + static_cast<size_t>(rb) * ldp);
+        const uint32_t* src = reinterpret_cast<const uint32_t*>(s_dp + r * lds);
+#pragma unroll 3
+        for (int c = lane; c < ldp / 2; c += 32) dst[c] = src[c];
     }
 }
 
@@ -633,13 +719,15 @@ struct ParamBlocks {
 // Adam (Flux's: bias-corrected moments) over the whole flat FP32 vector in
 // one launch; refreshes the BF16 weight copies and their transposes.  The
 // step size and the step count are read from device memory, so a captured
-// training step replays with the current values.
+// training step replays with the current values.  step_dev[0] is the step
+// count, step_dev[1] the blocks finished: the last block to finish counts
+// the step, after every block has read the count.
 __global__ void adam_kernel(float* __restrict__ w, float* __restrict__ m, float* __restrict__ v,
                             const float* __restrict__ g, const ParamBlocks pb, const float* __restrict__ lr_dev,
-                            float b1, float b2, float eps, const int* __restrict__ step_dev,
+                            float b1, float b2, float eps, int* __restrict__ step_dev,
                             const int* __restrict__ skip) {
-    if (*skip) return;  // a non-finite gradient: the step is skipped
-    const float t = static_cast<float>(*step_dev + 1);
+    if (*skip) return;  // a non-finite gradient: the step is skipped (and not counted)
+    const float t = static_cast<float>(*reinterpret_cast<volatile int*>(step_dev) + 1);
     const float c1 = 1.0f - powf(b1, t), c2 = 1.0f - powf(b2, t);
     const float lr = *lr_dev;
     const long long total = pb.off[pb.n];
@@ -661,11 +749,14 @@ __global__ void adam_kernel(float* __restrict__ w, float* __restrict__ m, float*
             pb.wt[k][(j % pb.cols[k]) * pb.rows[k] + j / pb.cols[k]] = h;
         }
     }
-}
-
-// Counts the step Adam took (after adam_kernel, in stream order).
-__global__ void step_count_kernel(int* __restrict__ step_dev, const int* __restrict__ skip) {
-    if (!*skip) ++*step_dev;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        __threadfence();
+        if (atomicAdd(step_dev + 1, 1) == static_cast<int>(gridDim.x) - 1) {
+            step_dev[1] = 0;
+            atomicAdd(step_dev, 1);
+        }
+    }
 }
 
 __global__ void to_bf16_kernel(const float* __restrict__ w, int n, int cols, int rows,
@@ -972,7 +1063,7 @@ struct ntp_flow {
     int* gemm_err = nullptr;
     int* skip = nullptr;     // set when a step's gradient is not finite
     long long skipped = 0;   // steps skipped for that reason
-    int* step_dev = nullptr;  // Adam's step count on the device
+    int* step_dev = nullptr;  // Adam's step count on the device, and its finished-block counter
     float* lr_dev = nullptr;  // Adam's step size on the device
     // the training step captured as a CUDA graph (per batch size and update flag)
     bool use_graph = true;
@@ -1097,7 +1188,7 @@ ntp_status pack(ntp_flow* f, const float* cond, int n_valid, int n, int on_devic
         F_CUDA(f, cudaMemcpyAsync(f->cond, cond, sizeof(float) * kCond * n_valid, cudaMemcpyHostToDevice, f->stream));
         dc = f->cond;
     }
-    ntp::pack_kernel<<<ntp::blocks_for(static_cast<long long>(n) * kIn), 256, 0, f->stream>>>(
+    ntp::pack_kernel<<<ntp::blocks_for(static_cast<long long>(n) * (kIn / 8)), 256, 0, f->stream>>>(
         dc, n_valid, n, f->in_mode, f->x, f->xt);
     F_CUDA(f, cudaGetLastError());
     return NTP_OK;
@@ -1168,22 +1259,12 @@ ntp_status record_step(ntp_flow* f, int B, bool update, bool rows_w) {
     auto gw = [&](int l) { return g + f->blk[2 * l].off; };
     auto gb = [&](int l) { return g + f->blk[2 * l + 1].off; };
     F_OK(launch_head(f, f->y, f->nh, f->hy, rows_w ? f->cw : nullptr, B, nullptr, gb(3)));
-    // The weight gradients dW_l = dZ_l^T X_l run on stream2 beside the chain
-    // of activation gradients dZ_{l-1} = (dZ_l W_l) * mask on the main stream;
-    // events order each dW_l after its dZ_l and join the two before Adam.
     cudaStream_t s2 = f->stream2;
-    F_CUDA(f, cudaEventRecord(f->ev[0], st));
-    F_CUDA(f, cudaStreamWaitEvent(s2, f->ev[0], 0));
-    ntp::GemmEpilogue ew{};  // output layer: dW4 = dP^T H3
-    ew.out_kind = 2;
-    ew.ldc = kHid;
-    ew.c = gw(3);
-    F_OK(gemm(f, f->dpt, B, f->ht[2], B, f->n_pad, kHid, B, ew, 0, s2));
     if (f->use_chain) {
         // dP -> dZ3 -> dZ2 -> dZ1 in one kernel per 128-row tile: each stage
         // masked by its layer's activations, its transpose and column sums
-        // (the bias gradient) to global memory; then the three weight
-        // gradients dW_l = dZ_l^T X_l on the second stream
+        // (the bias gradient) to global memory; then the four weight
+        // gradients dW_l = dZ_l^T X_l (dW4 = dP^T H3) in one grouped launch
         ntp::ChainSpec cs{};
         cs.n_stages = 3;
         cs.m = B;
@@ -1200,16 +1281,33 @@ ntp_status record_step(ntp_flow* f, int B, bool update, bool rows_w) {
         }
         const void* w[3] = {f->wt[3], f->wt[2], f->wt[1]};
         F_CUDA(f, ntp::layer_chain(f->dp, f->n_pad, w, cs, f->gemm_err, st));
-        F_CUDA(f, cudaEventRecord(f->ev[1], st));
-        F_CUDA(f, cudaStreamWaitEvent(s2, f->ev[1], 0));
-        for (int l = 2; l >= 0; --l) {
-            ntp::GemmEpilogue eg{};
-            eg.out_kind = 2;
-            eg.c = gw(l);
-            eg.ldc = l == 0 ? kIn : kHid;
-            const bf16* xt = l == 0 ? f->xt : f->ht[l - 1];
-            F_OK(gemm(f, f->dzt[l], B, xt, B, kHid, l == 0 ? kIn : kHid, B, eg, 0, l == 1 ? st : s2));
+        ntp::GemmProblem pr[4] = {};
+        for (int l = 3; l >= 0; --l) {
+            ntp::GemmProblem& q = pr[3 - l];
+            q.a = l == 3 ? f->dpt : f->dzt[l];
+            q.lda = B;
+            q.b = l == 0 ? f->xt : f->ht[l - 1];
+            q.ldb = B;
+            q.M = l == 3 ? f->n_pad : kHid;
+            q.N = l == 0 ? kIn : kHid;
+            q.K = B;
+            q.ep.out_kind = 2;
+            q.ep.c = gw(l);
+            q.ep.ldc = q.N;
         }
+        F_CUDA(f, ntp::gemm_bf16_group(pr, 4, f->gemm_err, st));
+    } else {
+        // The weight gradients dW_l = dZ_l^T X_l run on stream2 beside the
+        // chain of activation gradients dZ_{l-1} = (dZ_l W_l) * mask on the
+        // main stream; events order each dW_l after its dZ_l and join the
+        // two before Adam.
+        F_CUDA(f, cudaEventRecord(f->ev[0], st));
+        F_CUDA(f, cudaStreamWaitEvent(s2, f->ev[0], 0));
+        ntp::GemmEpilogue ew{};  // output layer: dW4 = dP^T H3
+        ew.out_kind = 2;
+        ew.ldc = kHid;
+        ew.c = gw(3);
+        F_OK(gemm(f, f->dpt, B, f->ht[2], B, f->n_pad, kHid, B, ew, 0, s2));
     }
     const bf16* dnext = f->dp;
     int k_next = f->n_pad;
@@ -1238,8 +1336,10 @@ ntp_status record_step(ntp_flow* f, int B, bool update, bool rows_w) {
         dnext = f->dz[l];
         k_next = kHid;
     }
-    F_CUDA(f, cudaEventRecord(f->ev[4], s2));
-    F_CUDA(f, cudaStreamWaitEvent(st, f->ev[4], 0));
+    if (!f->use_chain) {
+        F_CUDA(f, cudaEventRecord(f->ev[4], s2));
+        F_CUDA(f, cudaStreamWaitEvent(st, f->ev[4], 0));
+    }
     if (update) {
         ntp::ParamBlocks pb{};
         pb.n = 8;
@@ -1256,7 +1356,6 @@ ntp_status record_step(ntp_flow* f, int B, bool update, bool rows_w) {
         ntp::nonfinite_kernel<<<grid, 256, 0, st>>>(g, static_cast<long long>(f->n_params), f->skip);
         ntp::adam_kernel<<<grid, 256, 0, st>>>(f->theta, f->m, f->v, g, pb, f->lr_dev, f->b1, f->b2, f->eps,
                                                f->step_dev, f->skip);
-        ntp::step_count_kernel<<<1, 1, 0, st>>>(f->step_dev, f->skip);
         F_CUDA(f, cudaGetLastError());
     }
     return NTP_OK;
@@ -1352,7 +1451,7 @@ ntp_status ntp_flow_create(int32_t device, const ntp_flow_config* cfg, ntp_flow*
     if ((e = dalloc(&f->dp, B * np)) || (e = dalloc(&f->dpt, B * np)) || (e = dalloc(&f->P, B * np)) ||
         (e = dalloc(&f->cond, B * kCond)) || (e = dalloc(&f->y, B)) || (e = dalloc(&f->nh, B)) ||
         (e = dalloc(&f->hy, B)) || (e = dalloc(&f->cw, B)) || (e = dalloc(&f->loss, 1)) || (e = dalloc(&f->gemm_err, 1)) ||
-        (e = dalloc(&f->skip, 1)) || (e = dalloc(&f->step_dev, 1)) || (e = dalloc(&f->lr_dev, 1)))
+        (e = dalloc(&f->skip, 1)) || (e = dalloc(&f->step_dev, 2)) || (e = dalloc(&f->lr_dev, 1)))
         return fail(e);
     // He-uniform weights (seeded); zero biases, zero padding input columns of
     // W1 and zero padding rows of W4; the output layer scaled by 0.1
@@ -1418,7 +1517,7 @@ ntp_status ntp_flow_set_params(ntp_flow* f, const float* host, uint64_t n) {
     F_CUDA(f, cudaMemsetAsync(f->m, 0, sizeof(float) * n, f->stream));
     F_CUDA(f, cudaMemsetAsync(f->v, 0, sizeof(float) * n, f->stream));
     F_CUDA(f, cudaMemsetAsync(f->grad, 0, sizeof(float) * n, f->stream));
-    F_CUDA(f, cudaMemsetAsync(f->step_dev, 0, sizeof(int), f->stream));
+    F_CUDA(f, cudaMemsetAsync(f->step_dev, 0, 2 * sizeof(int), f->stream));
     F_CUDA(f, cudaMemcpyAsync(f->lr_dev, &f->lr, sizeof(float), cudaMemcpyHostToDevice, f->stream));
     F_CUDA(f, cudaStreamSynchronize(f->stream));
     f->step = 0;

@@ -69,19 +69,18 @@ struct Smem {
     uint32_t tmem;
 };
 
-// out_kind: 0 = FP32 store, 1 = BF16 store, 2 = FP32 atomic add (split-K)
+// One 128 x BN output tile over K slices [kt0, kt1) (the whole CTA).
+// out_kind: 0 = FP32 store, 1 = BF16 store, 2 = FP32 atomic add (split-K);
+// the bias is added by the first K split only (first_split).
 template <int BN>
-__global__ void __launch_bounds__(kThreads, 1)
-    gemm_bf16_kernel(const __grid_constant__ CUtensorMap map_a, const __grid_constant__ CUtensorMap map_b, int M,
-                     int N, int k_tiles_per_split, int k_tiles_total, const GemmEpilogue ep, int vec_ok,
-                     int* __restrict__ error, unsigned long long wait_ns, int withhold_first) {
+__device__ __forceinline__ void gemm_tile(const CUtensorMap& map_a, const CUtensorMap& map_b, int M, int N, int m0,
+                                          int n0, int kt0, int kt1, bool first_split, const GemmEpilogue& ep,
+                                          int vec_ok, int* __restrict__ error, unsigned long long wait_ns,
+                                          int withhold_first) {
     extern __shared__ unsigned char smem_raw[];
     Smem<BN>* s = reinterpret_cast<Smem<BN>*>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
     constexpr int kStages = Smem<BN>::kStages;
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    const int m0 = blockIdx.x * kBM, n0 = blockIdx.y * BN;
-    const int kt0 = blockIdx.z * k_tiles_per_split;
-    const int kt1 = min(kt0 + k_tiles_per_split, k_tiles_total);
     constexpr uint32_t kCols = BN <= 32 ? 32 : (BN <= 64 ? 64 : (BN <= 128 ? 128 : 256));
 
     if (warp == 0) {
@@ -181,7 +180,7 @@ __global__ void __launch_bounds__(kThreads, 1)
             float v[32];
             tmem_ld32(tmem + (static_cast<uint32_t>(warp * 32) << 16) + static_cast<uint32_t>(c0), v);
             const bool full = colb + 32 <= N;
-            if (ep.bias && blockIdx.z == 0) {
+            if (ep.bias && first_split) {
 #pragma unroll
                 for (int j = 0; j < 32; ++j)
                     if (full || colb + j < N) v[j] += __ldg(ep.bias + colb + j);
@@ -279,6 +278,51 @@ __global__ void __launch_bounds__(kThreads, 1)
     asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
     __syncthreads();
     if (warp == 0) asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(kCols));
+}
+
+// C = A B^T: grid (tiles of M, tiles of N, K splits)
+template <int BN>
+__global__ void __launch_bounds__(kThreads, 1)
+    gemm_bf16_kernel(const __grid_constant__ CUtensorMap map_a, const __grid_constant__ CUtensorMap map_b, int M,
+                     int N, int k_tiles_per_split, int k_tiles_total, const GemmEpilogue ep, int vec_ok,
+                     int* __restrict__ error, unsigned long long wait_ns, int withhold_first) {
+    const int kt0 = blockIdx.z * k_tiles_per_split;
+    gemm_tile<BN>(map_a, map_b, M, N, blockIdx.x * kBM, blockIdx.y * BN, kt0,
+                  min(kt0 + k_tiles_per_split, k_tiles_total), blockIdx.z == 0, ep, vec_ok, error, wait_ns,
+                  withhold_first);
+}
+
+// Several independent products in one launch: CTA b belongs to problem p
+// with cta_begin[p] <= b < cta_begin[p + 1], which it splits into (K split,
+// N tile, M tile) with the M tile fastest.
+struct GroupMaps {
+    CUtensorMap a[kMaxGemmGroup];
+    CUtensorMap b[kMaxGemmGroup];
+};
+struct GroupDesc {
+    int n;
+    int cta_begin[kMaxGemmGroup + 1];
+    int tiles_m[kMaxGemmGroup], tiles_n[kMaxGemmGroup];
+    int per[kMaxGemmGroup], k_tiles[kMaxGemmGroup];
+    int M[kMaxGemmGroup], N[kMaxGemmGroup];
+    int vec_ok[kMaxGemmGroup];
+    GemmEpilogue ep[kMaxGemmGroup];
+};
+
+template <int BN>
+__global__ void __launch_bounds__(kThreads, 1)
+    gemm_group_kernel(const __grid_constant__ GroupMaps maps, const __grid_constant__ GroupDesc g,
+                      int* __restrict__ error, unsigned long long wait_ns, int withhold_first) {
+    const int cta = static_cast<int>(blockIdx.x);
+    int p = 0;
+    while (p + 1 < g.n && cta >= g.cta_begin[p + 1]) ++p;
+    const int local = cta - g.cta_begin[p];
+    const int tiles = g.tiles_m[p] * g.tiles_n[p];
+    const int split = local / tiles, t = local % tiles;
+    const int kt0 = split * g.per[p];
+    gemm_tile<BN>(maps.a[p], maps.b[p], g.M[p], g.N[p], (t % g.tiles_m[p]) * kBM, (t / g.tiles_m[p]) * BN, kt0,
+                  min(kt0 + g.per[p], g.k_tiles[p]), split == 0, g.ep[p], g.vec_ok[p], error, wait_ns,
+                  withhold_first);
 }
 
 using EncodeTiled = CUresult (*)(CUtensorMap*, CUtensorMapDataType, cuuint32_t, void*, const cuuint64_t*,
@@ -447,8 +491,87 @@ cudaError_t gemm_bf16_ep(const void* A, int lda, const void* B, int ldb, int M, 
     return launch_bn<256>(ma, mb, M, N, splits, k_tiles, ep, vec_ok, error, st);
 }
 
+cudaError_t configure_group() {
+    static std::atomic<unsigned long long> configured{0};  // one bit per device
+    int dev = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e != cudaSuccess) return e;
+    const unsigned long long bit = 1ull << (dev & 63);
+    if (!(configured.load() & bit)) {
+        e = cudaFuncSetAttribute(gemm_group_kernel<64>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 static_cast<int>(sizeof(Smem<64>) + 1024));
+        if (e != cudaSuccess) return e;
+        configured.fetch_or(bit);
+    }
+    return cudaSuccess;
+}
+
+// Up to kMaxGemmGroup independent products C_p = A_p B_p^T in one launch
+// (64-column tiles); each problem is split along K so that the launch has
+// about two CTAs per SM, which needs the atomic FP32 output (out_kind 2)
+// wherever a split happens.  Shapes and alignment as in gemm_bf16_ep.
+cudaError_t gemm_bf16_group(const GemmProblem* pr, int n, int* error, cudaStream_t st) {
+    if (n < 1 || n > kMaxGemmGroup) return cudaErrorInvalidValue;
+    long long tiles_total = 0;
+    for (int p = 0; p < n; ++p) {
+        const GemmProblem& q = pr[p];
+        if (q.M <= 0 || q.N <= 0 || q.K <= 0 || q.K % kBK || q.lda % 8 || q.ldb % 8 ||
+            (reinterpret_cast<uintptr_t>(q.a) & 15) || (reinterpret_cast<uintptr_t>(q.b) & 15))
+            return cudaErrorInvalidValue;
+        tiles_total += static_cast<long long>((q.M + kBM - 1) / kBM) * ((q.N + 63) / 64);
+    }
+    cudaError_t e = configure_group();
+    if (e != cudaSuccess) return e;
+    GroupMaps maps;
+    GroupDesc g{};
+    g.n = n;
+    const long long want = (2ll * sm_count() + tiles_total - 1) / tiles_total;
+    int cta = 0;
+    for (int p = 0; p < n; ++p) {
+        const GemmProblem& q = pr[p];
+        const int k_tiles = q.K / kBK;
+        const bool atomic_out = q.ep.out_kind == 2 && !q.ep.ct && !q.ep.mask && !q.ep.colsum && !q.ep.relu;
+        long long sp = atomic_out ? std::min<long long>(want, std::max(1, k_tiles / 4)) : 1;
+        sp = std::max<long long>(1, sp);
+        const int per = static_cast<int>((k_tiles + sp - 1) / sp);
+        const int splits = (k_tiles + per - 1) / per;
+        g.cta_begin[p] = cta;
+        g.tiles_m[p] = (q.M + kBM - 1) / kBM;
+        g.tiles_n[p] = (q.N + 63) / 64;
+        g.per[p] = per;
+        g.k_tiles[p] = k_tiles;
+        g.M[p] = q.M;
+        g.N[p] = q.N;
+        g.ep[p] = q.ep;
+        const size_t esz = q.ep.out_kind == 1 ? 2 : 4;
+        g.vec_ok[p] = !((q.ep.c && ((reinterpret_cast<uintptr_t>(q.ep.c) & 15) || (static_cast<size_t>(q.ep.ldc) * esz) % 16)) ||
+                        (q.ep.mask && ((reinterpret_cast<uintptr_t>(q.ep.mask) & 15) || q.ep.ldm % 8)));
+        if (!make_map(&maps.a[p], q.a, q.M, q.K, q.lda, kBM) || !make_map(&maps.b[p], q.b, q.N, q.K, q.ldb, 64))
+            return cudaErrorInvalidValue;
+        cta += g.tiles_m[p] * g.tiles_n[p] * splits;
+    }
+    g.cta_begin[n] = cta;
+    for (int p = n; p < kMaxGemmGroup; ++p) {
+        maps.a[p] = maps.a[0];
+        maps.b[p] = maps.b[0];
+    }
+    cudaLaunchConfig_t cfg{};
+    cfg.gridDim = dim3(cta);
+    cfg.blockDim = dim3(kThreads);
+    cfg.dynamicSmemBytes = sizeof(Smem<64>) + 1024;
+    cfg.stream = st;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+    attr[0].val.programmaticStreamSerializationAllowed = g_pdl.load();
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    return cudaLaunchKernelEx(&cfg, gemm_group_kernel<64>, maps, g, error, g_wait_limit_ns.load(),
+                              g_withhold_first.load());
+}
+
 cudaError_t gemm_prepare() {
-    cudaError_t e = configure_bn<64>();
+    cudaError_t e = configure_group();
+    if (e == cudaSuccess) e = configure_bn<64>();
     if (e == cudaSuccess) e = configure_bn<128>();
     if (e == cudaSuccess) e = configure_bn<256>();
     if (e == cudaSuccess) (void)sm_count();

@@ -224,6 +224,19 @@ cudaError_t gemm_bf16_ep(const void* A, int lda, const void* B, int ldb, int M, 
                          int splits, int* error, cudaStream_t st);
 // Sets the GEMM kernels' function attributes (before a stream capture).
 cudaError_t gemm_prepare();
+// Independent products C_p = A_p B_p^T (each as in gemm_bf16_ep) in one
+// launch, split along K to about two CTAs per SM where the epilogue is the
+// atomic FP32 output alone (flow_gemm.cu).
+constexpr int kMaxGemmGroup = 4;
+struct GemmProblem {
+    const void* a;
+    int lda;
+    const void* b;
+    int ldb;
+    int M, N, K;
+    GemmEpilogue ep;
+};
+cudaError_t gemm_bf16_group(const GemmProblem* problems, int n, int* error, cudaStream_t st);
 
 // C = A * B^T, BF16 operands (K-major), FP32 accumulation on the tensor cores
 // (flow_gemm.cu).  out_kind: 0 = FP32, 1 = BF16, 2 = FP32 atomic add.
