@@ -1137,6 +1137,7 @@ ntp_status forward(ntp_flow* f, int n, bool keep_transposed) {
         ntp::ChainSpec cs{};
         cs.n_stages = 4;
         cs.m = n;
+        cs.weights_ready = 1;  // written by Adam or a parameter upload, before the pack kernel
         for (int l = 0; l < 3; ++l) {
             ntp::ChainStage& s = cs.st[l];
             s.n = kHid;
@@ -1268,6 +1269,7 @@ ntp_status record_step(ntp_flow* f, int B, bool update, bool rows_w) {
         ntp::ChainSpec cs{};
         cs.n_stages = 3;
         cs.m = B;
+        cs.weights_ready = 1;  // written by Adam or a parameter upload, before this step's kernels
         for (int i = 0; i < 3; ++i) {
             const int l = 2 - i;
             ntp::ChainStage& s = cs.st[i];

@@ -133,6 +133,16 @@ __device__ __forceinline__ bool mbar_wait_cluster(uint64_t* bar, uint32_t parity
     }
 }
 
+// 2-D TMA load delivered to the same shared-memory offset (data and
+// mbarrier) of every CTA of the pair
+__device__ __forceinline__ void tma_load_2d_pair(void* dst, const CUtensorMap* map, uint64_t* bar, int x, int y) {
+    asm volatile(
+        "cp.async.bulk.tensor.2d.shared::cluster.global.mbarrier::complete_tx::bytes.multicast::cluster"
+        " [%0], [%1, {%3, %4}], [%2], %5;" ::"r"(smem_u32(dst)),
+        "l"(reinterpret_cast<uint64_t>(map)), "r"(smem_u32(bar)), "r"(x), "r"(y), "h"(static_cast<uint16_t>(3))
+        : "memory");
+}
+
 __device__ __forceinline__ void cluster_sync_all() {
     asm volatile("barrier.cluster.arrive.release.aligned;" ::: "memory");
     asm volatile("barrier.cluster.wait.acquire.aligned;" ::: "memory");
@@ -188,9 +198,6 @@ __global__ void __launch_bounds__(kThreads, 1)
     cluster_sync_all();
     asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
     const uint32_t tmem = s->tmem;
-    // programmatic dependent launch: inputs, weights and biases are read only
-    // after the previous kernel of the stream has completed
-    asm volatile("griddepcontrol.wait;" ::: "memory");
 
     // the K slices of all stages in one sequence g = 0 .. total-1
     int first[kMaxChainStages + 1];
@@ -216,16 +223,27 @@ __global__ void __launch_bounds__(kThreads, 1)
         ++issued[r];
         next_load = g + 1;
     };
+    // the first weight slices, before the wait for the previous kernel when
+    // the caller says they were written before it started
+    if (threadIdx.x == 0 && spec.weights_ready)
+        for (int g = 0; g < kRing && g < total; ++g) load_slice(g);
+    // programmatic dependent launch: inputs (and otherwise the weights) and
+    // biases are read only after the previous kernel of the stream has
+    // completed
+    asm volatile("griddepcontrol.wait;" ::: "memory");
     if (threadIdx.x == 0) {
         const int ka = spec.st[0].k / kBK;
-        // failure-detection test: the input tile is not loaded, so its
-        // barrier is a flag that nothing completes and the first wait runs out
-        if (!withhold_first) {
-            mbar_expect_tx(&s->a_full, static_cast<uint32_t>(ka) * kRows * kBK * sizeof(__nv_bfloat16));
-            for (int j = 0; j < ka; ++j) tma_load_2d(s->act[0][j], &maps.a, &s->a_full, j * kBK, m0);
-            a_pending = true;
-        }
-        for (int g = 0; g < kRing && g < total; ++g) load_slice(g);
+        // the pair's input tile: each CTA loads every other 64-column slice
+        // into both CTAs (multicast); each CTA's barrier expects all of it.
+        // Failure-detection test: this CTA's slices are not loaded, so its
+        // barrier (and the partner's) never completes and the first wait
+        // runs out
+        mbar_expect_tx(&s->a_full, static_cast<uint32_t>(ka) * kRows * kBK * sizeof(__nv_bfloat16));
+        a_pending = true;
+        if (!withhold_first)
+            for (int j = static_cast<int>(q); j < ka; j += 2) tma_load_2d_pair(s->act[0][j], &maps.a, &s->a_full, j * kBK, m0);
+        if (!spec.weights_ready)
+            for (int g = 0; g < kRing && g < total; ++g) load_slice(g);
     }
     for (int st = 0; st < S; ++st) {
         const int nq = spec.st[st].n / 2;
@@ -324,6 +342,15 @@ __global__ void __launch_bounds__(kThreads, 1)
         // after each, thread 0 sends the pass's activation slice to the
         // partner and stores the pass's row-major and transposed tiles
         const int ql = static_cast<int>(q) * nq;  // first column of this CTA's half
+        // both passes' accumulator columns loaded at once, one wait
+        uint32_t acc[2][32];
+        if (have) {
+            const uint32_t lanes = static_cast<uint32_t>(quad * 32) << 16;
+            tmem_ld32_async(tmem + lanes + static_cast<uint32_t>(32 * half), acc[0]);
+            if (32 * half + 64 < nq) tmem_ld32_async(tmem + lanes + static_cast<uint32_t>(32 * half + 64), acc[1]);
+            tmem_wait_ld(acc[0]);
+            tmem_regs_ready(acc[1]);
+        }
 #pragma unroll
         for (int i = 0; i < 2; ++i) {
             const int c0 = 32 * half + 64 * i;  // column within this CTA's half
@@ -331,7 +358,8 @@ __global__ void __launch_bounds__(kThreads, 1)
             if (have && c0 < nq) {
                 const int col = ql + c0;
                 float v[32];
-                tmem_ld32(tmem + (static_cast<uint32_t>(quad * 32) << 16) + static_cast<uint32_t>(c0), v);
+#pragma unroll
+                for (int j = 0; j < 32; ++j) v[j] = __uint_as_float(acc[i][j]);
                 if (cs.bias) {
 #pragma unroll
                     for (int j = 0; j < 32; ++j) v[j] += s->bias[st][c0 + j];

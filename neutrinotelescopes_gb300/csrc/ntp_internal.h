@@ -267,6 +267,10 @@ struct ChainStage {
 struct ChainSpec {
     int n_stages;
     int m;  // rows
+    // nonzero: the weights were written before the previous kernel of the
+    // stream started, so the first slices may be loaded before the wait for
+    // that kernel (programmatic dependent launch)
+    int weights_ready;
     ChainStage st[kMaxChainStages];
 };
 cudaError_t layer_chain(const void* a, int lda, const void* const* w, const ChainSpec& spec, int* error,
