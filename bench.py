@@ -394,21 +394,18 @@ def train_hybrid_models(tab, seed: int, shape_steps: int, count_steps: int, coun
     ensemble of count_members conditioners with derived input columns, each
     trained on the table's (simulation, orientation, PMT) groups alone,
     information-weighted, from its own initialisation and shuffle.  Cosine
-    learning-rate schedules from 1e-3 to 1e-5."""
+    learning-rate schedules from 1e-3 to 1e-5.  The arrival-time flow starts
+    from two initialisations and keeps, after ten epochs, the one with the
+    lower NLL on held-out rows of the table."""
     from neutrinotelescopes_gb300.flow import CountEnsemble, RQNormFlow, RQNormFlowHParams
     t0 = time.perf_counter()
-    # the batch capacity also sets the chunk of conditions an inference pass
-    # takes at once: the hybrid evaluates millions of PMT conditions per batch
-    fl = RQNormFlow(RQNormFlowHParams(batch_size=8192, seed=31338 + 101 * seed), batch_capacity=131072)
-    fl.init_from_table(tab)
     per = len(tab) // 8192
     sched = _cosine(1e-3, 1e-5, shape_steps)
-    # the time density's NLL on a fixed sample of timed rows after every
-    # epoch; the parameters of the best epoch are kept, so that a run that
-    # degrades late does not end in its degraded state (two of about
-    # fourteen runs of this configuration ended with event KS medians of
-    # 0.04-0.5 against the usual 0.012; the training is not bit-reproducible:
-    # the weight gradients are summed with floating-point atomics)
+    # the time density's NLL on a fixed sample of timed rows (count term
+    # off) after every epoch; the parameters of the best epoch are kept, so
+    # that a run that degrades late does not end in its degraded state (the
+    # training is not bit-reproducible: the weight gradients are summed with
+    # floating-point atomics)
     import numpy as np
     import torch
     gen = torch.Generator(device=tab.tres.device)
@@ -416,19 +413,50 @@ def train_hybrid_models(tab, seed: int, shape_steps: int, count_steps: int, coun
     timed = torch.nonzero(tab.has_time, as_tuple=True)[0]
     vi = timed[torch.randperm(timed.numel(), device=timed.device, generator=gen)[:32768]]
     vc, vt, vh = tab.cond[vi].contiguous(), tab.tres[vi].contiguous(), tab.has_time[vi].contiguous()
-    vn, vw = torch.zeros_like(vt), torch.zeros_like(vt)  # count term off: the time NLL alone
-    best_nll, best_theta, nll_per_epoch = math.inf, None, []
-    done, ep = 0, 0
+    vn, vw = torch.zeros_like(vt), torch.zeros_like(vt)
+
+    def val_nll(f):
+        return float(np.mean(f.train_steps(vc, vt, vn, vh, 8192, 4, count_weight=vw, update=False)))
+
+    def train_epoch(f, done, ep):
+        f.set_lr(sched(done))
+        return done + len(f.fit_table(tab, epochs=1, seed=1000 * seed + ep, max_steps=min(per, shape_steps - done),
+                                      count_mode="information"))
+
+    # two initialisations for the first probe_epochs epochs; the one with the
+    # lower validation NLL goes on (the quality of a run is mostly set by its
+    # start: a run that ends 0.15 nats worse is already behind after ten
+    # epochs)
+    probe_epochs = 10
+    cands = []
+    for c in range(2):
+        # the batch capacity also sets the chunk of conditions an inference
+        # pass takes at once: the hybrid evaluates millions of PMT conditions
+        # per batch
+        f = RQNormFlow(RQNormFlowHParams(batch_size=8192, seed=31338 + 101 * seed + 7919 * c), batch_capacity=131072)
+        f.init_from_table(tab)
+        done, hist = 0, []
+        for ep in range(probe_epochs):
+            if done >= shape_steps:
+                break
+            done = train_epoch(f, done, ep)
+            hist.append(val_nll(f))
+        cands.append((min(hist), f, done, hist))
+    cands.sort(key=lambda x: x[0])
+    for _, f, _, _ in cands[1:]:
+        f.close()
+    _, fl, done, nll_per_epoch = cands[0]
+    probe_nll = [round(min(c[3]), 5) for c in cands]
+    best_nll, best_theta = nll_per_epoch[-1], fl.get_params()
+    ep = best_ep = len(nll_per_epoch)
     while done < shape_steps:
-        fl.set_lr(sched(done))
-        done += len(fl.fit_table(tab, epochs=1, seed=1000 * seed + ep, max_steps=min(per, shape_steps - done),
-                                 count_mode="information"))
+        done = train_epoch(fl, done, ep)
         ep += 1
-        nll = float(np.mean(fl.train_steps(vc, vt, vn, vh, 8192, 4, count_weight=vw, update=False)))
+        nll = val_nll(fl)
         nll_per_epoch.append(nll)
         if nll < best_nll:
-            best_nll, best_theta = nll, fl.get_params()
-    if best_theta is not None and best_nll < nll_per_epoch[-1]:
+            best_nll, best_theta, best_ep = nll, fl.get_params(), ep
+    if best_nll < nll_per_epoch[-1]:
         fl.set_params(best_theta)
     t_shape = time.perf_counter() - t0
     t0 = time.perf_counter()
@@ -442,8 +470,9 @@ def train_hybrid_models(tab, seed: int, shape_steps: int, count_steps: int, coun
         cf.fit_counts(tab, steps=count_steps, seed=100 * seed + j, lr_schedule=_cosine(1e-3, 1e-5, count_steps))
         members.append(cf)
     return fl, CountEnsemble(members), {"seed": seed, "shape_steps": shape_steps, "shape_seconds": t_shape,
+                                        "probe_epochs": probe_epochs, "probe_best_nll": probe_nll,
                                         "time_nll_last": nll_per_epoch[-1], "time_nll_best": best_nll,
-                                        "best_epoch": int(np.argmin(nll_per_epoch)) + 1, "epochs": ep,
+                                        "best_epoch": best_ep, "epochs": ep,
                                         "time_nll_per_epoch": [round(x, 5) for x in nll_per_epoch],
                                         "count_members": count_members, "count_steps_per_member": count_steps,
                                         "count_seconds": time.perf_counter() - t0}
