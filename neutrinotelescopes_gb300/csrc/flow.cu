@@ -41,6 +41,7 @@
 
 #include "ntp_device.cuh"
 #include "ntp_internal.h"
+#include "tc_ptx.cuh"
 
 namespace ntp {
 
@@ -362,6 +363,9 @@ __device__ __forceinline__ float input_column(const float* __restrict__ f, int j
 // contiguous, the row stores one 16-byte vector each.
 __global__ void pack_kernel(const float* __restrict__ cond, int n_valid, int n, int mode,
                             __nv_bfloat16* __restrict__ x, __nv_bfloat16* __restrict__ xt) {
+    // programmatic dependent launch: reads follow the previous kernel
+    asm volatile("griddepcontrol.wait;" ::: "memory");
+    asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n * (kIn / 8)) return;
     const int b = i % n, g = i / n;
@@ -421,6 +425,10 @@ __global__ void __launch_bounds__(32 * kMaxLayers) head_grad_kernel(
     __nv_bfloat16* __restrict__ dpt, float* __restrict__ gf, float* __restrict__ gbias, double* __restrict__ loss) {
     constexpr int NP = 3 * K + 1, NK = K + 1, KN = 3 * NK + 2 * K + NK;
     extern __shared__ float sm[];
+    // programmatic dependent launch: reads follow the previous kernel; the
+    // next kernel's blocks may take SMs as this kernel's blocks finish
+    asm volatile("griddepcontrol.wait;" ::: "memory");
+    asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const int S = L * 32;
     float* s_kn = sm;                          // [L][32][KN]
@@ -699,6 +707,8 @@ __global__ void __launch_bounds__(32 * kMaxLayers) head_grad_kernel(
 
 // Sets *flag if any of the n gradient values is not finite.
 __global__ void nonfinite_kernel(const float* __restrict__ g, long long n, int* __restrict__ flag) {
+    asm volatile("griddepcontrol.wait;" ::: "memory");
+    asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
     bool bad = false;
     for (long long i = blockIdx.x * static_cast<long long>(blockDim.x) + threadIdx.x; i < n;
          i += static_cast<long long>(gridDim.x) * blockDim.x)
@@ -726,6 +736,8 @@ __global__ void adam_kernel(float* __restrict__ w, float* __restrict__ m, float*
                             const float* __restrict__ g, const ParamBlocks pb, const float* __restrict__ lr_dev,
                             float b1, float b2, float eps, int* __restrict__ step_dev,
                             const int* __restrict__ skip) {
+    asm volatile("griddepcontrol.wait;" ::: "memory");
+    asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
     if (*skip) return;  // a non-finite gradient: the step is skipped (and not counted)
     const float t = static_cast<float>(*reinterpret_cast<volatile int*>(step_dev) + 1);
     const float c1 = 1.0f - powf(b1, t), c2 = 1.0f - powf(b2, t);
@@ -757,6 +769,47 @@ __global__ void adam_kernel(float* __restrict__ w, float* __restrict__ m, float*
             atomicAdd(step_dev, 1);
         }
     }
+}
+
+// The batch sources of a multi-step call whose rows are on the device, read
+// by the step's kernels from device memory so that one captured step serves
+// every batch: step i reads rows [i B, (i + 1) B); the step's last kernel
+// records its loss and skip flag and advances i.
+struct StepIO {
+    const float* cond;
+    const float* tres;
+    const float* nhits;
+    const int* has_time;
+    const float* count_w;  // may be null
+    double* loss_hist;
+    int* skip_hist;
+    int step;
+};
+
+// the step's rows into the staging buffers the step's kernels read
+__global__ void stage_kernel(const StepIO* __restrict__ io, int B, float* __restrict__ cond, float* __restrict__ y,
+                             float* __restrict__ nh, int* __restrict__ hy, float* __restrict__ cw) {
+    asm volatile("griddepcontrol.wait;" ::: "memory");
+    asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
+    const long long o = static_cast<long long>(io->step) * B;
+    const int stride = gridDim.x * blockDim.x;
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < B * kCond; i += stride) cond[i] = io->cond[o * kCond + i];
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < B; i += stride) {
+        y[i] = io->tres[o + i];
+        nh[i] = io->nhits[o + i];
+        hy[i] = io->has_time[o + i];
+        if (io->count_w) cw[i] = io->count_w[o + i];
+    }
+}
+
+// the step's loss (and skip flag) into the call's history; the next step
+// reads the next rows
+__global__ void step_end_kernel(StepIO* __restrict__ io, const double* __restrict__ loss,
+                                const int* __restrict__ skip, int update) {
+    asm volatile("griddepcontrol.wait;" ::: "memory");
+    io->loss_hist[io->step] = *loss;
+    if (update) io->skip_hist[io->step] = *skip;
+    io->step += 1;
 }
 
 __global__ void to_bf16_kernel(const float* __restrict__ w, int n, int cols, int rows,
@@ -1062,6 +1115,7 @@ struct ntp_flow {
     double* loss = nullptr;
     int* gemm_err = nullptr;
     int* skip = nullptr;     // set when a step's gradient is not finite
+    ntp::StepIO* io = nullptr;  // the batch sources of a multi-step call on the device
     long long skipped = 0;   // steps skipped for that reason
     int* step_dev = nullptr;  // Adam's step count on the device, and its finished-block counter
     float* lr_dev = nullptr;  // Adam's step size on the device
@@ -1071,7 +1125,7 @@ struct ntp_flow {
     // gradients as one fused kernel each (NTP_FLOW_CHAIN=0: one GEMM per layer)
     bool use_chain = true;
     cudaGraphExec_t gexec = nullptr;
-    int g_B = 0, g_update = -1, g_rows_w = -1;
+    int g_B = 0, g_update = -1, g_rows_w = -1, g_dev = -1;
     // per-step losses and skip flags of a multi-step call (grown on demand)
     double* loss_hist = nullptr;
     int* skip_hist = nullptr;
@@ -1114,6 +1168,23 @@ template <typename Fn>
 void with_bins(int K, Fn&& fn) {
     if (K == 10) fn(std::integral_constant<int, 10>{});
     else fn(std::integral_constant<int, 12>{});
+}
+
+// Launch with programmatic stream serialisation (the kernel waits for the
+// previous kernel of the stream with griddepcontrol.wait before it reads)
+template <typename... Exp, typename... Act>
+cudaError_t launch_dep(void (*kernel)(Exp...), dim3 grid, dim3 block, size_t smem, cudaStream_t st, Act&&... args) {
+    cudaLaunchConfig_t cfg{};
+    cfg.gridDim = grid;
+    cfg.blockDim = block;
+    cfg.dynamicSmemBytes = smem;
+    cfg.stream = st;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+    attr[0].val.programmaticStreamSerializationAllowed = ntp::tc::pdl_enabled();
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    return cudaLaunchKernelEx(&cfg, kernel, std::forward<Act>(args)...);
 }
 
 template <typename T>
@@ -1189,9 +1260,8 @@ ntp_status pack(ntp_flow* f, const float* cond, int n_valid, int n, int on_devic
         F_CUDA(f, cudaMemcpyAsync(f->cond, cond, sizeof(float) * kCond * n_valid, cudaMemcpyHostToDevice, f->stream));
         dc = f->cond;
     }
-    ntp::pack_kernel<<<ntp::blocks_for(static_cast<long long>(n) * (kIn / 8)), 256, 0, f->stream>>>(
-        dc, n_valid, n, f->in_mode, f->x, f->xt);
-    F_CUDA(f, cudaGetLastError());
+    F_CUDA(f, launch_dep(ntp::pack_kernel, dim3(ntp::blocks_for(static_cast<long long>(n) * (kIn / 8))), dim3(256), 0,
+                         f->stream, dc, n_valid, n, f->in_mode, f->x, f->xt));
     return NTP_OK;
 }
 
@@ -1219,10 +1289,9 @@ ntp_status launch_head(ntp_flow* f, const float* y, const float* nh, const int* 
             e = cudaFuncSetAttribute(ntp::head_grad_kernel<K>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                      static_cast<int>(smem));
         if (e == cudaSuccess) {
-            ntp::head_grad_kernel<K><<<(B + 31) / 32, 32 * f->L, smem, f->stream>>>(
-                f->P, f->n_pad, f->L, y, nh, hy, B, f->r0, f->r1, f->clip, f->count_w, cwr, f->dp, f->dpt, gf, gbias,
-                f->loss);
-            e = cudaGetLastError();
+            e = launch_dep(ntp::head_grad_kernel<K>, dim3((B + 31) / 32), dim3(32 * f->L), smem, f->stream, f->P,
+                           f->n_pad, f->L, y, nh, hy, B, f->r0, f->r1, f->clip, f->count_w, cwr, f->dp, f->dpt, gf,
+                           gbias, f->loss);
         }
     });
     if (e != cudaSuccess) return ferr(f, e, "head kernel");
@@ -1231,7 +1300,7 @@ ntp_status launch_head(ntp_flow* f, const float* y, const float* nh, const int* 
 
 void free_all(ntp_flow* f) {
     void* ps[] = {f->theta, f->m, f->v, f->grad, f->x, f->xt, f->dp, f->dpt, f->P, f->cond, f->y, f->nh, f->hy,
-                  f->loss, f->gemm_err, f->skip, f->step_dev, f->lr_dev, f->knots, f->loss_hist, f->skip_hist, f->cw,
+                  f->loss, f->gemm_err, f->skip, f->io, f->step_dev, f->lr_dev, f->knots, f->loss_hist, f->skip_hist, f->cw,
                   f->samp};
     for (void* p : ps)
         if (p) cudaFree(p);
@@ -1249,13 +1318,21 @@ void free_all(ntp_flow* f) {
 
 // Every device operation of one training step on the staged batch (f->cond,
 // f->y, f->nh, f->hy): no host synchronisation, so it can be captured.
-ntp_status record_step(ntp_flow* f, int B, bool update, bool rows_w) {
+// (dev_io: the batch is staged from the sources in f->io by the step's
+// first kernel and the step's loss and skip flag recorded by its last; the
+// memsets come first, so that every kernel follows a kernel and takes the
+// programmatic dependent launch.)
+ntp_status record_step(ntp_flow* f, int B, bool update, bool rows_w, bool dev_io) {
     cudaStream_t st = f->stream;
     F_CUDA(f, cudaMemsetAsync(f->gemm_err, 0, sizeof(int), st));
-    F_OK(pack(f, f->cond, B, B, 1));
-    F_OK(forward(f, B, true));
     F_CUDA(f, cudaMemsetAsync(f->loss, 0, sizeof(double), st));
     F_CUDA(f, cudaMemsetAsync(f->grad, 0, sizeof(float) * f->n_params, st));
+    if (update) F_CUDA(f, cudaMemsetAsync(f->skip, 0, sizeof(int), st));
+    if (dev_io)
+        F_CUDA(f, launch_dep(ntp::stage_kernel, dim3(ntp::blocks_for(static_cast<long long>(B) * kCond)), dim3(256), 0,
+                             st, f->io, B, f->cond, f->y, f->nh, f->hy, f->cw));
+    F_OK(pack(f, f->cond, B, B, 1));
+    F_OK(forward(f, B, true));
     float* g = f->grad;
     auto gw = [&](int l) { return g + f->blk[2 * l].off; };
     auto gb = [&](int l) { return g + f->blk[2 * l + 1].off; };
@@ -1354,12 +1431,14 @@ ntp_status record_step(ntp_flow* f, int B, bool update, bool rows_w) {
         }
         pb.off[8] = static_cast<long long>(f->n_params);
         const int grid = static_cast<int>(std::min<size_t>((f->n_params + 255) / 256, 152 * 8));
-        F_CUDA(f, cudaMemsetAsync(f->skip, 0, sizeof(int), st));
-        ntp::nonfinite_kernel<<<grid, 256, 0, st>>>(g, static_cast<long long>(f->n_params), f->skip);
-        ntp::adam_kernel<<<grid, 256, 0, st>>>(f->theta, f->m, f->v, g, pb, f->lr_dev, f->b1, f->b2, f->eps,
-                                               f->step_dev, f->skip);
-        F_CUDA(f, cudaGetLastError());
+        F_CUDA(f, launch_dep(ntp::nonfinite_kernel, dim3(grid), dim3(256), 0, st, g, static_cast<long long>(f->n_params),
+                             f->skip));
+        F_CUDA(f, launch_dep(ntp::adam_kernel, dim3(grid), dim3(256), 0, st, f->theta, f->m, f->v, g, pb, f->lr_dev,
+                             f->b1, f->b2, f->eps, f->step_dev, f->skip));
     }
+    if (dev_io)
+        F_CUDA(f, launch_dep(ntp::step_end_kernel, dim3(1), dim3(1), 0, st, f->io, f->loss, f->skip,
+                             update ? 1 : 0));
     return NTP_OK;
 }
 
@@ -1453,7 +1532,7 @@ ntp_status ntp_flow_create(int32_t device, const ntp_flow_config* cfg, ntp_flow*
     if ((e = dalloc(&f->dp, B * np)) || (e = dalloc(&f->dpt, B * np)) || (e = dalloc(&f->P, B * np)) ||
         (e = dalloc(&f->cond, B * kCond)) || (e = dalloc(&f->y, B)) || (e = dalloc(&f->nh, B)) ||
         (e = dalloc(&f->hy, B)) || (e = dalloc(&f->cw, B)) || (e = dalloc(&f->loss, 1)) || (e = dalloc(&f->gemm_err, 1)) ||
-        (e = dalloc(&f->skip, 1)) || (e = dalloc(&f->step_dev, 2)) || (e = dalloc(&f->lr_dev, 1)))
+        (e = dalloc(&f->skip, 1)) || (e = dalloc(&f->io, 1)) || (e = dalloc(&f->step_dev, 2)) || (e = dalloc(&f->lr_dev, 1)))
         return fail(e);
     // He-uniform weights (seeded); zero biases, zero padding input columns of
     // W1 and zero padding rows of W4; the output layer scaled by 0.1
@@ -1574,23 +1653,32 @@ ntp_status ntp_flow_train_steps(ntp_flow* f, const float* cond, const float* tre
     double* d_loss = f->loss_hist;
     int* d_skip = f->skip_hist;
     const bool rows_w = count_weight != nullptr;
+    const bool dev_io = on_device != 0;
     F_CUDA(f, cudaMemsetAsync(d_skip, 0, sizeof(int) * n_steps, st));
-    const cudaMemcpyKind kind = on_device ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice;
+    if (dev_io) {
+        // the sources once; each step stages its own rows and records its loss
+        ntp::StepIO io{cond, tres, nhits, has_time, count_weight, d_loss, d_skip, 0};
+        F_CUDA(f, cudaMemcpyAsync(f->io, &io, sizeof(io), cudaMemcpyHostToDevice, st));
+    }
     for (int i = 0; i < n_steps; ++i) {
         const size_t o = static_cast<size_t>(i) * B;
-        // the batch into the staging buffers the step reads
-        F_CUDA(f, cudaMemcpyAsync(f->cond, cond + o * kCond, sizeof(float) * kCond * B, kind, st));
-        F_CUDA(f, cudaMemcpyAsync(f->y, tres + o, sizeof(float) * B, kind, st));
-        F_CUDA(f, cudaMemcpyAsync(f->nh, nhits + o, sizeof(float) * B, kind, st));
-        F_CUDA(f, cudaMemcpyAsync(f->hy, has_time + o, sizeof(int) * B, kind, st));
-        if (rows_w) F_CUDA(f, cudaMemcpyAsync(f->cw, count_weight + o, sizeof(float) * B, kind, st));
+        if (!dev_io) {
+            // the batch into the staging buffers the step reads
+            F_CUDA(f, cudaMemcpyAsync(f->cond, cond + o * kCond, sizeof(float) * kCond * B, cudaMemcpyHostToDevice, st));
+            F_CUDA(f, cudaMemcpyAsync(f->y, tres + o, sizeof(float) * B, cudaMemcpyHostToDevice, st));
+            F_CUDA(f, cudaMemcpyAsync(f->nh, nhits + o, sizeof(float) * B, cudaMemcpyHostToDevice, st));
+            F_CUDA(f, cudaMemcpyAsync(f->hy, has_time + o, sizeof(int) * B, cudaMemcpyHostToDevice, st));
+            if (rows_w)
+                F_CUDA(f, cudaMemcpyAsync(f->cw, count_weight + o, sizeof(float) * B, cudaMemcpyHostToDevice, st));
+        }
         if (f->use_graph) {
-            if (!f->gexec || f->g_B != B || f->g_update != update || f->g_rows_w != static_cast<int>(rows_w)) {
+            if (!f->gexec || f->g_B != B || f->g_update != update || f->g_rows_w != static_cast<int>(rows_w) ||
+                f->g_dev != static_cast<int>(dev_io)) {
                 if (f->gexec) cudaGraphExecDestroy(f->gexec);
                 f->gexec = nullptr;
                 F_CUDA(f, prepare_kernels(f));
                 F_CUDA(f, cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
-                const ntp_status rs = record_step(f, B, update != 0, rows_w);
+                const ntp_status rs = record_step(f, B, update != 0, rows_w, dev_io);
                 cudaGraph_t graph = nullptr;
                 const cudaError_t ec = cudaStreamEndCapture(st, &graph);
                 if (rs != NTP_OK || ec != cudaSuccess) {
@@ -1607,13 +1695,16 @@ ntp_status ntp_flow_train_steps(ntp_flow* f, const float* cond, const float* tre
                 f->g_B = B;
                 f->g_update = update;
                 f->g_rows_w = static_cast<int>(rows_w);
+                f->g_dev = static_cast<int>(dev_io);
             }
             F_CUDA(f, cudaGraphLaunch(f->gexec, st));
         } else {
-            F_OK(record_step(f, B, update != 0, rows_w));
+            F_OK(record_step(f, B, update != 0, rows_w, dev_io));
         }
-        F_CUDA(f, cudaMemcpyAsync(d_loss + i, f->loss, sizeof(double), cudaMemcpyDeviceToDevice, st));
-        if (update) F_CUDA(f, cudaMemcpyAsync(d_skip + i, f->skip, sizeof(int), cudaMemcpyDeviceToDevice, st));
+        if (!dev_io) {
+            F_CUDA(f, cudaMemcpyAsync(d_loss + i, f->loss, sizeof(double), cudaMemcpyDeviceToDevice, st));
+            if (update) F_CUDA(f, cudaMemcpyAsync(d_skip + i, f->skip, sizeof(int), cudaMemcpyDeviceToDevice, st));
+        }
     }
     std::vector<double> hl(n_steps);
     std::vector<int> hs(n_steps);
