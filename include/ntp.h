@@ -408,11 +408,15 @@ ntp_status ntp_gemm_bf16(const void* A, int32_t lda, const void* B, int32_t ldb,
  * wait_limit_ns of the GPU's global timer (0 = the default, 2 s), sets an
  * error word, lets its copies in flight land, frees its tensor memory and
  * returns; ntp_gemm_bf16 (and the flow calls built on it) then return
- * NTP_ERR_TIMEOUT and the context stays usable.  withhold_first_copy != 0
- * makes the following GEMM launches leave out the first pipeline stage's
- * copies, so that the first wait has nothing to complete and runs out: this
- * is how the timeout path is tested (outputs are undefined while it is set).
- * Process-wide; applies to launches made after the call. */
+ * NTP_ERR_TIMEOUT and the context stays usable.  The same limit and switch
+ * govern the flow's fused layer-chain kernel (its first wait is for its
+ * input tile) and the grouped weight-gradient GEMM.  withhold_first_copy != 0
+ * makes the following launches leave out the first pipeline stage's copies
+ * (the chain: its input tile), so that the first wait has nothing to
+ * complete and runs out: this is how the timeout path is tested (outputs are
+ * undefined while it is set).  Process-wide; applies to launches made after
+ * the call.  NTP_GEMM_PDL=0 in the environment turns off the programmatic
+ * dependent launch of these kernels and of the flow's other kernels. */
 ntp_status ntp_gemm_set_wait_limit(uint64_t wait_limit_ns, int32_t withhold_first_copy);
 
 /* --------------------------------------------------------- arrival-time flow
