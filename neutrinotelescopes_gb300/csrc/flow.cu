@@ -445,6 +445,14 @@ __global__ void __launch_bounds__(32 * kMaxLayers) head_grad_kernel(
     uint16_t* s_dp = reinterpret_cast<uint16_t*>(s_f + 32);
     const int ldsp = ldp + 1;
     float* s_p = reinterpret_cast<float*>(s_dp) + 16 * lds;  // [32][ldp + 1]
+    const int b = blockIdx.x * 32 + lane;
+    const bool act = b < B;
+    // the sample's inputs, loaded before the rows of P arrive (warp 0's
+    // chains use the time, the hit count and the count weight)
+    const bool timed = act && has_y[b];
+    const float y_b = (warp == 0 && timed) ? y[b] : 0.0f;
+    const float n_b = (warp == 0 && act) ? nhits[b] : 0.0f;
+    const float cwr_b = (warp == 0 && act && count_w_rows) ? count_w_rows[b] : 1.0f;
     // warp w copies rows w, w + L, ..., four rows at a time (all loads in
     // flight before the stores); lane c the row's 16-byte columns c, c + 32
     // (ldp <= 256: at most two per lane)
@@ -477,14 +485,12 @@ __global__ void __launch_bounds__(32 * kMaxLayers) head_grad_kernel(
         }
     }
     __syncthreads();
-    const int b = blockIdx.x * 32 + lane;
-    const bool act = b < B;
     const float* p = s_p + lane * ldsp;
     const int li = warp;
     const int slot = li * 32 + lane;
     const int o_shift = L * NP, o_scale = o_shift + 1, o_le = o_shift + 2;
     const float inv_b = 1.0f / static_cast<float>(B);
-    const bool timed = act && has_y[b];
+    float l_loss = 0.0f;  // warp 0: the sample's loss, summed at the end
 
     // P1
     {
@@ -508,14 +514,14 @@ __global__ void __launch_bounds__(32 * kMaxLayers) head_grad_kernel(
     // P2
     if (warp == 0) {
         float l = 0.0f;
-        const float le_raw = p[o_le], n = act ? nhits[b] : 0.0f;
+        const float le_raw = p[o_le], n = n_b;
         const float le = clamp_le(le_raw);
         const float lam = expf(le);
-        const float cw = act ? (count_w_rows ? count_w * count_w_rows[b] : count_w) : 0.0f;
+        const float cw = act ? (count_w_rows ? count_w * cwr_b : count_w) : 0.0f;
         if (act && cw != 0.0f) l -= cw * (n * le - lam - lgammaf(n + 1.0f));
         float a = 0.0f, g_shift = 0.0f, g_scale = 0.0f;
         if (timed) {
-            float cur = y[b], ldsum = 0.0f;
+            float cur = y_b, ldsum = 0.0f;
             for (int k = L - 1; k >= 0; --k) {
                 const float* q = s_kn + (k * 32 + lane) * KN;
                 s_y[k * 32 + lane] = cur;
@@ -542,8 +548,7 @@ __global__ void __launch_bounds__(32 * kMaxLayers) head_grad_kernel(
         s_s[lane * 4 + 1] = g_shift;
         s_s[lane * 4 + 2] = g_scale;
         s_s[lane * 4 + 3] = act && le_raw == le ? cw * (lam - n) * inv_b : 0.0f;
-        l = warp_sum(l);
-        if (lane == 0 && l != 0.0f) atomicAdd(loss, static_cast<double>(l) / B);
+        l_loss = l;
     }
     __syncthreads();
     // P3
@@ -702,6 +707,11 @@ __global__ void __launch_bounds__(32 * kMaxLayers) head_grad_kernel(
         const uint32_t* src = reinterpret_cast<const uint32_t*>(s_dp + r * lds);
 #pragma unroll 3
         for (int c = lane; c < ldp / 2; c += 32) dst[c] = src[c];
+    }
+    // the batch-mean loss, off the path of the gradient phases
+    if (warp == 0) {
+        const float l = warp_sum(l_loss);
+        if (lane == 0 && l != 0.0f) atomicAdd(loss, static_cast<double>(l) / B);
     }
 }
 
